@@ -1,0 +1,152 @@
+/*
+ * rbx.h -- C ABI of the GB300-native rigid-body integrator (librbx.so).
+ *
+ * The library replaces the compute path of the OpenMM rigid-body plugin's
+ * CudaIntegrateRigidBodyStepKernel (platforms/cuda/src/CudaRigidBodyKernels.cpp) and the
+ * host-side RigidBodySystem (openmmapi/src/RigidBodySystem.cpp) it feeds. Every entry point
+ * takes plain pointers and sizes; device pointers are borrowed from the caller (an OpenMM
+ * CudaContext, or any CUDA allocation with the same layout) and never freed by the library.
+ * All calls return RBX_OK (0) or a non-zero rbx_status; rbx_last_error() gives the message of
+ * the calling thread's last failure.
+ *
+ * Device buffer layout (OpenMM CUDA platform conventions):
+ *   posq            float4 (single, mixed) or double4 (double) per atom slot; .w (charge) kept
+ *   posq_correction float4 per slot, mixed precision only (position = posq + correction)
+ *   velm            float4 (single) or double4 (mixed, double); .w = 1/mass, kept
+ *   force           long long, fixed point with scale 2^32, SoA: x at [slot], y at
+ *                   [slot + stride], z at [slot + 2*stride]; read only
+ * Atom i of the user's System lives in device slot location[i] (identity unless
+ * rbx_set_atom_locations says otherwise, mirroring OpenMM's atom reordering).
+ */
+#ifndef RBX_H
+#define RBX_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rbx_integrator rbx_integrator;
+
+enum rbx_precision { RBX_PRECISION_SINGLE = 0, RBX_PRECISION_MIXED = 1, RBX_PRECISION_DOUBLE = 2 };
+
+enum rbx_status {
+    RBX_OK = 0,
+    RBX_ERR_INVALID_ARGUMENT = 1, /* OpenMMException for misuse in the reference */
+    RBX_ERR_CUDA = 2,             /* a CUDA runtime call failed */
+    RBX_ERR_STATE = 3,            /* call order violated (e.g. step before rbx_upload_state) */
+    RBX_ERR_UNSUPPORTED = 4,      /* feature outside this build (e.g. body larger than a tile) */
+    RBX_ERR_NUMERIC = 5           /* non-finite result detected */
+};
+
+/* Device buffers of one OpenMM-style context (borrowed). */
+typedef struct rbx_buffers {
+    void* posq;
+    void* posq_correction; /* NULL unless mixed precision */
+    void* velm;
+    const long long* force;
+    int stride; /* force SoA stride (OpenMM paddedNumAtoms), >= number of atom slots */
+} rbx_buffers;
+
+/* Message of this thread's last failure ("" if none). */
+const char* rbx_last_error(void);
+/* ABI version of this build (major*10000 + minor*100 + patch). */
+int rbx_version(void);
+
+/*
+ * Create the integrator kernel for a System of num_atoms atoms.
+ * Replaces RigidBodyIntegrator(stepSize, bodyIndices) + setRotationMode
+ * (openmmapi/src/RigidBodyIntegrator.cpp:18-32), RigidBodySystem::initialize
+ * (openmmapi/src/RigidBodySystem.cpp:55-114) and CudaIntegrateRigidBodyStepKernel::initialize
+ * (platforms/cuda/src/CudaRigidBodyKernels.cpp:232-288).
+ *   body_indices  [num_atoms]: 0 (or negative) = free atom; atoms sharing a positive index form
+ *                 one rigid body. An index used by a single atom makes that atom free.
+ *   masses        [num_atoms] in amu; massless atoms may only be free (they are not moved).
+ *   rotation_mode 0 = exact (Jacobi elliptic), n > 0 = NO-SQUISH with n substeps.
+ *   precision     enum rbx_precision; device = CUDA device ordinal.
+ * Errors: RBX_ERR_INVALID_ARGUMENT for a negative mode (RigidBodyIntegrator.cpp:28-29), a bad
+ * count, or a massless body atom.
+ */
+int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, const double* masses,
+               int rotation_mode, int precision, int device);
+int rbx_destroy(rbx_integrator* h);
+
+/* Map user atom i -> device slot location[i] (OpenMM atom reordering; replaces the
+ * ReorderListener's atomLocation rebuild, CudaRigidBodyKernels.cpp:69-113). */
+int rbx_set_atom_locations(rbx_integrator* h, const int* location);
+
+/*
+ * Build the rigid-body state from atom positions and velocities (host arrays, user order,
+ * [num_atoms*3] doubles) and upload it. Replaces RigidBodySystem::update
+ * (RigidBodySystem.cpp:120-142) with RigidBody::buildGeometry/buildDynamics
+ * (openmmapi/src/RigidBody.cpp:65-142) and uploadBodySystem (CudaRigidBodyKernels.cpp:293-372).
+ * Uses a robust eigensolver; body velocities are projected onto rigid motion.
+ */
+int rbx_upload_state(rbx_integrator* h, const double* positions, const double* velocities);
+
+/* Counts: RigidBodySystem::getNumDOF/getNumBodies/getNumFree (RigidBodySystem.h:38-42). */
+int rbx_get_num_dof(const rbx_integrator* h, int* out);
+int rbx_get_num_bodies(const rbx_integrator* h, int* out);
+int rbx_get_num_free(const rbx_integrator* h, int* out);
+int rbx_get_rotation_mode(const rbx_integrator* h, int* out);
+
+/*
+ * One half of a step on OpenMM-layout device buffers, enqueued on `stream` (cudaStream_t,
+ * NULL = default stream). Replaces the integrateRigidBodyPart1 / integrateRigidBodyPart2
+ * kernels and freeAtomsDelta (platforms/cuda/src/kernels/rigidbodyintegrator.cu:270-396)
+ * launched by CudaIntegrateRigidBodyStepKernel::execute (CudaRigidBodyKernels.cpp:377-444).
+ *   part1: half kick by the forces in `force`, drift, free rotation, atom positions.
+ *   part2: half kick by the forces in `force`, atom velocities.
+ *   fused: part2 of step n followed by part1 of step n+1 in one pass; atom velocities of body
+ *          atoms are not written (call part2 to synchronise them).
+ * A full step is part1, force evaluation, part2.
+ */
+int rbx_integrate_part1(rbx_integrator* h, void* stream, const rbx_buffers* buf, double dt);
+int rbx_integrate_part2(rbx_integrator* h, void* stream, const rbx_buffers* buf, double dt);
+int rbx_integrate_fused(rbx_integrator* h, void* stream, const rbx_buffers* buf, double dt);
+
+/*
+ * Translational and rotational kinetic energy [KE_t, KE_r] in kJ/mol, reduced on the device in
+ * FP64 in a fixed order; synchronises `stream`. Replaces the kineticEnergies kernel plus host
+ * summation (rigidbodyintegrator.cu:416-427, CudaRigidBodyKernels.cpp:118-163) and
+ * RigidBodySystem::computeKineticEnergies (RigidBodySystem.cpp:210-220).
+ */
+int rbx_kinetic_energies(rbx_integrator* h, void* stream, const rbx_buffers* buf, double* out2);
+
+/*
+ * Body state exchange for tests and checkpoints, host arrays in the library's body order
+ * (bodies sorted by atom count, ties in order of first appearance):
+ *   state [num_bodies*14]: r[3], v[3], q[4], pi[4] per body (v = centre-of-mass velocity)
+ *   geometry [num_bodies*3] principal moments I (descending; I[2] = 0 for a linear body)
+ * rbx_get_body_atoms gives, for body-atom k in the library order, the user atom index.
+ */
+int rbx_get_body_state(rbx_integrator* h, double* state);
+int rbx_set_body_state(rbx_integrator* h, const double* state);
+int rbx_get_body_geometry(rbx_integrator* h, double* moments, double* body_fixed /* [nba*3] */);
+int rbx_get_body_atoms(rbx_integrator* h, int* first_atom /* [nb+1] */, int* atoms /* [nba] */);
+
+/*
+ * Host-buffer step, the counterpart of the Reference platform's step on host vectors
+ * (RigidBodySystem::integratePart1/integratePart2, RigidBodySystem.cpp:170-204):
+ * copies `forces` ([num_atoms*3] doubles, user order, pinned memory recommended) to the device,
+ * runs `nsteps` steps with that fixed force array (part1, fused x (nsteps-1), part2) on buffers
+ * owned by the integrator, and copies the resulting positions and velocities back into
+ * `positions`/`velocities` ([num_atoms*3]). Synchronous on `stream`.
+ * rbx_context_set_state loads the owned buffers from host positions/velocities and builds the
+ * body state (rbx_upload_state); rbx_context_buffers exposes the owned device buffers.
+ */
+int rbx_context_set_state(rbx_integrator* h, void* stream, const double* positions, const double* velocities);
+int rbx_context_buffers(rbx_integrator* h, rbx_buffers* out);
+int rbx_context_set_forces(rbx_integrator* h, void* stream, const double* forces);
+int rbx_context_get_state(rbx_integrator* h, void* stream, double* positions, double* velocities);
+int rbx_step_host(rbx_integrator* h, void* stream, int nsteps, double dt, const double* forces, double* positions,
+                  double* velocities);
+
+/* Number of kernel launches the last integrate/kinetic/step call enqueued (for accounting). */
+int rbx_last_launch_count(const rbx_integrator* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RBX_H */

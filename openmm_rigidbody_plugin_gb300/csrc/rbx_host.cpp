@@ -1,0 +1,692 @@
+// rbx_host.cpp -- host side of librbx: the C ABI declared in include/rbx.h.
+//
+// Holds the rigid-body system description (the role of RigidBodySystem,
+// openmmapi/src/RigidBodySystem.cpp), builds body geometry and momenta from atom positions and
+// velocities (RigidBody::buildGeometry/buildDynamics, openmmapi/src/RigidBody.cpp:65-142) with a
+// robust eigensolver, plans the tiles of the step kernels and owns every device allocation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/rbx.h"
+#include "rbx_internal.h"
+#include "rbx_math.cuh"
+
+using namespace rbx;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                            \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(RBX_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T> struct DevArray {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DevArray() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count) {
+        release();
+        n = count;
+        if (count == 0) return cudaSuccess;
+        return cudaMalloc((void**)&p, count * sizeof(T));
+    }
+};
+
+}  // namespace
+
+struct rbx_integrator {
+    int natoms = 0, nb = 0, nf = 0, nba = 0, ndof = 0, mode = 0, prec = PREC_MIXED, device = 0;
+    int max_location = 0;  // largest device slot in use; every buffer stride must exceed it
+    int nb_pad = 0, nba_pad = 0, n_body_tiles = 0, n_free_tiles = 0;
+    bool have_state = false;
+    int last_launches = 0;
+    std::vector<double> masses;
+    std::vector<int> location;          // user atom -> device slot
+    std::vector<int> free_atoms;        // user index of each free atom
+    std::vector<int> body_first;        // [nb+1] first body atom (library order)
+    std::vector<int> body_atoms;        // [nba] user index of each body atom
+    std::vector<int> tile_body0;        // [n_body_tiles+1]
+    std::vector<double> I;              // [nb*3] principal moments (host copy)
+    std::vector<double> dfix;           // [nba*3] body-frame positions (host copy)
+    std::vector<uint8_t> cls;           // [nb]
+    std::vector<int> dof;               // [nb]
+
+    DevArray<double> d_state, d_invm, d_invI;
+    DevArray<int> d_atom0, d_atom_loc, d_free_loc, d_tiles;
+    DevArray<uint8_t> d_cls;
+    DevArray<unsigned char> d_fixed;  // float or double SoA
+    DevArray<double> d_ke_partial, d_ke_out;
+    DevArray<unsigned int> d_ke_count;
+    double* h_ke = nullptr;  // pinned [2]
+
+    // owned OpenMM-layout context (host-buffer API)
+    int stride = 0;
+    DevArray<unsigned char> c_posq, c_corr, c_velm;
+    DevArray<long long> c_force;
+    DevArray<double> c_x, c_v, c_f, c_m;
+    DevArray<int> c_loc;
+
+    DevSys sys() const {
+        DevSys s;
+        s.nb = nb; s.nf = nf; s.nba = nba; s.nb_pad = nb_pad; s.nba_pad = nba_pad;
+        s.n_body_tiles = n_body_tiles; s.n_free_tiles = n_free_tiles; s.rot_n = mode;
+        s.state = d_state.p; s.invm = d_invm.p; s.invI = d_invI.p; s.atom0 = d_atom0.p; s.cls = d_cls.p;
+        s.d = d_fixed.p; s.atom_loc = d_atom_loc.p; s.free_loc = d_free_loc.p; s.tile_body0 = d_tiles.p;
+        return s;
+    }
+    ~rbx_integrator() {
+        if (h_ke) cudaFreeHost(h_ke);
+    }
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------------------------
+// Body geometry (robust): principal frame by cyclic Jacobi rotations, sorted descending, as the
+// rows of a proper rotation A (space -> body).
+// ---------------------------------------------------------------------------------------------
+void principal_axes(const double M[9], double w[3], double A[9]) {
+    double a[3][3], v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) a[i][j] = 0.5 * (M[3 * i + j] + M[3 * j + i]);
+    for (int sweep = 0; sweep < 60; sweep++) {
+        double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
+        double diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
+        if (off == 0.0 || off <= 1e-36 * diag) break;
+        for (int p = 0; p < 2; p++)
+            for (int r = p + 1; r < 3; r++) {
+                if (a[p][r] == 0.0) continue;
+                double theta = (a[r][r] - a[p][p]) / (2.0 * a[p][r]);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < 3; k++) {
+                    double akp = a[k][p], akr = a[k][r];
+                    a[k][p] = c * akp - s * akr;
+                    a[k][r] = s * akp + c * akr;
+                }
+                for (int k = 0; k < 3; k++) {
+                    double apk = a[p][k], ark = a[r][k];
+                    a[p][k] = c * apk - s * ark;
+                    a[r][k] = s * apk + c * ark;
+                }
+                for (int k = 0; k < 3; k++) {
+                    double vkp = v[k][p], vkr = v[k][r];
+                    v[k][p] = c * vkp - s * vkr;
+                    v[k][r] = s * vkp + c * vkr;
+                }
+            }
+    }
+    int idx[3] = {0, 1, 2};
+    for (int i = 0; i < 3; i++)
+        for (int j = i + 1; j < 3; j++)
+            if (a[idx[j]][idx[j]] > a[idx[i]][idx[i]]) std::swap(idx[i], idx[j]);
+    for (int i = 0; i < 3; i++) {
+        w[i] = a[idx[i]][idx[i]];
+        for (int k = 0; k < 3; k++) A[3 * i + k] = v[k][idx[i]];
+    }
+    A[6] = A[1] * A[5] - A[2] * A[4];
+    A[7] = A[2] * A[3] - A[0] * A[5];
+    A[8] = A[0] * A[4] - A[1] * A[3];
+}
+
+// Unit quaternion of a proper rotation matrix (Shepperd's method, as in MatVec.cpp:344-373).
+Q4<double> quaternion_of(const double* M) {
+    double t[4] = {1.0 + M[0] + M[4] + M[8], 1.0 + M[0] - M[4] - M[8], 1.0 - M[0] + M[4] - M[8], 1.0 - M[0] - M[4] + M[8]};
+    int k = 0;
+    for (int i = 1; i < 4; i++)
+        if (t[i] > t[k]) k = i;
+    double f = 0.5 / std::sqrt(t[k]);
+    double q[4];
+    switch (k) {
+        case 0: q[1] = (M[5] - M[7]) * f; q[2] = (M[6] - M[2]) * f; q[3] = (M[1] - M[3]) * f; break;
+        case 1: q[0] = (M[5] - M[7]) * f; q[2] = (M[1] + M[3]) * f; q[3] = (M[2] + M[6]) * f; break;
+        case 2: q[0] = (M[6] - M[2]) * f; q[1] = (M[1] + M[3]) * f; q[3] = (M[5] + M[7]) * f; break;
+        default: q[0] = (M[1] - M[3]) * f; q[1] = (M[2] + M[6]) * f; q[2] = (M[5] + M[7]) * f; break;
+    }
+    q[k] = t[k] * f;
+    return q4<double>(q[0], q[1], q[2], q[3]);
+}
+
+uint8_t rotation_class(const double I[3]) {
+    if (I[2] == 0.0) return ROT_SYMMETRIC_AXIS2;  // linear body
+    const double tol = 1e-12 * I[0];
+    bool g01 = I[0] - I[1] <= tol, g12 = I[1] - I[2] <= tol;
+    if (g01 && g12) return ROT_SPHERICAL;
+    if (g01) return ROT_SYMMETRIC_AXIS2;
+    if (g12) return ROT_SYMMETRIC_AXIS0;
+    return ROT_ASYMMETRIC;
+}
+
+struct BodySetup {
+    double mass, invm, I[3], invI[3];
+    int dof;
+    uint8_t cls;
+    V3<double> r, v;
+    Q4<double> q, pi;
+};
+
+// Geometry and momenta of one body from its atoms (RigidBody.cpp:65-142, robust variants:
+// longest displacement as the axis of a linear body, |component| orthonormal vector, Jacobi
+// principal axes, momenta recomputed from scratch on every call).
+void build_body(const int* atoms, int N, const double* masses, const double* R, const double* V, double* dfix,
+                BodySetup& out) {
+    double mass = 0.0;
+    V3<double> rcm = v3(0.0, 0.0, 0.0);
+    for (int j = 0; j < N; j++) {
+        int i = atoms[j];
+        mass += masses[i];
+        rcm = rcm + v3(R[3 * i], R[3 * i + 1], R[3 * i + 2]) * masses[i];
+    }
+    rcm = rcm * (1.0 / mass);
+    std::vector<V3<double>> delta(N);
+    std::vector<double> d2(N);
+    int jmax = 0;
+    for (int j = 0; j < N; j++) {
+        int i = atoms[j];
+        delta[j] = v3(R[3 * i], R[3 * i + 1], R[3 * i + 2]) - rcm;
+        d2[j] = dot(delta[j], delta[j]);
+        if (d2[j] > d2[jmax]) jmax = j;
+    }
+    const double TOL = 1.0e-5;
+    V3<double> u = delta[jmax] * (1.0 / std::sqrt(d2[jmax]));
+    bool linear = d2[jmax] > 0.0;
+    for (int j = 0; linear && j < N; j++) {
+        double udj = dot(u, delta[j]);
+        linear = d2[j] < TOL * d2[jmax] || std::fabs(udj * udj / d2[j] - 1.0) < TOL;
+    }
+    double A[9];
+    if (linear) {
+        double moi = 0.0;
+        for (int j = 0; j < N; j++) moi += masses[atoms[j]] * d2[j];
+        out.I[0] = out.I[1] = moi;
+        out.I[2] = 0.0;
+        double c[3] = {std::fabs(u.x), std::fabs(u.y), std::fabs(u.z)};
+        int imin = c[0] < c[1] ? 0 : 1;
+        if (c[2] < c[imin]) imin = 2;
+        V3<double> e = v3(imin == 0 ? 1.0 : 0.0, imin == 1 ? 1.0 : 0.0, imin == 2 ? 1.0 : 0.0);
+        V3<double> vv = e - u * dot(u, e);
+        vv = vv * (1.0 / std::sqrt(dot(vv, vv)));
+        V3<double> ww = cross(u, vv);
+        double rows[9] = {vv.x, vv.y, vv.z, ww.x, ww.y, ww.z, u.x, u.y, u.z};
+        std::memcpy(A, rows, sizeof rows);
+        out.dof = 5;
+    } else {
+        double M[9] = {0};
+        for (int j = 0; j < N; j++) {
+            double m = masses[atoms[j]];
+            double x[3] = {delta[j].x, delta[j].y, delta[j].z};
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) M[3 * r + c] += ((r == c ? d2[j] : 0.0) - x[r] * x[c]) * m;
+        }
+        principal_axes(M, out.I, A);
+        out.dof = 6;
+    }
+    out.q = quaternion_of(A);
+    for (int j = 0; j < N; j++)
+        for (int r = 0; r < 3; r++) dfix[3 * j + r] = A[3 * r] * delta[j].x + A[3 * r + 1] * delta[j].y + A[3 * r + 2] * delta[j].z;
+    out.mass = mass;
+    out.invm = 1.0 / mass;
+    for (int k = 0; k < 3; k++) out.invI[k] = out.I[k] == 0.0 ? 0.0 : 1.0 / out.I[k];
+    out.cls = rotation_class(out.I);
+    out.r = rcm;
+    V3<double> p = v3(0.0, 0.0, 0.0);
+    for (int j = 0; j < N; j++) {
+        int i = atoms[j];
+        p = p + v3(V[3 * i], V[3 * i + 1], V[3 * i + 2]) * masses[i];
+    }
+    V3<double> vcm = p * (1.0 / mass);
+    V3<double> L = v3(0.0, 0.0, 0.0);
+    for (int j = 0; j < N; j++) {
+        int i = atoms[j];
+        V3<double> dv = v3(V[3 * i], V[3 * i + 1], V[3 * i + 2]) - vcm;
+        V3<double> body = rotate_to_body(out.q, dv) * masses[i];
+        L = L + cross(v3(dfix[3 * j], dfix[3 * j + 1], dfix[3 * j + 2]), body);
+    }
+    out.v = vcm;
+    out.pi = qB(out.q, L * 2.0);
+}
+
+template <class T> int upload(DevArray<T>& a, const std::vector<T>& h) {
+    if (a.alloc(h.size()) != cudaSuccess) return fail(RBX_ERR_CUDA, "cudaMalloc of %zu bytes failed", h.size() * sizeof(T));
+    if (!h.empty()) CUDA_TRY(cudaMemcpy(a.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return RBX_OK;
+}
+
+int upload_maps(rbx_integrator* h) {
+    std::vector<int> atom_loc(h->nba), free_loc(h->nf);
+    for (int k = 0; k < h->nba; k++) atom_loc[k] = h->location[h->body_atoms[k]];
+    for (int j = 0; j < h->nf; j++) free_loc[j] = h->location[h->free_atoms[j]];
+    int rc = upload(h->d_atom_loc, atom_loc);
+    if (rc) return rc;
+    rc = upload(h->d_free_loc, free_loc);
+    if (rc) return rc;
+    return upload(h->c_loc, h->location);
+}
+
+int check(const rbx_integrator* h) {
+    if (!h) return fail(RBX_ERR_INVALID_ARGUMENT, "null integrator handle");
+    return RBX_OK;
+}
+
+int check_ready(const rbx_integrator* h, const rbx_buffers* buf) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body state: call rbx_upload_state first");
+    if (!buf || !buf->posq || !buf->velm || !buf->force) return fail(RBX_ERR_INVALID_ARGUMENT, "null device buffer");
+    if (h->prec == PREC_MIXED && !buf->posq_correction)
+        return fail(RBX_ERR_INVALID_ARGUMENT, "mixed precision needs posq_correction");
+    if (buf->stride < h->natoms) return fail(RBX_ERR_INVALID_ARGUMENT, "stride %d < number of atoms %d", buf->stride, h->natoms);
+    if (h->max_location >= buf->stride)
+        return fail(RBX_ERR_INVALID_ARGUMENT, "device slot %d outside buffers of stride %d", h->max_location, buf->stride);
+    return RBX_OK;
+}
+
+DevBuf devbuf(const rbx_buffers* b) {
+    DevBuf d;
+    d.posq = b->posq; d.corr = b->posq_correction; d.velm = b->velm; d.force = b->force; d.stride = b->stride;
+    return d;
+}
+
+int run_step(rbx_integrator* h, int kind, void* stream, const rbx_buffers* buf, double dt) {
+    int rc = check_ready(h, buf);
+    if (rc) return rc;
+    if (!(dt == dt) || dt == 0.0) return fail(RBX_ERR_INVALID_ARGUMENT, "step size must be finite and non-zero");
+    CUDA_TRY(cudaSetDevice(h->device));
+    int n = launch_step(h->prec, kind, h->sys(), devbuf(buf), dt, stream);
+    if (n < 0) return fail(RBX_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    h->last_launches = n;
+    return RBX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* rbx_last_error(void) { return g_err.c_str(); }
+int rbx_version(void) { return 100; }
+
+int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, const double* masses, int rotation_mode,
+               int precision, int device) {
+    if (!out) return fail(RBX_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    if (num_atoms <= 0 || !body_indices || !masses) return fail(RBX_ERR_INVALID_ARGUMENT, "need num_atoms > 0, body indices and masses");
+    if (rotation_mode < 0) return fail(RBX_ERR_INVALID_ARGUMENT, "Rotation mode cannot be negative");
+    if (precision < PREC_SINGLE || precision > PREC_DOUBLE) return fail(RBX_ERR_INVALID_ARGUMENT, "unknown precision %d", precision);
+    rbx_integrator* h = new (std::nothrow) rbx_integrator();
+    if (!h) return fail(RBX_ERR_INVALID_ARGUMENT, "out of host memory");
+    h->natoms = num_atoms;
+    h->mode = rotation_mode;
+    h->prec = precision;
+    h->device = device;
+    h->masses.assign(masses, masses + num_atoms);
+    h->location.resize(num_atoms);
+    for (int i = 0; i < num_atoms; i++) h->location[i] = i;
+    h->max_location = num_atoms - 1;
+
+    // Compact positive ids in ascending order (cleanBodyIndices, RigidBodySystem.cpp:28-49);
+    // an id used by one atom only makes that atom free.
+    int maxid = 0;
+    for (int i = 0; i < num_atoms; i++) maxid = std::max(maxid, body_indices[i]);
+    std::vector<int> count((size_t)maxid + 1, 0);
+    for (int i = 0; i < num_atoms; i++)
+        if (body_indices[i] > 0) count[body_indices[i]]++;
+    std::vector<int> compact((size_t)maxid + 1, -1);
+    int nb = 0;
+    for (int id = 1; id <= maxid; id++)
+        if (count[id] > 1) compact[id] = nb++;
+    std::vector<std::vector<int>> members(nb);
+    for (int i = 0; i < num_atoms; i++) {
+        int id = body_indices[i];
+        bool in_body = id > 0 && compact[id] >= 0;
+        if (!(masses[i] > 0.0)) {
+            if (in_body) { delete h; return fail(RBX_ERR_INVALID_ARGUMENT, "atom %d of a rigid body has no mass", i); }
+            if (masses[i] < 0.0) { delete h; return fail(RBX_ERR_INVALID_ARGUMENT, "atom %d has negative mass", i); }
+            continue;  // massless free atoms are not integrated
+        }
+        if (in_body) members[compact[id]].push_back(i);
+        else h->free_atoms.push_back(i);
+    }
+    // Library order: bodies by ascending size, ties by compacted id (stable).
+    std::vector<int> order(nb);
+    for (int b = 0; b < nb; b++) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return members[a].size() < members[b].size(); });
+    h->nb = nb;
+    h->nf = (int)h->free_atoms.size();
+    h->body_first.assign(1, 0);
+    for (int b : order) {
+        for (int i : members[b]) h->body_atoms.push_back(i);
+        h->body_first.push_back((int)h->body_atoms.size());
+    }
+    h->nba = (int)h->body_atoms.size();
+    // Tiles of consecutive bodies under the per-CTA body and atom limits.
+    const int TA = tile_atoms(precision);
+    h->tile_body0.assign(1, 0);
+    for (int b = 0; b < nb;) {
+        int atoms = 0, cnt = 0;
+        int n0 = h->body_first[b + 1] - h->body_first[b];
+        if (n0 > TA) {
+            delete h;
+            return fail(RBX_ERR_UNSUPPORTED, "a rigid body of %d atoms exceeds the %d-atom tile of this build", n0, TA);
+        }
+        while (b < nb && cnt < kTileBodies && atoms + (h->body_first[b + 1] - h->body_first[b]) <= TA) {
+            atoms += h->body_first[b + 1] - h->body_first[b];
+            cnt++;
+            b++;
+        }
+        h->tile_body0.push_back(b);
+    }
+    h->n_body_tiles = (int)h->tile_body0.size() - 1;
+    h->n_free_tiles = (h->nf + kFreePerTile - 1) / kFreePerTile;
+    h->nb_pad = ((std::max(nb, 1) + 31) / 32) * 32;
+    h->nba_pad = ((std::max(h->nba, 1) + 31) / 32) * 32;
+    h->I.assign((size_t)nb * 3, 0.0);
+    h->dfix.assign((size_t)h->nba * 3, 0.0);
+    h->cls.assign(nb, 0);
+    h->dof.assign(nb, 6);
+
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete h; return fail(RBX_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); }
+    int rc = upload(h->d_atom0, h->body_first);
+    if (!rc) rc = upload(h->d_tiles, h->tile_body0);
+    if (!rc) rc = upload_maps(h);
+    if (!rc && h->d_state.alloc((size_t)14 * h->nb_pad) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc body state");
+    if (!rc && h->d_invm.alloc(std::max(nb, 1)) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc invm");
+    if (!rc && h->d_invI.alloc((size_t)3 * h->nb_pad) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc invI");
+    if (!rc && h->d_cls.alloc(std::max(nb, 1)) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc cls");
+    const size_t dsz = precision == PREC_DOUBLE ? sizeof(double) : sizeof(float);
+    if (!rc && h->d_fixed.alloc((size_t)3 * h->nba_pad * dsz) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc body-frame positions");
+    if (!rc) {
+        DevSys s = h->sys();
+        int kb = kinetic_blocks(s);
+        if (h->d_ke_partial.alloc((size_t)2 * kb) != cudaSuccess || h->d_ke_out.alloc(2) != cudaSuccess ||
+            h->d_ke_count.alloc(1) != cudaSuccess)
+            rc = fail(RBX_ERR_CUDA, "cudaMalloc kinetic-energy scratch");
+        else if (cudaMemset(h->d_ke_count.p, 0, sizeof(unsigned int)) != cudaSuccess ||
+                 cudaMallocHost((void**)&h->h_ke, 2 * sizeof(double)) != cudaSuccess)
+            rc = fail(RBX_ERR_CUDA, "kinetic-energy scratch initialisation failed");
+    }
+    if (!rc && h->d_state.p) rc = cudaMemset(h->d_state.p, 0, sizeof(double) * 14 * h->nb_pad) == cudaSuccess ? 0 : fail(RBX_ERR_CUDA, "cudaMemset");
+    if (rc) { delete h; return rc; }
+    *out = h;
+    return RBX_OK;
+}
+
+int rbx_destroy(rbx_integrator* h) {
+    if (!h) return RBX_OK;
+    cudaSetDevice(h->device);
+    delete h;
+    return RBX_OK;
+}
+
+int rbx_set_atom_locations(rbx_integrator* h, const int* location) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!location) return fail(RBX_ERR_INVALID_ARGUMENT, "null location array");
+    std::vector<char> seen(h->natoms, 0);
+    for (int i = 0; i < h->natoms; i++) {
+        if (location[i] < 0) return fail(RBX_ERR_INVALID_ARGUMENT, "negative location for atom %d", i);
+        if (location[i] < h->natoms) {
+            if (seen[location[i]]) return fail(RBX_ERR_INVALID_ARGUMENT, "slot %d assigned twice", location[i]);
+            seen[location[i]] = 1;
+        }
+    }
+    h->location.assign(location, location + h->natoms);
+    h->max_location = *std::max_element(h->location.begin(), h->location.end());
+    CUDA_TRY(cudaSetDevice(h->device));
+    return upload_maps(h);
+}
+
+int rbx_upload_state(rbx_integrator* h, const double* positions, const double* velocities) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!positions || !velocities) return fail(RBX_ERR_INVALID_ARGUMENT, "null positions or velocities");
+    const int nb = h->nb, nbp = h->nb_pad;
+    std::vector<double> state((size_t)14 * nbp, 0.0), invm(std::max(nb, 1), 0.0), invI((size_t)3 * nbp, 0.0);
+    h->ndof = h->nf;
+    for (int b = 0; b < nb; b++) {
+        const int f = h->body_first[b], N = h->body_first[b + 1] - f;
+        BodySetup s;
+        build_body(&h->body_atoms[f], N, h->masses.data(), positions, velocities, &h->dfix[3 * (size_t)f], s);
+        for (int k = 0; k < 3; k++) { h->I[3 * b + k] = s.I[k]; invI[b + (size_t)k * nbp] = s.invI[k]; }
+        h->cls[b] = s.cls;
+        h->dof[b] = s.dof;
+        h->ndof += s.dof;
+        invm[b] = s.invm;
+        double row[14] = {s.r.x, s.r.y, s.r.z, s.v.x, s.v.y, s.v.z, s.q.w, s.q.x, s.q.y, s.q.z, s.pi.w, s.pi.x, s.pi.y, s.pi.z};
+        for (int k = 0; k < 14; k++) state[b + (size_t)k * nbp] = row[k];
+        for (int k = 0; k < 14; k++)
+            if (!std::isfinite(row[k])) return fail(RBX_ERR_NUMERIC, "non-finite rigid-body state for body %d", b);
+    }
+    CUDA_TRY(cudaSetDevice(h->device));
+    CUDA_TRY(cudaMemcpy(h->d_state.p, state.data(), state.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(h->d_invm.p, invm.data(), invm.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(h->d_invI.p, invI.data(), invI.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if (nb) CUDA_TRY(cudaMemcpy(h->d_cls.p, h->cls.data(), nb, cudaMemcpyHostToDevice));
+    const int nbap = h->nba_pad;
+    if (h->prec == PREC_DOUBLE) {
+        std::vector<double> d((size_t)3 * nbap, 0.0);
+        for (int k = 0; k < h->nba; k++)
+            for (int c = 0; c < 3; c++) d[k + (size_t)c * nbap] = h->dfix[3 * (size_t)k + c];
+        CUDA_TRY(cudaMemcpy(h->d_fixed.p, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> d((size_t)3 * nbap, 0.0f);
+        for (int k = 0; k < h->nba; k++)
+            for (int c = 0; c < 3; c++) d[k + (size_t)c * nbap] = (float)h->dfix[3 * (size_t)k + c];
+        CUDA_TRY(cudaMemcpy(h->d_fixed.p, d.data(), d.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    h->have_state = true;
+    return RBX_OK;
+}
+
+int rbx_get_num_dof(const rbx_integrator* h, int* out) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->have_state) return fail(RBX_ERR_STATE, "degrees of freedom are known after rbx_upload_state");
+    *out = h->ndof;
+    return RBX_OK;
+}
+int rbx_get_num_bodies(const rbx_integrator* h, int* out) { int rc = check(h); if (!rc) *out = h->nb; return rc; }
+int rbx_get_num_free(const rbx_integrator* h, int* out) { int rc = check(h); if (!rc) *out = h->nf; return rc; }
+int rbx_get_rotation_mode(const rbx_integrator* h, int* out) { int rc = check(h); if (!rc) *out = h->mode; return rc; }
+
+int rbx_integrate_part1(rbx_integrator* h, void* stream, const rbx_buffers* buf, double dt) {
+    return run_step(h, STEP_PART1, stream, buf, dt);
+}
+int rbx_integrate_part2(rbx_integrator* h, void* stream, const rbx_buffers* buf, double dt) {
+    return run_step(h, STEP_PART2, stream, buf, dt);
+}
+int rbx_integrate_fused(rbx_integrator* h, void* stream, const rbx_buffers* buf, double dt) {
+    return run_step(h, STEP_FUSED, stream, buf, dt);
+}
+
+int rbx_kinetic_energies(rbx_integrator* h, void* stream, const rbx_buffers* buf, double* out2) {
+    int rc = check_ready(h, buf);
+    if (rc) return rc;
+    if (!out2) return fail(RBX_ERR_INVALID_ARGUMENT, "null output");
+    CUDA_TRY(cudaSetDevice(h->device));
+    DevSys s = h->sys();
+    KEScratch k{h->d_ke_partial.p, h->d_ke_count.p, h->d_ke_out.p};
+    if (launch_kinetic(h->prec, s, devbuf(buf), k, kinetic_blocks(s), stream) < 0)
+        return fail(RBX_ERR_CUDA, "kinetic-energy launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    CUDA_TRY(cudaMemcpyAsync(h->h_ke, h->d_ke_out.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    out2[0] = h->h_ke[0];
+    out2[1] = h->h_ke[1];
+    h->last_launches = 1;
+    return RBX_OK;
+}
+
+int rbx_get_body_state(rbx_integrator* h, double* state) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body state");
+    std::vector<double> s((size_t)14 * h->nb_pad);
+    CUDA_TRY(cudaSetDevice(h->device));
+    CUDA_TRY(cudaMemcpy(s.data(), h->d_state.p, s.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int b = 0; b < h->nb; b++)
+        for (int k = 0; k < 14; k++) state[14 * (size_t)b + k] = s[b + (size_t)k * h->nb_pad];
+    return RBX_OK;
+}
+
+int rbx_set_body_state(rbx_integrator* h, const double* state) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body geometry: call rbx_upload_state first");
+    std::vector<double> s((size_t)14 * h->nb_pad, 0.0);
+    for (int b = 0; b < h->nb; b++)
+        for (int k = 0; k < 14; k++) s[b + (size_t)k * h->nb_pad] = state[14 * (size_t)b + k];
+    CUDA_TRY(cudaSetDevice(h->device));
+    CUDA_TRY(cudaMemcpy(h->d_state.p, s.data(), s.size() * sizeof(double), cudaMemcpyHostToDevice));
+    return RBX_OK;
+}
+
+int rbx_get_body_geometry(rbx_integrator* h, double* moments, double* body_fixed) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body geometry");
+    if (moments) std::memcpy(moments, h->I.data(), h->I.size() * sizeof(double));
+    if (body_fixed) std::memcpy(body_fixed, h->dfix.data(), h->dfix.size() * sizeof(double));
+    return RBX_OK;
+}
+
+int rbx_get_body_atoms(rbx_integrator* h, int* first_atom, int* atoms) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (first_atom) std::memcpy(first_atom, h->body_first.data(), h->body_first.size() * sizeof(int));
+    if (atoms) std::memcpy(atoms, h->body_atoms.data(), h->body_atoms.size() * sizeof(int));
+    return RBX_OK;
+}
+
+// ----------------------------------------------------------------------------------------------
+// Owned context buffers and the host-buffer step
+// ----------------------------------------------------------------------------------------------
+static int ensure_context(rbx_integrator* h) {
+    if (h->c_posq.p) {
+        if (h->max_location >= h->stride)
+            return fail(RBX_ERR_INVALID_ARGUMENT, "device slot %d outside the owned buffers (stride %d)", h->max_location, h->stride);
+        return RBX_OK;
+    }
+    CUDA_TRY(cudaSetDevice(h->device));
+    h->stride = ((std::max(h->natoms, h->max_location + 1) + 31) / 32) * 32;
+    const size_t p4 = h->prec == PREC_DOUBLE ? 32 : 16, v4 = h->prec == PREC_SINGLE ? 16 : 32;
+    if (h->c_posq.alloc(p4 * h->stride) != cudaSuccess || h->c_velm.alloc(v4 * h->stride) != cudaSuccess ||
+        h->c_force.alloc((size_t)3 * h->stride) != cudaSuccess || h->c_x.alloc((size_t)3 * h->natoms) != cudaSuccess ||
+        h->c_v.alloc((size_t)3 * h->natoms) != cudaSuccess || h->c_f.alloc((size_t)3 * h->natoms) != cudaSuccess ||
+        h->c_m.alloc(h->natoms) != cudaSuccess)
+        return fail(RBX_ERR_CUDA, "cudaMalloc of context buffers failed");
+    if (h->prec == PREC_MIXED && h->c_corr.alloc(16 * (size_t)h->stride) != cudaSuccess)
+        return fail(RBX_ERR_CUDA, "cudaMalloc of position corrections failed");
+    CUDA_TRY(cudaMemset(h->c_posq.p, 0, p4 * h->stride));
+    CUDA_TRY(cudaMemset(h->c_velm.p, 0, v4 * h->stride));
+    CUDA_TRY(cudaMemset(h->c_force.p, 0, sizeof(long long) * 3 * h->stride));
+    if (h->c_corr.p) CUDA_TRY(cudaMemset(h->c_corr.p, 0, 16 * (size_t)h->stride));
+    CUDA_TRY(cudaMemcpy(h->c_m.p, h->masses.data(), sizeof(double) * h->natoms, cudaMemcpyHostToDevice));
+    return RBX_OK;
+}
+
+int rbx_context_buffers(rbx_integrator* h, rbx_buffers* out) {
+    int rc = check(h);
+    if (rc) return rc;
+    if ((rc = ensure_context(h))) return rc;
+    out->posq = h->c_posq.p;
+    out->posq_correction = h->c_corr.p;
+    out->velm = h->c_velm.p;
+    out->force = h->c_force.p;
+    out->stride = h->stride;
+    return RBX_OK;
+}
+
+int rbx_context_set_state(rbx_integrator* h, void* stream, const double* positions, const double* velocities) {
+    int rc = check(h);
+    if (rc) return rc;
+    if ((rc = ensure_context(h))) return rc;
+    if ((rc = rbx_upload_state(h, positions, velocities))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(h->c_x.p, positions, sizeof(double) * 3 * h->natoms, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(h->c_v.p, velocities, sizeof(double) * 3 * h->natoms, cudaMemcpyHostToDevice, st));
+    rbx_buffers b;
+    rbx_context_buffers(h, &b);
+    if (launch_load_positions(h->prec, h->c_x.p, h->c_v.p, h->c_m.p, h->c_loc.p, h->natoms, devbuf(&b), stream) < 0)
+        return fail(RBX_ERR_CUDA, "position upload kernel failed");
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RBX_OK;
+}
+
+int rbx_context_set_forces(rbx_integrator* h, void* stream, const double* forces) {
+    int rc = check(h);
+    if (rc) return rc;
+    if ((rc = ensure_context(h))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(h->c_f.p, forces, sizeof(double) * 3 * h->natoms, cudaMemcpyHostToDevice, st));
+    if (launch_forces_from_host(h->prec, h->c_f.p, h->c_loc.p, h->natoms, h->c_force.p, h->stride, stream) < 0)
+        return fail(RBX_ERR_CUDA, "force conversion kernel failed");
+    return RBX_OK;
+}
+
+int rbx_context_get_state(rbx_integrator* h, void* stream, double* positions, double* velocities) {
+    int rc = check(h);
+    if (rc) return rc;
+    if ((rc = ensure_context(h))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    rbx_buffers b;
+    rbx_context_buffers(h, &b);
+    if (launch_store_positions(h->prec, devbuf(&b), h->c_loc.p, h->natoms, h->c_x.p, velocities ? h->c_v.p : nullptr,
+                               stream) < 0)
+        return fail(RBX_ERR_CUDA, "position download kernel failed");
+    if (positions) CUDA_TRY(cudaMemcpyAsync(positions, h->c_x.p, sizeof(double) * 3 * h->natoms, cudaMemcpyDeviceToHost, st));
+    if (velocities) CUDA_TRY(cudaMemcpyAsync(velocities, h->c_v.p, sizeof(double) * 3 * h->natoms, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RBX_OK;
+}
+
+int rbx_step_host(rbx_integrator* h, void* stream, int nsteps, double dt, const double* forces, double* positions,
+                  double* velocities) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (nsteps < 1) return fail(RBX_ERR_INVALID_ARGUMENT, "nsteps must be >= 1");
+    if (!forces) return fail(RBX_ERR_INVALID_ARGUMENT, "null forces");
+    if ((rc = rbx_context_set_forces(h, stream, forces))) return rc;
+    rbx_buffers b;
+    rbx_context_buffers(h, &b);
+    int launches = 1;
+    if ((rc = rbx_integrate_part1(h, stream, &b, dt))) return rc;
+    for (int n = 1; n < nsteps; n++) {
+        if ((rc = rbx_integrate_fused(h, stream, &b, dt))) return rc;
+        launches++;
+    }
+    if ((rc = rbx_integrate_part2(h, stream, &b, dt))) return rc;
+    launches += 2;  // part2 + force conversion
+    if ((rc = rbx_context_get_state(h, stream, positions, velocities))) return rc;
+    h->last_launches = launches + 1;
+    return RBX_OK;
+}
+
+int rbx_last_launch_count(const rbx_integrator* h) { return h ? h->last_launches : 0; }
+
+}  // extern "C"

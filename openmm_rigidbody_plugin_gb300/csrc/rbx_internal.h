@@ -1,0 +1,71 @@
+// rbx_internal.h -- device-side system description shared by the host code (rbx_host.cpp) and
+// the CUDA kernels (rbx_kernels.cu).
+//
+// HBM layout (one integrator):
+//   body state   double SoA, 14 rows of nb_pad: r.xyz, v.xyz, q.wxyz, pi.wxyz (112 B/body)
+//   invm, invI   double [nb], double SoA 3 x nb_pad                             (32 B/body)
+//   atom0        int [nb+1]: first body atom of each body, bodies sorted by size  (4 B/body)
+//   cls          uint8 [nb]: rotation class (rbx::RotClass)                      (1 B/body)
+//   d            body-frame atom positions, SoA 3 x nba_pad, float (single/mixed) or double
+//   atom_loc     int [nba]: device slot of each body atom (library order)
+//   free_loc     int [nf]:  device slot of each free atom
+//   tile_body0   int [n_body_tiles+1]: bodies of tile t are [tile_body0[t], tile_body0[t+1])
+#pragma once
+
+#include <cstdint>
+
+namespace rbx {
+
+enum Precision : int { PREC_SINGLE = 0, PREC_MIXED = 1, PREC_DOUBLE = 2 };
+enum StepKind : int { STEP_PART1 = 0, STEP_PART2 = 1, STEP_FUSED = 2 };
+
+constexpr int kThreads = 256;       // threads per CTA of the step kernels
+constexpr int kTileBodies = 256;    // max bodies per tile (one body per thread in the body phase)
+constexpr int kTileAtomsF = 1024;   // max body atoms per tile, single/mixed
+constexpr int kTileAtomsD = 512;    // max body atoms per tile, double
+constexpr int kFreePerTile = 256;   // free atoms per free-atom tile
+
+inline int tile_atoms(int prec) { return prec == PREC_DOUBLE ? kTileAtomsD : kTileAtomsF; }
+
+struct DevSys {
+    int nb, nf, nba, nb_pad, nba_pad;
+    int n_body_tiles, n_free_tiles;
+    int rot_n;  // NO-SQUISH substeps; 0 = exact rotation
+    double* state;
+    const double* invm;
+    const double* invI;
+    const int* atom0;
+    const uint8_t* cls;
+    const void* d;
+    const int* atom_loc;
+    const int* free_loc;
+    const int* tile_body0;
+};
+
+struct DevBuf {
+    void* posq;
+    void* corr;
+    void* velm;
+    const long long* force;
+    int stride;
+};
+
+struct KEScratch {
+    double* partial;      // 2 * n_blocks
+    unsigned int* count;  // 1
+    double* out;          // 2
+};
+
+// Launchers (rbx_kernels.cu). Return the number of kernels enqueued, or -1 on a launch error.
+int launch_step(int prec, int kind, const DevSys& s, const DevBuf& b, double dt, void* stream);
+int launch_kinetic(int prec, const DevSys& s, const DevBuf& b, const KEScratch& k, int n_blocks, void* stream);
+int launch_forces_from_host(int prec, const double* f_dev_user, const int* location, int natoms, long long* force,
+                            int stride, void* stream);
+int launch_load_positions(int prec, const double* x_dev_user, const double* v_dev_user, const double* masses,
+                          const int* location, int natoms, const DevBuf& b, void* stream);
+int launch_store_positions(int prec, const DevBuf& b, const int* location, int natoms, double* x_dev_user,
+                           double* v_dev_user, void* stream);
+int kinetic_blocks(const DevSys& s);
+size_t step_smem_bytes(int prec);
+
+}  // namespace rbx

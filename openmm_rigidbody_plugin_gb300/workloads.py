@@ -1,0 +1,215 @@
+"""Seeded synthetic systems of rigid bodies and free atoms (units: nm, ps, amu, kJ/mol).
+
+No public dataset is involved: every workload is generated here from a seed.
+
+* ``water_box`` -- rigid 3-site waters on a cubic lattice at 1 g/cm^3, random orientations,
+  Maxwell-Boltzmann velocities (the 512-water plain-method case).
+* ``mixed_system`` -- the single-large-system case: 70 % waters, 20 % 5-atom tetrahedra
+  (C + 4 H at 0.109 nm, masses 12/1), 10 % 12-atom planar rings (6 C on a 0.14 nm hexagon,
+  6 H radially outside at 0.109 nm, masses 12.011/1.008), plus free LJ atoms (mass 39.95).
+* ``gaussian_forces`` -- seeded per-atom Gaussian forces (sd 500 kJ/mol/nm by default) for
+  integrator-only timing.
+
+Every builder returns a ``System`` with masses, body indices (1-based per molecule, 0 = free
+atom, atoms of a molecule contiguous), positions, velocities and the cubic box edge.
+"""
+from dataclasses import dataclass, field
+
+import numpy as np
+
+KB = 0.00831446261815324  # kJ/mol/K
+AVOGADRO = 6.02214076e23
+
+WATER_OH = 0.09572
+WATER_HOH_DEG = 104.52
+WATER_MASSES = (15.999, 1.008, 1.008)
+WATER_CHARGES = (-0.834, 0.417, 0.417)
+WATER_SIGMA = 0.315061
+WATER_EPSILON = 0.636386
+
+TETRA_ARM = 0.109
+TETRA_MASSES = (12.0, 1.0, 1.0, 1.0, 1.0)
+RING_CC = 0.14
+RING_CH = 0.109
+RING_MASSES = (12.011,) * 6 + (1.008,) * 6
+ARGON_MASS = 39.95
+ARGON_SIGMA = 0.34
+ARGON_EPSILON = 0.996
+
+
+@dataclass
+class System:
+    masses: np.ndarray
+    body_indices: np.ndarray
+    positions: np.ndarray
+    velocities: np.ndarray
+    box: float
+    kinds: dict = field(default_factory=dict)
+
+    @property
+    def num_atoms(self):
+        return len(self.masses)
+
+    @property
+    def num_bodies(self):
+        return int(len(np.unique(self.body_indices[self.body_indices > 0])))
+
+
+def water_template():
+    half = np.deg2rad(WATER_HOH_DEG) / 2
+    return np.array([[0.0, 0.0, 0.0],
+                     [WATER_OH * np.sin(half), WATER_OH * np.cos(half), 0.0],
+                     [-WATER_OH * np.sin(half), WATER_OH * np.cos(half), 0.0]])
+
+
+def tetra_template():
+    dirs = np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]], dtype=np.float64) / np.sqrt(3.0)
+    return np.vstack([np.zeros(3), TETRA_ARM * dirs])
+
+
+def ring_template():
+    ang = np.arange(6) * np.pi / 3
+    c = RING_CC * np.stack([np.cos(ang), np.sin(ang), np.zeros(6)], axis=1)
+    h = (RING_CC + RING_CH) * np.stack([np.cos(ang), np.sin(ang), np.zeros(6)], axis=1)
+    return np.vstack([c, h])
+
+
+def random_rotations(rng, n):
+    """Uniform random rotation matrices from uniform unit quaternions (Shoemake)."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    a, b = np.sqrt(1 - u1), np.sqrt(u1)
+    q = np.stack([a * np.sin(2 * np.pi * u2), a * np.cos(2 * np.pi * u2),
+                  b * np.sin(2 * np.pi * u3), b * np.cos(2 * np.pi * u3)], axis=1)
+    w, x, y, z = q.T
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z); R[:, 0, 1] = 2 * (x * y - z * w); R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w); R[:, 1, 1] = 1 - 2 * (x * x + z * z); R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w); R[:, 2, 1] = 2 * (y * z + x * w); R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def _lattice(n, box, rng=None):
+    k = int(np.ceil(n ** (1.0 / 3.0)))
+    g = (np.arange(k) + 0.5) * (box / k)
+    pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), axis=-1).reshape(-1, 3)[:n]
+    return pts
+
+
+def _mb_velocities(rng, masses, temperature):
+    sd = np.sqrt(KB * temperature / masses)
+    return rng.standard_normal((len(masses), 3)) * sd[:, None]
+
+
+def _box_for_mass(total_amu, density_g_cm3=1.0):
+    grams = total_amu / AVOGADRO
+    cm3 = grams / density_g_cm3
+    return (cm3 * 1e21) ** (1.0 / 3.0)  # 1 cm^3 = 1e21 nm^3
+
+
+def _assemble(templates, masses_of, kinds, n_free, rng, temperature, box=None, free_mass=ARGON_MASS):
+    """Place molecules of the given kinds (in the given order) plus free atoms on a lattice."""
+    nmol = len(kinds)
+    total_mass = sum(sum(masses_of[k]) for k in kinds) + n_free * free_mass
+    if box is None:
+        box = _box_for_mass(total_mass)
+    sites = _lattice(nmol + n_free, box)
+    order = rng.permutation(nmol + n_free)
+    rot = random_rotations(rng, nmol)
+    pos, mass, bidx = [], [], []
+    body = 0
+    kind_count = {}
+    for slot in order:
+        centre = sites[slot]
+        if slot < nmol:
+            k = kinds[slot]
+            t = templates[k]
+            m = np.asarray(masses_of[k])
+            t = t - (m[:, None] * t).sum(0) / m.sum()
+            body += 1
+            pos.append(centre + t @ rot[slot].T)
+            mass.append(m)
+            bidx.append(np.full(len(m), body, dtype=np.int32))
+            kind_count[k] = kind_count.get(k, 0) + 1
+        else:
+            pos.append(centre[None, :])
+            mass.append(np.array([free_mass]))
+            bidx.append(np.zeros(1, dtype=np.int32))
+    masses = np.concatenate(mass)
+    vel = _mb_velocities(rng, masses, temperature)
+    kind_count["free"] = n_free
+    return System(masses, np.concatenate(bidx), np.vstack(pos), vel, box, kind_count)
+
+
+TEMPLATES = {"water": water_template(), "tetra": tetra_template(), "ring": ring_template()}
+MASSES = {"water": WATER_MASSES, "tetra": TETRA_MASSES, "ring": RING_MASSES}
+
+
+def water_box(n_waters=512, seed=1, temperature=300.0, box=None):
+    """Rigid waters on a cubic lattice at 1 g/cm^3 (seeded orientations and velocities)."""
+    rng = np.random.default_rng(seed)
+    kinds = ["water"] * n_waters
+    return _assemble(TEMPLATES, MASSES, kinds, 0, rng, temperature, box)
+
+
+def mixed_system(n_bodies=1_000_000, n_free=100_000, fractions=(0.7, 0.2, 0.1), seed=3,
+                 temperature=300.0):
+    """Waters, tetrahedra and planar rings in the given fractions plus free LJ atoms."""
+    rng = np.random.default_rng(seed)
+    nw = int(round(fractions[0] * n_bodies))
+    nt = int(round(fractions[1] * n_bodies))
+    nr = n_bodies - nw - nt
+    kinds = ["water"] * nw + ["tetra"] * nt + ["ring"] * nr
+    return _assemble_fast(kinds, n_free, rng, temperature)
+
+
+def _assemble_fast(kinds, n_free, rng, temperature, free_mass=ARGON_MASS):
+    """Vectorised version of _assemble for millions of molecules."""
+    names = ["water", "tetra", "ring"]
+    kid = np.array([names.index(k) for k in kinds], dtype=np.int8) if kinds else np.zeros(0, np.int8)
+    nmol = len(kid)
+    sizes = np.array([len(MASSES[n]) for n in names])
+    total_mass = sum(np.sum(MASSES[n]) * np.count_nonzero(kid == i) for i, n in enumerate(names))
+    total_mass += n_free * free_mass
+    box = _box_for_mass(total_mass)
+    sites = _lattice(nmol + n_free, box)
+    order = rng.permutation(nmol + n_free)
+    rot = random_rotations(rng, nmol)
+    # slot -> (kind, n atoms)
+    slot_kind = np.full(nmol + n_free, 3, dtype=np.int8)  # 3 = free atom
+    slot_kind[:nmol] = kid
+    seq_kind = slot_kind[order]
+    seq_n = np.where(seq_kind == 3, 1, sizes[np.minimum(seq_kind, 2)])
+    starts = np.concatenate([[0], np.cumsum(seq_n)[:-1]])
+    natoms = int(seq_n.sum())
+    pos = np.empty((natoms, 3))
+    mass = np.empty(natoms)
+    bidx = np.zeros(natoms, dtype=np.int32)
+    is_mol = seq_kind != 3
+    body_id = np.zeros(len(order), dtype=np.int64)
+    body_id[is_mol] = np.arange(1, int(is_mol.sum()) + 1)
+    free_sel = ~is_mol
+    pos[starts[free_sel]] = sites[order[free_sel]]
+    mass[starts[free_sel]] = free_mass
+    for i, n in enumerate(names):
+        sel = np.nonzero(seq_kind == i)[0]
+        if len(sel) == 0:
+            continue
+        t = TEMPLATES[n]
+        m = np.asarray(MASSES[n])
+        t = t - (m[:, None] * t).sum(0) / m.sum()
+        slots = order[sel]
+        R = rot[slots]  # (k, 3, 3)
+        placed = sites[slots][:, None, :] + np.einsum("aj,kij->kai", t, R)
+        idx = starts[sel][:, None] + np.arange(len(m))[None, :]
+        pos[idx] = placed
+        mass[idx] = m[None, :]
+        bidx[idx] = body_id[sel][:, None]
+    vel = _mb_velocities(rng, mass, temperature)
+    counts = {n: int(np.count_nonzero(kid == i)) for i, n in enumerate(names)}
+    counts["free"] = n_free
+    return System(mass, bidx, pos, vel, box, counts)
+
+
+def gaussian_forces(n_atoms, seed=5, sd=500.0):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((n_atoms, 3)) * sd

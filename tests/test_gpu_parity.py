@@ -1,0 +1,187 @@
+"""CUDA path (through the C ABI) against the reference's golden vectors and the oracle.
+
+Tolerances (normwise relative, max|gpu - ref| / max|ref|), from the target "positions and
+velocities within 1e-6 relative after 100 steps in mixed/FP64":
+  double: positions 1e-9, velocities 1e-8 (FP64 throughout; differences are rounding order)
+  mixed:  positions 1e-6, velocities 1e-6 (FP32 per-atom work, FP64 body state)
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"double": (1e-9, 1e-8, 1e-9), "mixed": (1e-6, 1e-6, 1e-6)}
+
+
+@pytest.fixture(scope="module")
+def rbx():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need CUDA"
+    from openmm_rigidbody_plugin_gb300 import build, kernel
+    build.build_library()
+    return kernel
+
+
+def make(rbx, masses, bidx, R, V, mode, prec, location=None):
+    k = rbx.IntegratorKernel(masses, bidx, rotation_mode=mode, precision=prec)
+    buf = rbx.DeviceBuffers(len(masses), precision=prec)
+    if location is not None:
+        buf.location = np.asarray(location)
+        k.set_atom_locations(location)
+    buf.set_positions(R)
+    buf.set_velocities(V, masses)
+    k.upload_state(R, V)
+    return k, buf
+
+
+@pytest.mark.parametrize("prec", ["double", "mixed"])
+@pytest.mark.parametrize("mode", [0, 1, 10])
+def test_water_fixed_force_vs_reference(rbx, golden, mode, prec):
+    g = golden(f"water64_mode{mode}")
+    k, buf = make(rbx, g["masses"], g["body_indices"], g["R0"], g["V0"], mode, prec)
+    buf.set_forces(g["F"])
+    dt = float(g["dt"])
+    assert k.num_dof == int(g["dof"])
+    for n in range(int(g["nsteps"])):
+        k.part1(buf, dt)
+        k.part2(buf, dt)
+    tp, tv, tk = TOL[prec]
+    assert rel_err(buf.get_positions(), g["R"][-1]) < tp
+    assert rel_err(buf.get_velocities(), g["V"][-1]) < tv
+    np.testing.assert_allclose(k.kinetic_energies(buf), g["ke"][-1], rtol=tk)
+
+
+@pytest.mark.parametrize("prec", ["double", "mixed"])
+@pytest.mark.parametrize("mode", [0, 10])
+def test_fused_steps_equal_split_steps(rbx, golden, mode, prec):
+    """part1, fused x (n-1), part2 == n x (part1, part2) with fixed forces."""
+    g = golden(f"water64_mode{mode}")
+    k, buf = make(rbx, g["masses"], g["body_indices"], g["R0"], g["V0"], mode, prec)
+    buf.set_forces(g["F"])
+    dt, n = float(g["dt"]), int(g["nsteps"])
+    k.part1(buf, dt)
+    for _ in range(n - 1):
+        k.fused(buf, dt)
+    k.part2(buf, dt)
+    tp, tv, tk = TOL[prec]
+    assert rel_err(buf.get_positions(), g["R"][-1]) < tp
+    assert rel_err(buf.get_velocities(), g["V"][-1]) < tv
+    np.testing.assert_allclose(k.kinetic_energies(buf), g["ke"][-1], rtol=tk)
+
+
+@pytest.mark.parametrize("prec", ["double", "mixed"])
+@pytest.mark.parametrize("name", ["water27_tether_mode0", "water27_tether_mode4"])
+def test_position_dependent_forces_vs_reference(rbx, golden, name, prec):
+    g = golden(name)
+    kk, dt, R0 = float(g["k"]), float(g["dt"]), g["R0"]
+    k, buf = make(rbx, g["masses"], g["body_indices"], R0, g["V0"], int(g["mode"]), prec)
+    buf.set_forces(-kk * (R0 - R0))
+    for n in range(int(g["nsteps"])):
+        k.part1(buf, dt)
+        R = buf.get_positions()
+        buf.set_forces(-kk * (R - R0))
+        k.part2(buf, dt)
+        if (n + 1) % 10 == 0:
+            j = (n + 1) // 10 - 1
+            U = 0.5 * kk * np.sum((R - R0) ** 2)
+            np.testing.assert_allclose([U, *k.kinetic_energies(buf)], g["energy"][j], rtol=TOL[prec][2] * 10)
+    assert rel_err(buf.get_positions(), g["R"][-1]) < TOL[prec][0]
+    assert rel_err(buf.get_velocities(), g["V"][-1]) < TOL[prec][1] * 10
+
+
+def test_single_bond_free_atoms(rbx, golden):
+    """Free atoms only (the reference's testSingleBond), mixed precision, against the reference run."""
+    g = golden("single_bond")
+    k, buf = make(rbx, g["masses"], g["body_indices"], g["R0"], g["V0"], 0, "mixed")
+    dt = float(g["dt"])
+
+    def force(x):
+        d = x[1] - x[0]
+        r = np.linalg.norm(d)
+        f = -1.0 * (r - 1.5) * d / r
+        return np.array([-f, f])
+
+    buf.set_forces(force(g["R0"]))
+    for n in range(int(g["nsteps"])):
+        k.part1(buf, dt)
+        buf.set_forces(force(buf.get_positions()))
+        k.part2(buf, dt)
+    np.testing.assert_allclose(buf.get_positions(), g["R"][-1], atol=1e-9)
+    np.testing.assert_allclose(buf.get_velocities(), g["V"][-1], atol=1e-9)
+
+
+def _mixed_case(seed=3):
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    s = W.mixed_system(n_bodies=300, n_free=40, fractions=(0.5, 0.3, 0.2), seed=seed)
+    F = np.round(W.gaussian_forces(s.num_atoms, seed=5) * 2.0 ** 32) / 2.0 ** 32
+    return s, F
+
+
+@pytest.mark.parametrize("prec", ["double", "mixed"])
+@pytest.mark.parametrize("mode", [0, 10])
+def test_mixed_body_types_vs_robust_oracle(rbx, oracle_mod, mode, prec):
+    """Waters, spherical-top tetrahedra and symmetric-top rings (the reference gives NaN or
+    distorted bodies for the last two): parity against the robust FP64 oracle."""
+    s, F = _mixed_case()
+    k, buf = make(rbx, s.masses, s.body_indices, s.positions, s.velocities, mode, prec)
+    buf.set_forces(F)
+    o = oracle_mod.Oracle(s.masses, s.body_indices, mode=mode, robust=True)
+    o.setup(s.positions, s.velocities, F)
+    assert k.num_dof == o.num_dof
+    dt = 0.002
+    for n in range(100):
+        k.part1(buf, dt)
+        k.part2(buf, dt)
+        o.part1(dt, F)
+        o.part2(dt, F)
+    tp, tv, tk = TOL[prec]
+    assert rel_err(buf.get_positions(), o.R) < tp
+    assert rel_err(buf.get_velocities(), o.V) < tv
+    np.testing.assert_allclose(k.kinetic_energies(buf), o.kinetic(), rtol=tk)
+
+
+@pytest.mark.parametrize("prec", ["double", "mixed"])
+def test_atom_reordering_is_transparent(rbx, golden, prec):
+    """Device slots permuted as OpenMM's reordering would: identical user-order results."""
+    g = golden("water64_mode0")
+    perm = np.random.default_rng(7).permutation(len(g["masses"]))
+    k, buf = make(rbx, g["masses"], g["body_indices"], g["R0"], g["V0"], 0, prec, location=perm)
+    buf.set_forces(g["F"])
+    for _ in range(int(g["nsteps"])):
+        k.part1(buf, float(g["dt"]))
+        k.part2(buf, float(g["dt"]))
+    assert rel_err(buf.get_positions(), g["R"][-1]) < TOL[prec][0]
+    assert rel_err(buf.get_velocities(), g["V"][-1]) < TOL[prec][1]
+
+
+@pytest.mark.parametrize("prec", ["single", "mixed", "double"])
+def test_host_buffer_step(rbx, golden, prec):
+    """rbx_step_host (host arrays in, host arrays out) against the reference."""
+    g = golden("water64_mode10")
+    k = rbx.IntegratorKernel(g["masses"], g["body_indices"], rotation_mode=10, precision=prec)
+    k.context_set_state(g["R0"], g["V0"])
+    R = np.zeros_like(g["R0"])
+    V = np.zeros_like(g["V0"])
+    F = np.ascontiguousarray(g["F"])
+    k.step_host(int(g["nsteps"]), float(g["dt"]), F, R, V)
+    tol = {"single": 1e-4, "mixed": 1e-6, "double": 1e-9}[prec]
+    assert rel_err(R, g["R"][-1]) < tol
+    assert rel_err(V, g["V"][-1]) < tol * 10
+    np.testing.assert_allclose(k.context_kinetic_energies(), g["ke"][-1], rtol=tol * 10)
+
+
+def test_determinism(rbx, golden):
+    """Two identical runs give bit-identical results (fixed-order reductions, no atomics)."""
+    g = golden("water64_mode0")
+    outs = []
+    for _ in range(2):
+        k, buf = make(rbx, g["masses"], g["body_indices"], g["R0"], g["V0"], 0, "mixed")
+        buf.set_forces(g["F"])
+        for _ in range(20):
+            k.part1(buf, 0.002)
+            k.part2(buf, 0.002)
+        outs.append((buf.get_positions(), buf.get_velocities(), k.kinetic_energies(buf)))
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)

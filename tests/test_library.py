@@ -1,0 +1,76 @@
+"""librbx.so loads, exports every entry point of include/rbx.h, and validates arguments before
+touching a GPU (runs without one)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from openmm_rigidbody_plugin_gb300 import _lib, build
+    build.build_library()
+    return _lib.load()
+
+
+def header_functions():
+    text = open(os.path.join(ROOT, "include", "rbx.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rbx_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+    names = header_functions()
+    assert "rbx_create" in names and "rbx_integrate_fused" in names
+    assert len(names) >= 20
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [n for n in header_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_header():
+    from openmm_rigidbody_plugin_gb300 import _lib
+    bound = {s[0] for s in _lib.SIGNATURES}
+    assert set(header_functions()) == bound
+
+
+def _create(lib, masses, bidx, mode=0, prec=1):
+    h = ctypes.c_void_p()
+    m = np.ascontiguousarray(masses, dtype=np.float64)
+    b = np.ascontiguousarray(bidx, dtype=np.int32)
+    rc = lib.rbx_create(ctypes.byref(h), len(m), b.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                        m.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), mode, prec, 0)
+    return rc, h
+
+
+def test_negative_rotation_mode_rejected(lib):
+    """RigidBodyIntegrator::setRotationMode throws for mode < 0 (RigidBodyIntegrator.cpp:28-29)."""
+    rc, _ = _create(lib, [1.0, 1.0, 1.0], [1, 1, 1], mode=-1)
+    assert rc == 1
+    assert b"negative" in lib.rbx_last_error()
+
+
+def test_bad_precision_and_sizes_rejected(lib):
+    rc, _ = _create(lib, [1.0, 1.0], [1, 1], prec=7)
+    assert rc == 1
+    h = ctypes.c_void_p()
+    assert lib.rbx_create(ctypes.byref(h), 0, None, None, 0, 1, 0) == 1
+
+
+def test_massless_body_atom_rejected(lib):
+    rc, _ = _create(lib, [1.0, 0.0, 1.0], [1, 1, 1])
+    assert rc == 1
+    assert b"no mass" in lib.rbx_last_error()
+
+
+def test_null_handle_calls_fail_cleanly(lib):
+    out = ctypes.c_int()
+    assert lib.rbx_get_num_bodies(None, ctypes.byref(out)) == 1
+    assert lib.rbx_destroy(None) == 0
+    assert lib.rbx_last_launch_count(None) == 0

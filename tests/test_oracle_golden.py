@@ -1,0 +1,111 @@
+"""The oracle restatement against golden vectors produced by the reference plugin's own CPU code
+(tests/golden/make_golden.py), plus the reference's known-answer test (testSingleBond)."""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+MODES = (0, 1, 10)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_reference_mode_matches_reference_water(oracle_mod, golden, mode):
+    g = golden(f"water64_mode{mode}")
+    o = oracle_mod.Oracle(g["masses"], g["body_indices"], mode=mode, robust=False)
+    o.setup(g["R0"], g["V0"], g["F"])
+    np.testing.assert_allclose(o.kinetic(), g["ke0"], rtol=1e-13)
+    assert o.num_dof == int(g["dof"])
+    for n in range(int(g["nsteps"])):
+        o.part1(float(g["dt"]), g["F"])
+        o.part2(float(g["dt"]), g["F"])
+        if (n + 1) % 10 == 0:
+            k = (n + 1) // 10 - 1
+            assert rel_err(o.R, g["R"][k]) < 1e-13
+            assert rel_err(o.V, g["V"][k]) < 1e-12
+            np.testing.assert_allclose(o.kinetic(), g["ke"][k], rtol=1e-12)
+
+
+@pytest.mark.parametrize("mode", MODES)
+def test_robust_oracle_matches_reference_water(oracle_mod, golden, mode):
+    """Water is an asymmetric top: the robust oracle (Jacobi frame) agrees physically."""
+    g = golden(f"water64_mode{mode}")
+    o = oracle_mod.Oracle(g["masses"], g["body_indices"], mode=mode, robust=True)
+    o.setup(g["R0"], g["V0"], g["F"])
+    for n in range(int(g["nsteps"])):
+        o.part1(float(g["dt"]), g["F"])
+        o.part2(float(g["dt"]), g["F"])
+    assert rel_err(o.R, g["R"][-1]) < 1e-9
+    assert rel_err(o.V, g["V"][-1]) < 1e-8
+    np.testing.assert_allclose(o.kinetic(), g["ke"][-1], rtol=1e-8)
+
+
+@pytest.mark.parametrize("name", ["water27_tether_mode0", "water27_tether_mode4"])
+def test_reference_mode_tether(oracle_mod, golden, name):
+    g = golden(name)
+    k, dt = float(g["k"]), float(g["dt"])
+    R0 = g["R0"]
+
+    def force(R):
+        return np.round(-k * (R - R0) * 2.0 ** 32) / 2.0 ** 32
+
+    o = oracle_mod.Oracle(g["masses"], g["body_indices"], mode=int(g["mode"]), robust=False)
+    o.setup(R0, g["V0"], force(R0))
+    F = force(R0)
+    for n in range(int(g["nsteps"])):
+        o.part1(dt, F)
+        F = force(o.R)
+        o.part2(dt, F)
+        if (n + 1) % 10 == 0:
+            j = (n + 1) // 10 - 1
+            U = 0.5 * k * np.sum((o.R - R0) ** 2)
+            np.testing.assert_allclose([U, *o.kinetic()], g["energy"][j], rtol=1e-11)
+    assert rel_err(o.R, g["R"][-1]) < 1e-12
+
+
+def test_reference_mode_linear_bodies(oracle_mod, golden):
+    g = golden("linear10_mode10")
+    o = oracle_mod.Oracle(g["masses"], g["body_indices"], mode=int(g["mode"]), robust=False)
+    o.setup(g["R0"], g["V0"], g["F"])
+    for n in range(int(g["nsteps"])):
+        o.part1(float(g["dt"]), g["F"])
+        o.part2(float(g["dt"]), g["F"])
+    assert o.num_dof == int(g["dof"]) == 50
+    assert rel_err(o.R, g["R"]) < 1e-13
+    np.testing.assert_allclose(o.kinetic(), g["ke"], rtol=1e-12)
+
+
+def test_single_bond_known_answer(oracle_mod, golden):
+    """tests/TestRigidBodyIntegrator.h:49-83: harmonic oscillator against the analytic solution
+    (positions and velocities within 0.02, energy within 0.01) and against the reference run."""
+    g = golden("single_bond")
+    o = oracle_mod.Oracle(g["masses"], g["body_indices"], mode=0, robust=True)
+
+    def force(x):
+        d = x[1] - x[0]
+        r = np.linalg.norm(d)
+        f = -1.0 * (r - 1.5) * d / r
+        return np.round(np.array([-f, f]) * 2.0 ** 32) / 2.0 ** 32
+
+    F = force(g["R0"])
+    o.setup(g["R0"], g["V0"], F)
+    dt = float(g["dt"])
+    e0 = None
+    for n in range(int(g["nsteps"]) + 1):
+        t = n * dt
+        dist = 1.5 + 0.5 * np.cos(t)
+        np.testing.assert_allclose(o.R[0], [-0.5 * dist, 0, 0], atol=0.02)
+        np.testing.assert_allclose(o.R[1], [0.5 * dist, 0, 0], atol=0.02)
+        speed = -0.5 * np.sin(t)
+        np.testing.assert_allclose(o.V[0], [-0.5 * speed, 0, 0], atol=0.02)
+        np.testing.assert_allclose(o.V[1], [0.5 * speed, 0, 0], atol=0.02)
+        r = np.linalg.norm(o.R[1] - o.R[0])
+        e = 0.5 * (r - 1.5) ** 2 + 0.5 * np.sum(g["masses"][:, None] * o.V ** 2)
+        e0 = e if e0 is None else e0
+        assert abs(e - e0) < 0.01
+        np.testing.assert_allclose(o.R, g["R"][n], rtol=0, atol=1e-12)
+        if n == int(g["nsteps"]):
+            break
+        o.part1(dt, F)
+        F = force(o.R)
+        o.part2(dt, F)
+    assert abs(int(g["nsteps"]) * dt - 10.0) < 1e-12
