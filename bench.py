@@ -1,0 +1,324 @@
+"""Benchmark of the rigid-body integration step (one JSON line on rank 0).
+
+Workload (the single-large-system configuration): 1,000,000 rigid bodies (70 % 3-site waters,
+20 % 5-atom tetrahedra, 10 % 12-atom planar rings) plus 100,000 free LJ atoms, seeded random
+orientations and 300 K velocities, integrator-only with fixed seeded Gaussian forces
+(sd 500 kJ/mol/nm), rotation mode 0 (exact), mixed precision, dt 2 fs. One step is one fused
+kernel pass (second half kick of step n + first half kick, drift, rotation and position rebuild
+of step n+1) over all bodies and free atoms with every input resident in HBM; the working set
+(~0.6 GB) exceeds the 129 MB L2, so no flush is needed between steps.
+
+  value   body-steps/s = bodies x steps / device time (CUDA events on the launching stream,
+          max over ranks)
+  e2e     the same metric through the host-buffer C ABI call (rbx_step_host): per step the
+          forces go host->device from pinned memory and positions and velocities come back
+  roofline  algorithmic bytes of the step kernel / its average launch time vs measured HBM peak
+  cpu_baseline  the CPU port of the reference integrator (oracle) on the machine's host cores
+
+--impl reference times the CPU implementation of the same step (the oracle port of the
+reference's RigidBodySystem::integratePart1/2 with all host threads) on the same workload.
+Multi-GPU (torchrun): every rank integrates its own full-size system (weak scaling, no collective
+on the data path); timings are max-reduced over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s batched/served vs plain at equal energy drift; p50/p99 latency"
+UNIT = "body-steps/s"
+WORKLOAD = ("single large system: 1,000,000 rigid bodies (70% 3-site water, 20% 5-atom tetrahedra, "
+            "10% 12-atom rings) + 100,000 free LJ atoms; integrator-only, fixed seeded Gaussian forces "
+            "sd 500 kJ/mol/nm; dt 2 fs")
+# Algorithmic bytes of one fused step (drop-in OpenMM layout, atom velocities not materialised):
+#   per body   264 B: r, v, q, pi FP64 read + write (224) + invm, invI, first atom, class (40)
+#   per atom    64 B: body-frame d FP32 (12) + slot (4) + fixed-point force (24) + posq.xyz and
+#                     posqCorrection.xyz written (24)
+#   per free   128 B: force (24) + velocity read/write (48) + position and correction read/write
+#                     (48) + 1/m (8)
+BYTES_PER_BODY, BYTES_PER_BODY_ATOM, BYTES_PER_FREE = 264, 64, 128
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="rbx", choices=["rbx", "reference"])
+    p.add_argument("--mode", type=int, default=0, help="rotation mode: 0 exact, n NO-SQUISH substeps")
+    p.add_argument("--precision", default="mixed", choices=["single", "mixed", "double"])
+    p.add_argument("--bodies", type=int, default=1_000_000)
+    p.add_argument("--free", type=int, default=100_000)
+    p.add_argument("--e2e-steps", type=int, default=10)
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def build_workload(args, seed_offset=0):
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    s = W.mixed_system(n_bodies=args.bodies, n_free=args.free, seed=3 + seed_offset)
+    F = W.gaussian_forces(s.num_atoms, seed=5 + seed_offset)
+    return s, F
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(key):
+    """DRAM bytes per launch of the step kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    return d.get(key)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        self.file.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.file.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.file.name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(s, F, args, seconds):
+    """The oracle port of the reference CPU integrator on a bounded sample of the workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    threads = os.cpu_count() or 1
+    frac = 0.05
+    sub = W.mixed_system(n_bodies=int(args.bodies * frac), n_free=int(args.free * frac), seed=3)
+    Fs = W.gaussian_forces(sub.num_atoms, seed=5)
+    o = oracle.Oracle(sub.masses, sub.body_indices, mode=args.mode, robust=True)
+    o.setup(sub.positions, sub.velocities, Fs)
+    o.run_fixed_force(0.002, Fs, 1, threads)
+    t = o.run_fixed_force(0.002, Fs, 1, threads)
+    steps = max(1, min(1000, int(seconds / max(t, 1e-6))))
+    t = o.run_fixed_force(0.002, Fs, steps, threads)
+    nb = o.num_bodies
+    return {"value": nb * steps / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{nb} bodies + {o.num_free} free atoms of the same mix, {steps} steps "
+                      f"(part1+part2, fixed forces), {t:.1f} s, {threads} threads"}
+
+
+def run_reference(args, world, rank):
+    """CPU implementation of the step on the host cores (rank 0 only)."""
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    s, F = build_workload(args)
+    threads = os.cpu_count() or 1
+    o = oracle.Oracle(s.masses, s.body_indices, mode=args.mode, robust=True)
+    o.setup(s.positions, s.velocities, F)
+    for _ in range(args.warmup):
+        o.run_fixed_force(0.002, F, 1, threads)
+    t = o.run_fixed_force(0.002, F, args.steps, threads)
+    nb = o.num_bodies
+    value = nb * args.steps / t
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD + f"; rotation mode {args.mode}", "bodies": nb,
+                      "atoms": int(s.num_atoms), "implementation": "CPU port of RigidBodySystem::integratePart1/2 "
+                      "(robust variant: the reference's own eigen-solver and exact rotation produce NaN for the "
+                      "tetrahedra and rings of this mix)"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                            "sample": f"full workload, {args.steps} steps, {threads} threads"},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_gpu(args, world, rank, local):
+    import torch
+    from openmm_rigidbody_plugin_gb300 import build, kernel
+    torch.cuda.set_device(local)
+    build.build_library()
+    s, F = build_workload(args, seed_offset=0)
+    dt = 0.002
+    k = kernel.IntegratorKernel(s.masses, s.body_indices, rotation_mode=args.mode, precision=args.precision,
+                                device=local)
+    buf = kernel.DeviceBuffers(s.num_atoms, precision=args.precision, device=local)
+    buf.set_positions(s.positions)
+    buf.set_velocities(s.velocities, s.masses)
+    buf.set_forces(F)
+    k.upload_state(s.positions, s.velocities)
+    nb, nf = k.num_bodies, k.num_free
+    nba = int(s.num_atoms) - nf
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+
+    k.part1(buf, dt, stream)
+    for _ in range(args.warmup):
+        k.fused(buf, dt, stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        time.sleep(0.3)
+        torch.cuda.synchronize()
+        start.record(stream)
+        for _ in range(args.steps):
+            k.fused(buf, dt, stream)
+        end.record(stream)
+        torch.cuda.synchronize()
+    launches = args.steps
+    t_dev = start.elapsed_time(end) / 1e3
+    t_dev = max_over_ranks(t_dev, world)
+    k.part2(buf, dt, stream)
+    ke = k.kinetic_energies(buf, stream)
+    if not np.all(np.isfinite(ke)):
+        raise RuntimeError(f"non-finite kinetic energy after the timed steps: {ke}")
+    value = world * nb * args.steps / t_dev
+    bytes_step = BYTES_PER_BODY * nb + BYTES_PER_BODY_ATOM * nba + BYTES_PER_FREE * nf
+    per_launch = t_dev / args.steps
+    peak, peak_kind = peaks()
+    achieved = bytes_step / per_launch / 1e9
+    traffic = ncu_traffic(f"fused_mode{args.mode}_{args.precision}")
+
+    # e2e through the host-buffer C ABI (pinned host arrays, copies inside the timed region)
+    x_h = torch.empty((s.num_atoms, 3), dtype=torch.float64).pin_memory().numpy()
+    v_h = torch.empty((s.num_atoms, 3), dtype=torch.float64).pin_memory().numpy()
+    f_h = torch.from_numpy(np.ascontiguousarray(F)).pin_memory().numpy()
+    ke2 = kernel.IntegratorKernel(s.masses, s.body_indices, rotation_mode=args.mode, precision=args.precision,
+                                  device=local)
+    ke2.context_set_state(s.positions, s.velocities, stream)
+    for _ in range(2):
+        ke2.step_host(1, dt, f_h, x_h, v_h, stream)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        ke2.step_host(1, dt, f_h, x_h, v_h, stream)
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.e2e_steps, world)
+    e2e = {"value": world * nb / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(F.size * 8),
+           "d2h_bytes_per_step": int(2 * s.num_atoms * 3 * 8),
+           "call": "rbx_step_host: forces in, one step (part1 + part2), positions and velocities out"}
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(s, F, args, args.cpu_seconds)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": {"mixed": "f32 atoms + f64 body state", "double": "f64", "single": "f32"}[args.precision],
+           "data": "synthetic",
+           "config": {"workload": WORKLOAD + f"; rotation mode {args.mode}; {args.precision} precision",
+                      "bodies_per_gpu": nb, "body_atoms_per_gpu": nba, "free_atoms_per_gpu": nf,
+                      "l2": "working set > 129 MB L2 (no flush needed)", "parallelism": f"{world} independent replicas"},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes_per_launch": bytes_step,
+                        "kernel": "rbx::step_kernel (fused)"},
+           "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(), "gpu_launches": launches,
+           "kinetic_energy_after": [float(ke[0]), float(ke[1])]}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_gpu(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -34,7 +34,7 @@ def _compile(src, verbose):
         if verbose:
             cmd += ["-Xptxas", "-v"]
     else:
-        cmd += ["-x", "c++"]
+        cmd += ["-x", "c++", "-Xcompiler", "-ffp-contract=off"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"compilation of {src} failed:\n{res.stdout}\n{res.stderr}")

@@ -183,6 +183,48 @@ uint8_t rotation_class(const double I[3]) {
     return ROT_ASYMMETRIC;
 }
 
+// Canonical body frame: each eigenvector row gets its largest-magnitude component positive; a top
+// with two equal moments has its degenerate axes fixed by the first atom off the unique axis; a
+// spherical top uses the space frame. Equivalent frames therefore never depend on rounding.
+void canon_sign(V3<double>& v) {
+    double a[3] = {std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)};
+    double c[3] = {v.x, v.y, v.z};
+    int k = 0;
+    for (int i = 1; i < 3; i++)
+        if (a[i] > a[k]) k = i;
+    if (c[k] < 0) v = v * -1.0;
+}
+
+void canonical_frame(double* A, const double* I, const std::vector<V3<double>>& delta, const std::vector<double>& d2) {
+    const uint8_t cls = rotation_class(I);
+    auto row = [&](int r) { return v3(A[3 * r], A[3 * r + 1], A[3 * r + 2]); };
+    auto set = [&](int r, V3<double> v) { A[3 * r] = v.x; A[3 * r + 1] = v.y; A[3 * r + 2] = v.z; };
+    if (cls == ROT_SPHERICAL) {
+        for (int i = 0; i < 9; i++) A[i] = (i % 4 == 0) ? 1.0 : 0.0;
+        return;
+    }
+    if (cls == ROT_ASYMMETRIC) {
+        V3<double> a = row(0), b = row(1);
+        canon_sign(a);
+        canon_sign(b);
+        set(0, a); set(1, b); set(2, cross(a, b));
+        return;
+    }
+    const int k = cls == ROT_SYMMETRIC_AXIS0 ? 0 : 2;
+    V3<double> u = row(k), e1 = row(k == 0 ? 1 : 0);
+    canon_sign(u);
+    double d2max = 0.0;
+    for (double x : d2) d2max = std::max(d2max, x);
+    for (size_t j = 0; j < delta.size(); j++) {
+        V3<double> p = delta[j] - u * dot(u, delta[j]);
+        double pp = dot(p, p);
+        if (pp > 1e-6 * d2max) { e1 = p * (1.0 / std::sqrt(pp)); break; }
+    }
+    V3<double> e2 = cross(u, e1);
+    if (k == 0) { set(0, u); set(1, e1); set(2, e2); }
+    else { set(0, e1); set(1, e2); set(2, u); }
+}
+
 struct BodySetup {
     double mass, invm, I[3], invI[3];
     int dof;
@@ -215,6 +257,7 @@ void build_body(const int* atoms, int N, const double* masses, const double* R, 
     }
     const double TOL = 1.0e-5;
     V3<double> u = delta[jmax] * (1.0 / std::sqrt(d2[jmax]));
+    canon_sign(u);
     bool linear = d2[jmax] > 0.0;
     for (int j = 0; linear && j < N; j++) {
         double udj = dot(u, delta[j]);
@@ -245,6 +288,7 @@ void build_body(const int* atoms, int N, const double* masses, const double* R, 
                 for (int c = 0; c < 3; c++) M[3 * r + c] += ((r == c ? d2[j] : 0.0) - x[r] * x[c]) * m;
         }
         principal_axes(M, out.I, A);
+        canonical_frame(A, out.I, delta, d2);
         out.dof = 6;
     }
     out.q = quaternion_of(A);

@@ -545,6 +545,59 @@ static void jacobi_eigen(const double* M, double* w, double* V) {
     cross3(V, V + 3, V + 6);
 }
 
+/* Canonical body frame for the robust oracle, so that equivalent frames never depend on
+ * rounding: each eigenvector row gets its largest-magnitude component positive; for a top with
+ * two equal moments (relative gap <= 1e-12) the two degenerate axes are fixed by the first atom
+ * with a displacement off the unique axis; a spherical top takes the space frame. */
+static int rot_class(const double* I) {
+    if (I[2] == 0.0) return 2;
+    double tol = 1e-12 * I[0];
+    int g01 = I[0] - I[1] <= tol, g12 = I[1] - I[2] <= tol;
+    if (g01 && g12) return 3;
+    if (g01) return 2;
+    if (g12) return 1;
+    return 0;
+}
+static void canon_sign(double* v) {
+    int k = 0;
+    for (int i = 1; i < 3; i++) if (fabs(v[i]) > fabs(v[k])) k = i;
+    if (v[k] < 0) { v[0] = -v[0]; v[1] = -v[1]; v[2] = -v[2]; }
+}
+static void canonical_frame(double* A, const double* I, const double* delta, const double* d2, int N) {
+    int cls = rot_class(I);
+    if (cls == 3) {
+        memset(A, 0, 9 * sizeof(double));
+        A[0] = A[4] = A[8] = 1.0;
+        return;
+    }
+    if (cls == 0) {
+        canon_sign(A); canon_sign(A + 3);
+        cross3(A, A + 3, A + 6);
+        return;
+    }
+    int k = cls == 1 ? 0 : 2; /* unique axis */
+    double u[3] = {A[3 * k], A[3 * k + 1], A[3 * k + 2]}, e1[3] = {0, 0, 0}, e2[3];
+    canon_sign(u);
+    double d2max = 0.0;
+    for (int j = 0; j < N; j++) d2max = fmax(d2max, d2[j]);
+    int found = 0;
+    for (int j = 0; j < N && !found; j++) {
+        const double* x = delta + 3 * j;
+        double ux = dot3(u, x);
+        double p[3] = {x[0] - ux * u[0], x[1] - ux * u[1], x[2] - ux * u[2]};
+        double pp = dot3(p, p);
+        if (pp > 1e-6 * d2max) {
+            double s = 1.0 / sqrt(pp);
+            e1[0] = p[0] * s; e1[1] = p[1] * s; e1[2] = p[2] * s;
+            found = 1;
+        }
+    }
+    if (!found) { memcpy(e1, A + 3 * (k == 0 ? 1 : 0), sizeof e1); }
+    cross3(u, e1, e2);
+    if (k == 0) { memcpy(A, u, sizeof u); memcpy(A + 3, e1, sizeof e1); memcpy(A + 6, e2, sizeof e2); }
+    else { memcpy(A, e1, sizeof e1); memcpy(A + 3, e2, sizeof e2); memcpy(A + 6, u, sizeof u); }
+}
+
 void orc_eigen(const double* M, double* w, double* V, int robust) {
     if (robust) { jacobi_eigen(M, w, V); return; }
     smith_eigenvalues(M, w);
@@ -715,6 +768,7 @@ static void build_geometry(orc_system* s, int b, const double* R, const double* 
         I[0] = moi; I[1] = moi; I[2] = 0.0;
         invI[0] = 1.0 / moi; invI[1] = 1.0 / moi; invI[2] = 0.0;
         double v[3], w[3];
+        if (s->robust) canon_sign(u);
         orthonormal(u, v, s->robust);
         cross3(u, v, w);
         if (s->robust) { /* rows v, u x v, u: the molecular axis is body axis 3 */
@@ -732,6 +786,7 @@ static void build_geometry(orc_system* s, int b, const double* R, const double* 
                 for (int c = 0; c < 3; c++) M[3 * r + c] += ((-x[c] * x[r]) + (r == c ? xx : 0.0)) * m;
         }
         orc_eigen(M, I, A, s->robust);
+        if (s->robust) canonical_frame(A, I, delta, d2, N);
         invI[0] = 1.0 / I[0]; invI[1] = 1.0 / I[1]; invI[2] = 1.0 / I[2];
         s->bdof[b] = 6;
     }

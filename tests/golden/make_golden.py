@@ -28,10 +28,11 @@ def quantise(f):
     return np.round(np.asarray(f, dtype=np.float64) * 2.0 ** 32) / 2.0 ** 32
 
 
-def water_fixed_force(mode, nsteps=100, dt=0.002):
-    """64 rigid waters + 8 free argon atoms, fixed seeded Gaussian forces."""
+def water_fixed_force(mode, nsteps=100, dt=0.002, sd=500.0):
+    """64 rigid waters + 8 free argon atoms, fixed seeded Gaussian forces of standard deviation sd
+    (kJ/mol/nm)."""
     s = W.mixed_system(n_bodies=64, n_free=8, fractions=(1.0, 0.0, 0.0), seed=11)
-    F = quantise(W.gaussian_forces(s.num_atoms, seed=5))
+    F = quantise(W.gaussian_forces(s.num_atoms, seed=5, sd=sd))
     r = Reference(s.masses, s.body_indices, mode)
     r.setup(s.positions, s.velocities, F)
     ke0 = r.kinetic()
@@ -123,6 +124,8 @@ def main():
     if not reference_available():
         sys.exit("oracle/_ref/librefrb.so missing: build it with `make -C oracle ref`")
     cases = {f"water64_mode{m}": water_fixed_force(m) for m in (0, 1, 10)}
+    for m in (0, 10):
+        cases[f"water64_sd50_mode{m}"] = water_fixed_force(m, sd=50.0)
     cases["water27_tether_mode0"] = water_tether(0)
     cases["water27_tether_mode4"] = water_tether(4)
     cases["single_bond"] = single_bond()
