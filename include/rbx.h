@@ -143,6 +143,34 @@ int rbx_context_get_state(rbx_integrator* h, void* stream, double* positions, do
 int rbx_step_host(rbx_integrator* h, void* stream, int nsteps, double dt, const double* forces, double* positions,
                   double* velocities);
 
+/*
+ * Allocation-free kinetic energy. This entry point has no counterpart in the reference plugin.
+ *
+ * For callers that cannot call cudaMalloc: a serving process that has reserved its whole
+ * device-memory budget up front and admits work only against that reservation, a host framework
+ * whose own pool owns every device allocation, or a latency-sensitive loop that cannot take the
+ * device synchronisation an allocation may cause. It computes the same [KE_t, KE_r] as
+ * rbx_kinetic_energies, from caller-owned device arrays, and allocates nothing: no cudaMalloc,
+ * no cudaFree, no allocating library call. Its scratch (block partial sums and a ticket counter)
+ * is a fixed static device array of 16 KB + 256 B that every GPU which loads librbx holds until
+ * the process exits.
+ *   body_state   [14 * body_stride] FP64 rows r.xyz, v.xyz, q.wxyz, pi.wxyz (the state layout of
+ *                rbx_get_body_state, transposed to rows of body_stride)
+ *   inv_mass     [num_bodies] 1/m; inv_inertia [3 * body_stride] rows of 1/I (0 for the axis of a
+ *                linear body)
+ *   velm         device velm array (float4 for single, double4 otherwise); free_slots
+ *                [num_free] device slot of each free atom
+ *   out_device   device double[2] receiving [KE_t, KE_r] (kJ/mol); asynchronous on `stream`.
+ * Limit: at most 4,194,304 bodies and 4,194,304 free atoms (1024 block sums of 4096 items);
+ * larger systems get RBX_ERR_UNSUPPORTED. The first call on a device looks up the scratch
+ * address with that device current; make that first call before any stream capture. All calls
+ * share the one scratch array, so calls that overlap on the GPU (concurrent streams, several host
+ * threads) race and must be serialised by the caller.
+ */
+int rbx_kinetic_energies_static(const double* body_state, int num_bodies, int body_stride, const double* inv_mass,
+                                const double* inv_inertia, const void* velm, const int* free_slots, int num_free,
+                                int precision, void* stream, double* out_device);
+
 /* Number of kernel launches the last integrate/kinetic/step call enqueued (for accounting). */
 int rbx_last_launch_count(const rbx_integrator* h);
 

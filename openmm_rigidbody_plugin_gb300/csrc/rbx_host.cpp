@@ -60,6 +60,16 @@ template <class T> struct DevArray {
 
 }  // namespace
 
+int rbx::set_error(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
 struct rbx_integrator {
     int natoms = 0, nb = 0, nf = 0, nba = 0, ndof = 0, mode = 0, prec = PREC_MIXED, device = 0;
     int max_location = 0;  // largest device slot in use; every buffer stride must exceed it

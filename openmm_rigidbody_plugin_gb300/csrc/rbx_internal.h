@@ -68,4 +68,7 @@ int launch_store_positions(int prec, const DevBuf& b, const int* location, int n
 int kinetic_blocks(const DevSys& s);
 size_t step_smem_bytes(int prec);
 
+// Record an error message for rbx_last_error() and return `code` (defined in rbx_host.cpp).
+int set_error(int code, const char* fmt, ...);
+
 }  // namespace rbx

@@ -17,6 +17,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
+#include <mutex>
+
+#include "../../include/rbx.h"
 
 #include "rbx_internal.h"
 #include "rbx_math.cuh"
@@ -492,4 +495,141 @@ int launch_store_positions(int prec, const DevBuf& b, const int* location, int n
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
+// ------------------------------------------------------------------------------------------
+// Kinetic energy without device allocation (rbx_kinetic_energies_static).
+//
+// Some callers cannot call cudaMalloc: a serving process that has reserved its whole
+// device-memory budget up front and admits work only against that reservation, a host
+// framework that owns every device allocation through its own pool, or a latency-sensitive
+// loop that cannot afford the device synchronisation an allocation may cause. For them the
+// reduction's scratch (one pair of partial sums per block and the block ticket counter) lives
+// in a fixed static device array of this file instead of memory owned by an integrator handle.
+// ------------------------------------------------------------------------------------------
+constexpr int kStaticKEMaxBlocks = 1024;
+constexpr int kStaticKEItemsPerBlock = kKEThreads * 16;  // bodies (and free atoms) per block
+constexpr long long kStaticKEMaxItems = (long long)kStaticKEMaxBlocks * kStaticKEItemsPerBlock;  // 4,194,304
+constexpr int kMaxDevices = 64;
+// [0, 2*kStaticKEMaxBlocks): per-block partial sums; then one unsigned ticket counter.
+// 16 KB + 256 B, resident on every device that loads the library until the process exits.
+static __device__ __align__(256) double g_static_ke_scratch[2 * kStaticKEMaxBlocks + 32];
+
+template <int P>
+__global__ void __launch_bounds__(kKEThreads) kinetic_static_kernel(DevSys S, DevBuf B, double* scratch, double* out) {
+    using V4 = typename Tr<P>::V4;
+    __shared__ double s_t[kKEThreads], s_r[kKEThreads];
+    __shared__ bool s_last;
+    double* partial = scratch;
+    unsigned int* count = (unsigned int*)(scratch + 2 * kStaticKEMaxBlocks);
+    const int nbp = S.nb_pad;
+    const double* st = S.state;
+    const int first = blockIdx.x * kStaticKEItemsPerBlock;
+    const int last = first + kStaticKEItemsPerBlock;
+    double kt = 0.0, kr = 0.0;
+    for (int b = first + (int)threadIdx.x; b < last && b < S.nb; b += kKEThreads) {
+        V3<double> v = v3<double>(st[b + 3 * nbp], st[b + 4 * nbp], st[b + 5 * nbp]);
+        Q4<double> q = q4<double>(st[b + 6 * nbp], st[b + 7 * nbp], st[b + 8 * nbp], st[b + 9 * nbp]);
+        Q4<double> pi = q4<double>(st[b + 10 * nbp], st[b + 11 * nbp], st[b + 12 * nbp], st[b + 13 * nbp]);
+        V3<double> invI = v3<double>(S.invI[b], S.invI[b + nbp], S.invI[b + 2 * nbp]);
+        V3<double> L = qBt(q, pi) * 0.5;
+        kt += dot(v, v) / S.invm[b];
+        kr += dot(L, mul(invI, L));
+    }
+    const V4* vel = (const V4*)B.velm;
+    for (int j = first + (int)threadIdx.x; j < last && j < S.nf; j += kKEThreads) {
+        V4 vm = vel[S.free_loc[j]];
+        double vx = vm.x, vy = vm.y, vz = vm.z;
+        kt += (vx * vx + vy * vy + vz * vz) / (double)vm.w;
+    }
+    s_t[threadIdx.x] = kt;
+    s_r[threadIdx.x] = kr;
+    __syncthreads();
+    for (int w = kKEThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            s_t[threadIdx.x] += s_t[threadIdx.x + w];
+            s_r[threadIdx.x] += s_r[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = s_t[0];
+        partial[2 * blockIdx.x + 1] = s_r[0];
+        __threadfence();
+        unsigned int ticket = atomicAdd(count, 1u);
+        s_last = ticket == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x == 0) {
+        __threadfence();
+        double t = 0.0, r = 0.0;
+        for (unsigned int i = 0; i < gridDim.x; i++) {
+            t += ((volatile double*)partial)[2 * i];
+            r += ((volatile double*)partial)[2 * i + 1];
+        }
+        out[0] = 0.5 * t;
+        out[1] = 0.5 * r;
+        *count = 0u;
+    }
+}
+
+// Device address of the static scratch, looked up once per device (with that device current).
+static int static_scratch_address(double** out) {
+    static std::mutex mu;
+    static void* addr[kMaxDevices] = {};
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(RBX_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return set_error(RBX_ERR_UNSUPPORTED, "device %d beyond %d", dev, kMaxDevices);
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_static_ke_scratch);
+        if (e != cudaSuccess)
+            return set_error(RBX_ERR_CUDA, "cudaGetSymbolAddress of the static scratch: %s", cudaGetErrorString(e));
+        addr[dev] = p;
+    }
+    *out = (double*)addr[dev];
+    return RBX_OK;
+}
+
 }  // namespace rbx
+
+extern "C" int rbx_kinetic_energies_static(const double* body_state, int num_bodies, int body_stride,
+                                           const double* inv_mass, const double* inv_inertia, const void* velm,
+                                           const int* free_slots, int num_free, int precision, void* stream,
+                                           double* out_device) {
+    using namespace rbx;
+    if (num_bodies < 0 || num_free < 0) return set_error(RBX_ERR_INVALID_ARGUMENT, "negative counts");
+    if ((long long)num_bodies > kStaticKEMaxItems || (long long)num_free > kStaticKEMaxItems)
+        return set_error(RBX_ERR_UNSUPPORTED,
+                         "rbx_kinetic_energies_static handles at most %lld bodies and %lld free atoms "
+                         "(its fixed scratch holds %d block sums); got %d bodies, %d free atoms",
+                         kStaticKEMaxItems, kStaticKEMaxItems, kStaticKEMaxBlocks, num_bodies, num_free);
+    if (num_bodies > 0 && (!body_state || !inv_mass || !inv_inertia || body_stride < num_bodies))
+        return set_error(RBX_ERR_INVALID_ARGUMENT, "body arrays missing or body_stride < num_bodies");
+    if (num_free > 0 && (!velm || !free_slots)) return set_error(RBX_ERR_INVALID_ARGUMENT, "free-atom arrays missing");
+    if (!out_device) return set_error(RBX_ERR_INVALID_ARGUMENT, "null output");
+    if (precision < PREC_SINGLE || precision > PREC_DOUBLE) return set_error(RBX_ERR_INVALID_ARGUMENT, "unknown precision");
+    double* scratch = nullptr;
+    int rc = static_scratch_address(&scratch);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    // The array keeps the previous call's contents: the ticket counter must start at zero.
+    cudaError_t e = cudaMemsetAsync(scratch + 2 * kStaticKEMaxBlocks, 0, sizeof(unsigned int), st);
+    if (e != cudaSuccess) return set_error(RBX_ERR_CUDA, "clearing the static scratch: %s", cudaGetErrorString(e));
+    DevSys s{};
+    s.nb = num_bodies; s.nf = num_free; s.nb_pad = body_stride;
+    s.state = const_cast<double*>(body_state); s.invm = inv_mass; s.invI = inv_inertia; s.free_loc = free_slots;
+    DevBuf b{};
+    b.velm = const_cast<void*>(velm);
+    long long items = num_bodies > num_free ? num_bodies : num_free;
+    int grid = (int)((items + kStaticKEItemsPerBlock - 1) / kStaticKEItemsPerBlock);
+    if (grid < 1) grid = 1;
+    switch (precision) {
+        case PREC_SINGLE: kinetic_static_kernel<PREC_SINGLE><<<grid, kKEThreads, 0, st>>>(s, b, scratch, out_device); break;
+        case PREC_MIXED: kinetic_static_kernel<PREC_MIXED><<<grid, kKEThreads, 0, st>>>(s, b, scratch, out_device); break;
+        default: kinetic_static_kernel<PREC_DOUBLE><<<grid, kKEThreads, 0, st>>>(s, b, scratch, out_device); break;
+    }
+    e = cudaPeekAtLastError();
+    if (e != cudaSuccess) return set_error(RBX_ERR_CUDA, "kinetic-energy launch: %s", cudaGetErrorString(e));
+    return RBX_OK;
+}
