@@ -39,12 +39,17 @@ WORKLOAD = ("single large system: 1,000,000 rigid bodies (70% 3-site water, 20% 
             "10% 12-atom rings) + 100,000 free LJ atoms; integrator-only, fixed seeded Gaussian forces "
             "sd 500 kJ/mol/nm; dt 2 fs")
 # Algorithmic bytes of one fused step (drop-in OpenMM layout, atom velocities not materialised):
-#   per body   264 B: r, v, q, pi FP64 read + write (224) + invm, invI, first atom, class (40)
+#   per body   273 B (single/mixed): r, v, q, pi float-float read + write (224) + 1/m and 1/I as
+#                     float-float, three moment gaps (44) + first atom (4) + rotation class (1)
+#              261 B (double): FP64 state (224) + 1/m, 1/I (32) + first atom (4) + class (1)
 #   per atom    64 B: body-frame d FP32 (12) + slot (4) + fixed-point force (24) + posq.xyz and
-#                     posqCorrection.xyz written (24)
+#                     posqCorrection.xyz written (24); double: d FP64 (24) + slot + force + posq.xyz
+#                     FP64 written (24) = 76 B
 #   per free   128 B: force (24) + velocity read/write (48) + position and correction read/write
 #                     (48) + 1/m (8)
-BYTES_PER_BODY, BYTES_PER_BODY_ATOM, BYTES_PER_FREE = 264, 64, 128
+BYTES_PER_BODY = {"single": 273, "mixed": 273, "double": 261}
+BYTES_PER_BODY_ATOM = {"single": 64, "mixed": 64, "double": 76}
+BYTES_PER_FREE = 128
 
 
 def parse():
@@ -262,7 +267,7 @@ def run_gpu(args, world, rank, local):
     if not np.all(np.isfinite(ke)):
         raise RuntimeError(f"non-finite kinetic energy after the timed steps: {ke}")
     value = world * nb * args.steps / t_dev
-    bytes_step = BYTES_PER_BODY * nb + BYTES_PER_BODY_ATOM * nba + BYTES_PER_FREE * nf
+    bytes_step = BYTES_PER_BODY[args.precision] * nb + BYTES_PER_BODY_ATOM[args.precision] * nba + BYTES_PER_FREE * nf
     per_launch = t_dev / args.steps
     peak, peak_kind = peaks()
     achieved = bytes_step / per_launch / 1e9

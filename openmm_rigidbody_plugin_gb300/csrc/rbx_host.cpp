@@ -87,7 +87,8 @@ struct rbx_integrator {
     std::vector<uint8_t> cls;           // [nb]
     std::vector<int> dof;               // [nb]
 
-    DevArray<double> d_state, d_invm, d_invI;
+    DevArray<double> d_state, d_invm, d_invI;  // d_state holds FP64 rows or float-float rows
+    DevArray<float> d_bconst;                   // single/mixed: 11 rows (see kBconstRows)
     DevArray<int> d_atom0, d_atom_loc, d_free_loc, d_tiles;
     DevArray<uint8_t> d_cls;
     DevArray<unsigned char> d_fixed;  // float or double SoA
@@ -106,7 +107,8 @@ struct rbx_integrator {
         DevSys s;
         s.nb = nb; s.nf = nf; s.nba = nba; s.nb_pad = nb_pad; s.nba_pad = nba_pad;
         s.n_body_tiles = n_body_tiles; s.n_free_tiles = n_free_tiles; s.rot_n = mode;
-        s.state = d_state.p; s.invm = d_invm.p; s.invI = d_invI.p; s.atom0 = d_atom0.p; s.cls = d_cls.p;
+        s.state = d_state.p; s.invm = d_invm.p; s.invI = d_invI.p; s.bconst = d_bconst.p;
+        s.atom0 = d_atom0.p; s.cls = d_cls.p;
         s.d = d_fixed.p; s.atom_loc = d_atom_loc.p; s.free_loc = d_free_loc.p; s.tile_body0 = d_tiles.p;
         return s;
     }
@@ -470,8 +472,12 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
     if (!rc) rc = upload(h->d_tiles, h->tile_body0);
     if (!rc) rc = upload_maps(h);
     if (!rc && h->d_state.alloc((size_t)14 * h->nb_pad) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc body state");
-    if (!rc && h->d_invm.alloc(std::max(nb, 1)) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc invm");
-    if (!rc && h->d_invI.alloc((size_t)3 * h->nb_pad) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc invI");
+    if (precision == PREC_DOUBLE) {
+        if (!rc && h->d_invm.alloc(std::max(nb, 1)) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc invm");
+        if (!rc && h->d_invI.alloc((size_t)3 * h->nb_pad) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc invI");
+    } else if (!rc && h->d_bconst.alloc((size_t)kBconstRows * h->nb_pad) != cudaSuccess) {
+        rc = fail(RBX_ERR_CUDA, "cudaMalloc body constants");
+    }
     if (!rc && h->d_cls.alloc(std::max(nb, 1)) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc cls");
     const size_t dsz = precision == PREC_DOUBLE ? sizeof(double) : sizeof(float);
     if (!rc && h->d_fixed.alloc((size_t)3 * h->nba_pad * dsz) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc body-frame positions");
@@ -516,12 +522,44 @@ int rbx_set_atom_locations(rbx_integrator* h, const int* location) {
     return upload_maps(h);
 }
 
+// Body state rows (14 per body, library order) -> device layout of the integrator's precision:
+// FP64 rows for double, float-float rows (14 hi rows then 14 lo rows) for single and mixed.
+static int put_state(rbx_integrator* h, const std::vector<double>& rows /* 14 x nb_pad */) {
+    const size_t n = rows.size();
+    if (h->prec == PREC_DOUBLE) {
+        CUDA_TRY(cudaMemcpy(h->d_state.p, rows.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        return RBX_OK;
+    }
+    std::vector<float> f(2 * n);
+    for (size_t i = 0; i < n; i++) {
+        float hi = (float)rows[i];
+        f[i] = hi;
+        f[n + i] = (float)(rows[i] - (double)hi);
+    }
+    CUDA_TRY(cudaMemcpy(h->d_state.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return RBX_OK;
+}
+
+static int get_state(rbx_integrator* h, std::vector<double>& rows) {
+    const size_t n = (size_t)14 * h->nb_pad;
+    rows.assign(n, 0.0);
+    if (h->prec == PREC_DOUBLE) {
+        CUDA_TRY(cudaMemcpy(rows.data(), h->d_state.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+        return RBX_OK;
+    }
+    std::vector<float> f(2 * n);
+    CUDA_TRY(cudaMemcpy(f.data(), h->d_state.p, f.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; i++) rows[i] = (double)f[i] + (double)f[n + i];
+    return RBX_OK;
+}
+
 int rbx_upload_state(rbx_integrator* h, const double* positions, const double* velocities) {
     int rc = check(h);
     if (rc) return rc;
     if (!positions || !velocities) return fail(RBX_ERR_INVALID_ARGUMENT, "null positions or velocities");
     const int nb = h->nb, nbp = h->nb_pad;
     std::vector<double> state((size_t)14 * nbp, 0.0), invm(std::max(nb, 1), 0.0), invI((size_t)3 * nbp, 0.0);
+    std::vector<float> bconst((size_t)kBconstRows * nbp, 0.0f);
     h->ndof = h->nf;
     for (int b = 0; b < nb; b++) {
         const int f = h->body_first[b], N = h->body_first[b + 1] - f;
@@ -532,15 +570,25 @@ int rbx_upload_state(rbx_integrator* h, const double* positions, const double* v
         h->dof[b] = s.dof;
         h->ndof += s.dof;
         invm[b] = s.invm;
+        // FP32 constants: 1/m and 1/I as float-float (rows 0-3 hi, 7-10 lo); the moment gaps are
+        // formed in FP64 so that they keep their relative accuracy for nearly degenerate tops.
+        const double gaps[3] = {s.I[0] - s.I[1], s.I[1] - s.I[2], s.I[0] - s.I[2]};
+        const double cst[7] = {s.invm, s.invI[0], s.invI[1], s.invI[2], gaps[0], gaps[1], gaps[2]};
+        for (int k = 0; k < 7; k++) bconst[b + (size_t)k * nbp] = (float)cst[k];
+        for (int k = 0; k < 4; k++) bconst[b + (size_t)(7 + k) * nbp] = (float)(cst[k] - (double)(float)cst[k]);
         double row[14] = {s.r.x, s.r.y, s.r.z, s.v.x, s.v.y, s.v.z, s.q.w, s.q.x, s.q.y, s.q.z, s.pi.w, s.pi.x, s.pi.y, s.pi.z};
         for (int k = 0; k < 14; k++) state[b + (size_t)k * nbp] = row[k];
         for (int k = 0; k < 14; k++)
             if (!std::isfinite(row[k])) return fail(RBX_ERR_NUMERIC, "non-finite rigid-body state for body %d", b);
     }
     CUDA_TRY(cudaSetDevice(h->device));
-    CUDA_TRY(cudaMemcpy(h->d_state.p, state.data(), state.size() * sizeof(double), cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(h->d_invm.p, invm.data(), invm.size() * sizeof(double), cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(h->d_invI.p, invI.data(), invI.size() * sizeof(double), cudaMemcpyHostToDevice));
+    if ((rc = put_state(h, state))) return rc;
+    if (h->prec == PREC_DOUBLE) {
+        CUDA_TRY(cudaMemcpy(h->d_invm.p, invm.data(), invm.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(h->d_invI.p, invI.data(), invI.size() * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        CUDA_TRY(cudaMemcpy(h->d_bconst.p, bconst.data(), bconst.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
     if (nb) CUDA_TRY(cudaMemcpy(h->d_cls.p, h->cls.data(), nb, cudaMemcpyHostToDevice));
     const int nbap = h->nba_pad;
     if (h->prec == PREC_DOUBLE) {
@@ -600,9 +648,9 @@ int rbx_get_body_state(rbx_integrator* h, double* state) {
     int rc = check(h);
     if (rc) return rc;
     if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body state");
-    std::vector<double> s((size_t)14 * h->nb_pad);
+    std::vector<double> s;
     CUDA_TRY(cudaSetDevice(h->device));
-    CUDA_TRY(cudaMemcpy(s.data(), h->d_state.p, s.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    if ((rc = get_state(h, s))) return rc;
     for (int b = 0; b < h->nb; b++)
         for (int k = 0; k < 14; k++) state[14 * (size_t)b + k] = s[b + (size_t)k * h->nb_pad];
     return RBX_OK;
@@ -616,8 +664,7 @@ int rbx_set_body_state(rbx_integrator* h, const double* state) {
     for (int b = 0; b < h->nb; b++)
         for (int k = 0; k < 14; k++) s[b + (size_t)k * h->nb_pad] = state[14 * (size_t)b + k];
     CUDA_TRY(cudaSetDevice(h->device));
-    CUDA_TRY(cudaMemcpy(h->d_state.p, s.data(), s.size() * sizeof(double), cudaMemcpyHostToDevice));
-    return RBX_OK;
+    return put_state(h, s);
 }
 
 int rbx_get_body_geometry(rbx_integrator* h, double* moments, double* body_fixed) {

@@ -2,8 +2,12 @@
 // the CUDA kernels (rbx_kernels.cu).
 //
 // HBM layout (one integrator):
-//   body state   double SoA, 14 rows of nb_pad: r.xyz, v.xyz, q.wxyz, pi.wxyz (112 B/body)
-//   invm, invI   double [nb], double SoA 3 x nb_pad                             (32 B/body)
+//   body state   14 components r.xyz, v.xyz, q.wxyz, pi.wxyz per body (112 B/body):
+//                  double precision: FP64 SoA, 14 rows of nb_pad
+//                  single/mixed:     float-float SoA, 14 rows of hi parts then 14 rows of lo
+//   constants    double: invm [nb] + invI FP64 SoA 3 x nb_pad                   (32 B/body)
+//                single/mixed: FP32 SoA 11 x nb_pad: invm, invI.xyz, I0-I1, I1-I2, I0-I2, then
+//                the low parts of invm and invI.xyz (float-float)                  (44 B/body)
 //   atom0        int [nb+1]: first body atom of each body, bodies sorted by size  (4 B/body)
 //   cls          uint8 [nb]: rotation class (rbx::RotClass)                      (1 B/body)
 //   d            body-frame atom positions, SoA 3 x nba_pad, float (single/mixed) or double
@@ -24,6 +28,7 @@ constexpr int kTileBodies = 256;    // max bodies per tile (one body per thread 
 constexpr int kTileAtomsF = 1024;   // max body atoms per tile, single/mixed
 constexpr int kTileAtomsD = 512;    // max body atoms per tile, double
 constexpr int kFreePerTile = 256;   // free atoms per free-atom tile
+constexpr int kBconstRows = 11;     // rows of the FP32 body-constant table (single/mixed)
 
 inline int tile_atoms(int prec) { return prec == PREC_DOUBLE ? kTileAtomsD : kTileAtomsF; }
 
@@ -31,9 +36,10 @@ struct DevSys {
     int nb, nf, nba, nb_pad, nba_pad;
     int n_body_tiles, n_free_tiles;
     int rot_n;  // NO-SQUISH substeps; 0 = exact rotation
-    double* state;
-    const double* invm;
-    const double* invI;
+    void* state;           // double* (double precision) or float* (float-float, single/mixed)
+    const double* invm;    // double precision only
+    const double* invI;    // double precision only
+    const float* bconst;   // single/mixed only: kBconstRows rows of nb_pad
     const int* atom0;
     const uint8_t* cls;
     const void* d;

@@ -1,18 +1,22 @@
 // rbx_kernels.cu -- sm_103a kernels of the rigid-body integrator.
 //
-// One step kernel serves the three step kinds (part1, part2, fused part2+part1) of the plugin's
+// The step kernels serve the three step kinds (part1, part2, fused part2+part1) of the plugin's
 // integrateRigidBodyPart1/Part2 and freeAtomsDelta (platforms/cuda/src/kernels/
 // rigidbodyintegrator.cu:270-396). A CTA owns one tile: a run of bodies whose atoms are
 // contiguous in the library's body-atom order (bodies sorted by size so that a tile holds bodies
 // of one kind). Four phases, separated by __syncthreads:
-//   0. one thread per body stages its orientation and marks its atoms in shared memory;
+//   0. one thread per body loads its state and stages its orientation, and marks its atoms
+//      with the tile-local body index in shared memory;
 //   1. one thread per atom gathers the fixed-point force, rebuilds the COM displacement
 //      delta = At(q) d and its torque delta x F, and parks F and tau in shared memory;
-//   2. one thread per body sums its atoms' F and tau in a fixed order (deterministic), applies
-//      the half kick(s), drift and free rotation (NO-SQUISH or exact) on the FP64 state;
+//   2. one thread per body sums its atoms' F and tau in a fixed order (deterministic, no
+//      atomics), applies the half kick(s), drift and free rotation, and writes its state;
 //   3. one thread per atom writes the new position r + At(q) d (or, for part2, the velocity
 //      v + omega x delta) to its device slot.
 // Free atoms live in separate tiles of the same launch (velocity Verlet).
+// step_kernel_d runs double precision in FP64 throughout (the reference formulas, the parity
+// anchor). step_kernel_f runs single and mixed precision on the FP32 pipe: float-float body
+// state, FP32 rotation increments (rbx_fast.cuh), FP32 per-atom work.
 // The kinetic-energy kernel reduces [KE_t, KE_r] in FP64 in a fixed order.
 #include <cuda_runtime.h>
 
@@ -21,6 +25,7 @@
 
 #include "../../include/rbx.h"
 
+#include "rbx_fast.cuh"
 #include "rbx_internal.h"
 #include "rbx_math.cuh"
 
@@ -44,7 +49,7 @@ template <> struct Tr<PREC_SINGLE> {
 };
 template <> struct Tr<PREC_MIXED> {
     using A = float;
-    using R = double;
+    using R = double;  // free-atom arithmetic (velm is FP64)
     using D = float;
     using P4 = float4;
     using V4 = dq4;
@@ -123,10 +128,6 @@ template <> struct PosIO<PREC_DOUBLE> {
     }
 };
 
-template <class T> struct SmemLayout {
-    // byte offsets of the shared-memory arrays of one step CTA
-    static constexpr size_t align(size_t x) { return (x + 15) & ~size_t(15); }
-};
 
 template <int P> __host__ __device__ constexpr size_t step_smem() {
     using A = typename Tr<P>::A;
@@ -160,133 +161,317 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
     vel[loc] = vm;
 }
 
-template <int P, int KIND, bool EXACT>
-__global__ void __launch_bounds__(kThreads) step_kernel(DevSys S, DevBuf B, double dt) {
-    using A = typename Tr<P>::A;
-    using R = typename Tr<P>::R;
-    using D = typename Tr<P>::D;
-    using V4 = typename Tr<P>::V4;
-    constexpr int TA = Tr<P>::kTA, TB = kTileBodies;
+// Shared-memory carve-up common to both step kernels.
+template <class A> struct StepSmem {
+    A *sF, *sT, *sX, *sQ, *sW;
+    double* sRb;
+    unsigned short* sBody;
+    template <int TA, int TB> __device__ __forceinline__ void carve(unsigned char* smem) {
+        sF = (A*)smem;
+        sT = sF + 3 * TA;
+        sX = sT + 3 * TA;
+        sQ = sX + 3 * TA;
+        sRb = (double*)(sQ + 4 * TB);
+        sW = (A*)(sRb + 3 * TB);
+        sBody = (unsigned short*)(sW + 3 * TB);
+    }
+};
 
+// Phase 1 (both kernels): per-atom force, displacement from the COM and torque. Each thread
+// owns up to TA / kThreads atoms; all of their loads are issued before any is used so that the
+// gathers overlap.
+template <int P, int KIND, class A, class D>
+__device__ __forceinline__ void atom_forces(const DevSys& S, const DevBuf& B, const StepSmem<A>& sm, int a0, int nat) {
+    constexpr int APT = Tr<P>::kTA / kThreads;
+    const D* __restrict__ dg = (const D*)S.d;
+    int loc[APT];
+    V3<A> F[APT], d[APT];
+#pragma unroll
+    for (int i = 0; i < APT; i++) {
+        const int a = threadIdx.x + i * kThreads;
+        loc[i] = a < nat ? __ldg(S.atom_loc + a0 + a) : 0;
+    }
+#pragma unroll
+    for (int i = 0; i < APT; i++) {
+        const int a = threadIdx.x + i * kThreads;
+        if (a < nat) {
+            const int k = a0 + a;
+            d[i] = v3<A>((A)__ldg(dg + k), (A)__ldg(dg + k + S.nba_pad), (A)__ldg(dg + k + 2 * S.nba_pad));
+            F[i] = load_force<A>(B.force, loc[i], B.stride);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < APT; i++) {
+        const int a = threadIdx.x + i * kThreads;
+        if (a < nat) {
+            const int t = sm.sBody[a];
+            Q4<A> q = q4<A>(sm.sQ[4 * t], sm.sQ[4 * t + 1], sm.sQ[4 * t + 2], sm.sQ[4 * t + 3]);
+            V3<A> delta = rotate_to_space(q, d[i]);
+            V3<A> tau = cross(delta, F[i]);
+            sm.sF[3 * a] = F[i].x; sm.sF[3 * a + 1] = F[i].y; sm.sF[3 * a + 2] = F[i].z;
+            sm.sT[3 * a] = tau.x; sm.sT[3 * a + 1] = tau.y; sm.sT[3 * a + 2] = tau.z;
+            V3<A> x = KIND == STEP_PART2 ? delta : d[i];
+            sm.sX[3 * a] = x.x; sm.sX[3 * a + 1] = x.y; sm.sX[3 * a + 2] = x.z;
+        }
+    }
+}
+
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// Fixed-order sum of the tile-local atoms [s, e) of one body.
+template <class A>
+__device__ __forceinline__ void body_sums(const StepSmem<A>& sm, int s, int e, V3<A>& F, V3<A>& T) {
+    F = v3<A>(A(0), A(0), A(0));
+    T = F;
+    for (int j = s; j < e; j++) {
+        F = F + v3<A>(sm.sF[3 * j], sm.sF[3 * j + 1], sm.sF[3 * j + 2]);
+        T = T + v3<A>(sm.sT[3 * j], sm.sT[3 * j + 1], sm.sT[3 * j + 2]);
+    }
+}
+
+// Phase 3, part2: atom velocities v + omega_space x delta.
+template <int P, class A>
+__device__ __forceinline__ void atom_velocities(const DevSys& S, const DevBuf& B, const StepSmem<A>& sm, int a0, int nat) {
+    using V4 = typename Tr<P>::V4;
+    V4* vel = (V4*)B.velm;
+    for (int a = threadIdx.x; a < nat; a += kThreads) {
+        const int t = sm.sBody[a];
+        const int loc = __ldg(S.atom_loc + a0 + a);
+        V3<A> x = v3<A>(sm.sX[3 * a], sm.sX[3 * a + 1], sm.sX[3 * a + 2]);
+        V3<A> w = v3<A>(sm.sW[3 * t], sm.sW[3 * t + 1], sm.sW[3 * t + 2]);
+        V3<A> rel = cross(w, x);
+        V4 vm = vel[loc];
+        vm.x = sm.sRb[3 * t] + (double)rel.x;
+        vm.y = sm.sRb[3 * t + 1] + (double)rel.y;
+        vm.z = sm.sRb[3 * t + 2] + (double)rel.z;
+        vel[loc] = vm;
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Double precision: FP64 throughout, the plugin's formulas (RigidBody.cpp, rigidbodyintegrator.cu).
+// ------------------------------------------------------------------------------------------
+template <int KIND, bool EXACT>
+__global__ void __launch_bounds__(kThreads) step_kernel_d(DevSys S, DevBuf B, double dt) {
+    constexpr int P = PREC_DOUBLE;
+    constexpr int TA = Tr<P>::kTA, TB = kTileBodies;
     if ((int)blockIdx.x >= S.n_body_tiles) {
         free_atom_tile<P, KIND>(S, B, dt, (int)blockIdx.x - S.n_body_tiles);
         return;
     }
     extern __shared__ __align__(16) unsigned char smem[];
-    A* sF = (A*)smem;
-    A* sT = sF + 3 * TA;
-    A* sX = sT + 3 * TA;
-    A* sQ = sX + 3 * TA;
-    double* sRb = (double*)(sQ + 4 * TB);
-    A* sW = (A*)(sRb + 3 * TB);
-    unsigned short* sBody = (unsigned short*)(sW + 3 * TB);
-
+    StepSmem<double> sm;
+    sm.carve<TA, TB>(smem);
     const int tid = threadIdx.x;
     const int b0 = __ldg(S.tile_body0 + blockIdx.x), b1 = __ldg(S.tile_body0 + blockIdx.x + 1);
     const int nbt = b1 - b0;
     const int a0 = __ldg(S.atom0 + b0), nat = __ldg(S.atom0 + b1) - a0;
     const int nbp = S.nb_pad;
-    double* __restrict__ st = S.state;
+    double* __restrict__ st = (double*)S.state;
 
-    // Phase 0: stage orientation, mark atoms with their tile-local body.
     if (tid < nbt) {
         const int b = b0 + tid;
-        sQ[4 * tid + 0] = (A)st[b + 6 * nbp];
-        sQ[4 * tid + 1] = (A)st[b + 7 * nbp];
-        sQ[4 * tid + 2] = (A)st[b + 8 * nbp];
-        sQ[4 * tid + 3] = (A)st[b + 9 * nbp];
+        for (int c = 0; c < 4; c++) sm.sQ[4 * tid + c] = st[b + (6 + c) * nbp];
         const int s = __ldg(S.atom0 + b) - a0, e = __ldg(S.atom0 + b + 1) - a0;
-        for (int j = s; j < e; j++) sBody[j] = (unsigned short)tid;
+        for (int j = s; j < e; j++) sm.sBody[j] = (unsigned short)tid;
     }
     __syncthreads();
-
-    // Phase 1: per-atom force, displacement and torque.
-    const D* __restrict__ dg = (const D*)S.d;
-    for (int a = tid; a < nat; a += kThreads) {
-        const int k = a0 + a;
-        const int t = sBody[a];
-        Q4<A> q = q4<A>(sQ[4 * t], sQ[4 * t + 1], sQ[4 * t + 2], sQ[4 * t + 3]);
-        V3<A> d = v3<A>((A)__ldg(dg + k), (A)__ldg(dg + k + S.nba_pad), (A)__ldg(dg + k + 2 * S.nba_pad));
-        const int loc = __ldg(S.atom_loc + k);
-        V3<A> F = load_force<A>(B.force, loc, B.stride);
-        V3<A> delta = rotate_to_space(q, d);
-        V3<A> tau = cross(delta, F);
-        sF[3 * a] = F.x; sF[3 * a + 1] = F.y; sF[3 * a + 2] = F.z;
-        sT[3 * a] = tau.x; sT[3 * a + 1] = tau.y; sT[3 * a + 2] = tau.z;
-        V3<A> x = KIND == STEP_PART2 ? delta : d;
-        sX[3 * a] = x.x; sX[3 * a + 1] = x.y; sX[3 * a + 2] = x.z;
-    }
+    atom_forces<P, KIND, double, double>(S, B, sm, a0, nat);
     __syncthreads();
-
-    // Phase 2: per-body reduction, kicks, drift, rotation.
     if (tid < nbt) {
         const int b = b0 + tid;
-        const int s = __ldg(S.atom0 + b) - a0, e = __ldg(S.atom0 + b + 1) - a0;
-        V3<A> Fa = v3<A>(A(0), A(0), A(0)), Ta = Fa;
-        for (int j = s; j < e; j++) {
-            Fa = Fa + v3<A>(sF[3 * j], sF[3 * j + 1], sF[3 * j + 2]);
-            Ta = Ta + v3<A>(sT[3 * j], sT[3 * j + 1], sT[3 * j + 2]);
-        }
+        V3<double> Fa, Ta;
+        body_sums(sm, __ldg(S.atom0 + b) - a0, __ldg(S.atom0 + b + 1) - a0, Fa, Ta);
         V3<double> r = v3<double>(st[b], st[b + nbp], st[b + 2 * nbp]);
-        V3<R> v = v3<R>((R)st[b + 3 * nbp], (R)st[b + 4 * nbp], (R)st[b + 5 * nbp]);
-        Q4<R> q = q4<R>((R)st[b + 6 * nbp], (R)st[b + 7 * nbp], (R)st[b + 8 * nbp], (R)st[b + 9 * nbp]);
-        Q4<R> pi = q4<R>((R)st[b + 10 * nbp], (R)st[b + 11 * nbp], (R)st[b + 12 * nbp], (R)st[b + 13 * nbp]);
-        const R invm = (R)__ldg(S.invm + b);
-        const V3<R> invI = v3<R>((R)__ldg(S.invI + b), (R)__ldg(S.invI + b + nbp), (R)__ldg(S.invI + b + 2 * nbp));
-        const R rdt = (R)dt, halfDt = R(0.5) * rdt;
-        const V3<R> F = cvt<R>(Fa);
-        const Q4<R> Ctau = qC(q, cvt<R>(Ta));
-        const V3<R> dv = F * (invm * halfDt);
+        V3<double> v = v3<double>(st[b + 3 * nbp], st[b + 4 * nbp], st[b + 5 * nbp]);
+        Q4<double> q = q4<double>(st[b + 6 * nbp], st[b + 7 * nbp], st[b + 8 * nbp], st[b + 9 * nbp]);
+        Q4<double> pi = q4<double>(st[b + 10 * nbp], st[b + 11 * nbp], st[b + 12 * nbp], st[b + 13 * nbp]);
+        const double invm = __ldg(S.invm + b);
+        const V3<double> invI = v3<double>(__ldg(S.invI + b), __ldg(S.invI + b + nbp), __ldg(S.invI + b + 2 * nbp));
+        const double halfDt = 0.5 * dt;
+        const Q4<double> Ctau = qC(q, Ta);
+        const V3<double> dv = Fa * (invm * halfDt);
         const int kicks = KIND == STEP_FUSED ? 2 : 1;
         for (int kk = 0; kk < kicks; kk++) {
             v = v + dv;
-            pi = pi + Ctau * rdt;
+            pi = pi + Ctau * dt;
         }
-        st[b + 3 * nbp] = (double)v.x; st[b + 4 * nbp] = (double)v.y; st[b + 5 * nbp] = (double)v.z;
+        st[b + 3 * nbp] = v.x; st[b + 4 * nbp] = v.y; st[b + 5 * nbp] = v.z;
         if (KIND == STEP_PART2) {
-            V3<R> omega = mul(invI, qBt(q, pi)) * R(0.5);
-            V3<R> ws = rotate_to_space(q, omega);
-            sRb[3 * tid] = (double)v.x; sRb[3 * tid + 1] = (double)v.y; sRb[3 * tid + 2] = (double)v.z;
-            sW[3 * tid] = (A)ws.x; sW[3 * tid + 1] = (A)ws.y; sW[3 * tid + 2] = (A)ws.z;
+            V3<double> ws = rotate_to_space(q, mul(invI, qBt(q, pi)) * 0.5);
+            sm.sRb[3 * tid] = v.x; sm.sRb[3 * tid + 1] = v.y; sm.sRb[3 * tid + 2] = v.z;
+            sm.sW[3 * tid] = ws.x; sm.sW[3 * tid + 1] = ws.y; sm.sW[3 * tid + 2] = ws.z;
         } else {
-            r = r + cvt<double>(v * rdt);
+            r = r + v * dt;
             if (EXACT) {
                 const int cls = __ldg(S.cls + b);
-                V3<R> I = v3<R>(R(1) / invI.x, R(1) / invI.y, invI.z != R(0) ? R(1) / invI.z : R(0));
-                exact_rotation<R>(cls, I, invI, q, pi, rdt);
+                V3<double> I = v3<double>(1.0 / invI.x, 1.0 / invI.y, invI.z != 0.0 ? 1.0 / invI.z : 0.0);
+                exact_rotation<double>(cls, I, invI, q, pi, dt);
             } else {
-                nosquish_rotation<R>(invI, invI.z != R(0), q, pi, rdt, S.rot_n);
+                nosquish_rotation<double>(invI, invI.z != 0.0, q, pi, dt, S.rot_n);
             }
             st[b] = r.x; st[b + nbp] = r.y; st[b + 2 * nbp] = r.z;
-            sRb[3 * tid] = r.x; sRb[3 * tid + 1] = r.y; sRb[3 * tid + 2] = r.z;
-            sQ[4 * tid] = (A)q.w; sQ[4 * tid + 1] = (A)q.x; sQ[4 * tid + 2] = (A)q.y; sQ[4 * tid + 3] = (A)q.z;
+            sm.sRb[3 * tid] = r.x; sm.sRb[3 * tid + 1] = r.y; sm.sRb[3 * tid + 2] = r.z;
+            sm.sQ[4 * tid] = q.w; sm.sQ[4 * tid + 1] = q.x; sm.sQ[4 * tid + 2] = q.y; sm.sQ[4 * tid + 3] = q.z;
+            st[b + 6 * nbp] = q.w; st[b + 7 * nbp] = q.x; st[b + 8 * nbp] = q.y; st[b + 9 * nbp] = q.z;
         }
-        st[b + 6 * nbp] = (double)q.w; st[b + 7 * nbp] = (double)q.x;
-        st[b + 8 * nbp] = (double)q.y; st[b + 9 * nbp] = (double)q.z;
-        st[b + 10 * nbp] = (double)pi.w; st[b + 11 * nbp] = (double)pi.x;
-        st[b + 12 * nbp] = (double)pi.y; st[b + 13 * nbp] = (double)pi.z;
+        st[b + 10 * nbp] = pi.w; st[b + 11 * nbp] = pi.x; st[b + 12 * nbp] = pi.y; st[b + 13 * nbp] = pi.z;
+    }
+    __syncthreads();
+    if (KIND == STEP_PART2) {
+        atom_velocities<P, double>(S, B, sm, a0, nat);
+    } else {
+        for (int a = tid; a < nat; a += kThreads) {
+            const int t = sm.sBody[a];
+            const int loc = __ldg(S.atom_loc + a0 + a);
+            Q4<double> q = q4<double>(sm.sQ[4 * t], sm.sQ[4 * t + 1], sm.sQ[4 * t + 2], sm.sQ[4 * t + 3]);
+            V3<double> delta = rotate_to_space(q, v3<double>(sm.sX[3 * a], sm.sX[3 * a + 1], sm.sX[3 * a + 2]));
+            PosIO<P>::store(B, loc, v3<double>(sm.sRb[3 * t], sm.sRb[3 * t + 1], sm.sRb[3 * t + 2]), delta);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Single and mixed precision: FP32 arithmetic, float-float body state, rotation increments.
+// ------------------------------------------------------------------------------------------
+template <int P, int KIND, bool EXACT>
+__global__ void __launch_bounds__(kThreads, 4) step_kernel_f(DevSys S, DevBuf B, double dt_d) {
+    constexpr int TA = Tr<P>::kTA, TB = kTileBodies;
+    if ((int)blockIdx.x >= S.n_body_tiles) {
+        free_atom_tile<P, KIND>(S, B, dt_d, (int)blockIdx.x - S.n_body_tiles);
+        return;
+    }
+    extern __shared__ __align__(16) unsigned char smem[];
+    StepSmem<float> sm;
+    sm.carve<TA, TB>(smem);
+    const int tid = threadIdx.x;
+    const int b0 = __ldg(S.tile_body0 + blockIdx.x), b1 = __ldg(S.tile_body0 + blockIdx.x + 1);
+    const int nbt = b1 - b0;
+    const int a0 = __ldg(S.atom0 + b0), nat = __ldg(S.atom0 + b1) - a0;
+    const int nbp = S.nb_pad;
+    float* __restrict__ hi = (float*)S.state;  // rows 0..13
+    float* __restrict__ lo = hi + 14 * nbp;    // rows 14..27
+    const float dt = (float)dt_d;
+
+    // Phase 0: orientation into shared memory, the rest of the body record prefetched into L2
+    // (loaded after the atom phase, keeping registers free for the atom gathers).
+    if (tid < nbt) {
+        const int b = b0 + tid;
+#pragma unroll
+        for (int c = 0; c < 4; c++) sm.sQ[4 * tid + c] = hi[b + (6 + c) * nbp];
+#pragma unroll
+        for (int c = 0; c < 14; c++) {
+            if (c < 6 || c > 9) prefetch_l2(hi + b + c * nbp);
+            prefetch_l2(lo + b + c * nbp);
+        }
+#pragma unroll
+        for (int c = 0; c < kBconstRows; c++) prefetch_l2(S.bconst + b + c * nbp);
+        const int s = __ldg(S.atom0 + b) - a0, e = __ldg(S.atom0 + b + 1) - a0;
+        for (int j = s; j < e; j++) sm.sBody[j] = (unsigned short)tid;
+    }
+    __syncthreads();
+    atom_forces<P, KIND, float, float>(S, B, sm, a0, nat);
+    __syncthreads();
+
+    // Phase 2: kicks, drift and rotation on the float-float state.
+    if (tid < nbt) {
+        const int b = b0 + tid;
+        ff x[14];
+#pragma unroll
+        for (int c = 0; c < 14; c++) x[c] = ff{hi[b + c * nbp], lo[b + c * nbp]};
+        V3<float> Fa, Ta;
+        body_sums(sm, __ldg(S.atom0 + b) - a0, __ldg(S.atom0 + b + 1) - a0, Fa, Ta);
+        const float* bc = S.bconst;
+        const float invm = __ldg(bc + b), invm_lo = __ldg(bc + b + 7 * nbp);
+        Rotor R;
+        R.invI = v3<float>(__ldg(bc + b + nbp), __ldg(bc + b + 2 * nbp), __ldg(bc + b + 3 * nbp));
+        R.g01 = __ldg(bc + b + 4 * nbp);
+        R.g12 = __ldg(bc + b + 5 * nbp);
+        R.g02 = __ldg(bc + b + 6 * nbp);
+        R.invI_lo = v3<float>(__ldg(bc + b + 8 * nbp), __ldg(bc + b + 9 * nbp), __ldg(bc + b + 10 * nbp));
+        const Q4<float> qh = q4<float>(x[6].hi, x[7].hi, x[8].hi, x[9].hi);
+        const Q4<float> Ctau = qC(qh, Ta) * dt;              // pi kick, full dt (RigidBodySystem.cpp:179)
+        const float hdt = 0.5f * dt;                         // COM velocity half kick, 1/m as hi + lo
+        const V3<float> dv = v3<float>(fmaf(Fa.x, invm_lo * hdt, Fa.x * (invm * hdt)),
+                                       fmaf(Fa.y, invm_lo * hdt, Fa.y * (invm * hdt)),
+                                       fmaf(Fa.z, invm_lo * hdt, Fa.z * (invm * hdt)));
+        const int kicks = KIND == STEP_FUSED ? 2 : 1;
+        for (int kk = 0; kk < kicks; kk++) {
+            x[3] = ff_add(x[3], dv.x); x[4] = ff_add(x[4], dv.y); x[5] = ff_add(x[5], dv.z);
+            x[10] = ff_add(x[10], Ctau.w); x[11] = ff_add(x[11], Ctau.x);
+            x[12] = ff_add(x[12], Ctau.y); x[13] = ff_add(x[13], Ctau.z);
+        }
+        const Q4<float> ph = q4<float>(x[10].hi, x[11].hi, x[12].hi, x[13].hi);
+        if (KIND == STEP_PART2) {
+            V3<float> ws = rotate_to_space(qh, mul(R.invI, qBt(qh, ph)) * 0.5f);
+            sm.sRb[3 * tid] = (double)x[3].hi + (double)x[3].lo;
+            sm.sRb[3 * tid + 1] = (double)x[4].hi + (double)x[4].lo;
+            sm.sRb[3 * tid + 2] = (double)x[5].hi + (double)x[5].lo;
+            sm.sW[3 * tid] = ws.x; sm.sW[3 * tid + 1] = ws.y; sm.sW[3 * tid + 2] = ws.z;
+        } else {
+            // drift
+#pragma unroll
+            for (int c = 0; c < 3; c++) x[c] = ff_add(x[c], fmaf(x[3 + c].hi, dt, x[3 + c].lo * dt));
+            // free rotation as an increment of q and pi
+            const V3<float> L = qBt(qh, ph) * 0.5f;
+            Q4<float> dr;
+            if (EXACT) dr = dq_exact(__ldg(S.cls + b), L, R, dt);
+            else dr = nosquish_increment(L, R, R.invI.z != 0.0f, dt, S.rot_n);
+            const Q4<float> dq = qmul(qh, dr), dp = qmul(ph, dr);
+            x[6] = ff_add(x[6], dq.w); x[7] = ff_add(x[7], dq.x); x[8] = ff_add(x[8], dq.y); x[9] = ff_add(x[9], dq.z);
+            x[10] = ff_add(x[10], dp.w); x[11] = ff_add(x[11], dp.x);
+            x[12] = ff_add(x[12], dp.y); x[13] = ff_add(x[13], dp.z);
+            // renormalise q: eps = |q|^2 - 1 from exact squares, q <- q (1 - eps/2)
+            ff n2 = ff{0.0f, 0.0f};
+            float tail = 0.0f;
+#pragma unroll
+            for (int c = 6; c < 10; c++) {
+                float p = x[c].hi * x[c].hi;
+                tail += fmaf(x[c].hi, x[c].hi, -p) + 2.0f * x[c].hi * x[c].lo;
+                n2 = ff_add(n2, p);
+            }
+            const float eps = ((n2.hi - 1.0f) + n2.lo) + tail;
+#pragma unroll
+            for (int c = 6; c < 10; c++) x[c] = ff_add(x[c], -0.5f * eps * x[c].hi);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {  // COM as float-float pairs in the double slots
+                ((float*)(sm.sRb + 3 * tid))[2 * c] = x[c].hi;
+                ((float*)(sm.sRb + 3 * tid))[2 * c + 1] = x[c].lo;
+            }
+#pragma unroll
+            for (int c = 0; c < 4; c++) sm.sQ[4 * tid + c] = x[6 + c].hi;
+        }
+#pragma unroll
+        for (int c = 0; c < 14; c++) {
+            hi[b + c * nbp] = x[c].hi;
+            lo[b + c * nbp] = x[c].lo;
+        }
     }
     __syncthreads();
 
-    // Phase 3: scatter positions (part1, fused) or velocities (part2).
-    for (int a = tid; a < nat; a += kThreads) {
-        const int k = a0 + a;
-        const int t = sBody[a];
-        const int loc = __ldg(S.atom_loc + k);
-        V3<A> x = v3<A>(sX[3 * a], sX[3 * a + 1], sX[3 * a + 2]);
-        if (KIND == STEP_PART2) {
-            V3<A> w = v3<A>(sW[3 * t], sW[3 * t + 1], sW[3 * t + 2]);
-            V3<A> rel = cross(w, x);
-            V4* vel = (V4*)B.velm;
-            V4 vm = vel[loc];
-            vm.x = sRb[3 * t] + (double)rel.x;
-            vm.y = sRb[3 * t + 1] + (double)rel.y;
-            vm.z = sRb[3 * t + 2] + (double)rel.z;
-            vel[loc] = vm;
-        } else {
-            Q4<A> q = q4<A>(sQ[4 * t], sQ[4 * t + 1], sQ[4 * t + 2], sQ[4 * t + 3]);
-            V3<A> delta = rotate_to_space(q, x);
-            PosIO<P>::store(B, loc, v3<double>(sRb[3 * t], sRb[3 * t + 1], sRb[3 * t + 2]), delta);
+    // Phase 3
+    if (KIND == STEP_PART2) {
+        atom_velocities<P, float>(S, B, sm, a0, nat);
+    } else {
+        for (int a = tid; a < nat; a += kThreads) {
+            const int t = sm.sBody[a];
+            const int loc = __ldg(S.atom_loc + a0 + a);
+            Q4<float> q = q4<float>(sm.sQ[4 * t], sm.sQ[4 * t + 1], sm.sQ[4 * t + 2], sm.sQ[4 * t + 3]);
+            V3<float> delta = rotate_to_space(q, v3<float>(sm.sX[3 * a], sm.sX[3 * a + 1], sm.sX[3 * a + 2]));
+            const float* rf = (const float*)(sm.sRb + 3 * t);
+            // posq.w (the charge) is left untouched: x, y written as one 8-byte store, z as 4 bytes
+            float* pq = (float*)B.posq + 4 * (size_t)loc;
+            if (P == PREC_MIXED) {
+                ff px = ff_add(ff{rf[0], rf[1]}, delta.x);
+                ff py = ff_add(ff{rf[2], rf[3]}, delta.y);
+                ff pz = ff_add(ff{rf[4], rf[5]}, delta.z);
+                *(float2*)pq = make_float2(px.hi, py.hi);
+                pq[2] = pz.hi;
+                ((float4*)B.corr)[loc] = make_float4(px.lo, py.lo, pz.lo, 0.0f);
+            } else {
+                *(float2*)pq = make_float2(rf[0] + (rf[1] + delta.x), rf[2] + (rf[3] + delta.y));
+                pq[2] = rf[4] + (rf[5] + delta.z);
+            }
         }
     }
 }
@@ -296,22 +481,48 @@ __global__ void __launch_bounds__(kThreads) step_kernel(DevSys S, DevBuf B, doub
 // ------------------------------------------------------------------------------------------
 constexpr int kKEThreads = 256;
 
+// Body state and constants of body b as FP64, for either state layout.
+template <int P> struct BodyRead {
+    static __device__ __forceinline__ void get(const DevSys& S, int b, V3<double>& v, Q4<double>& q, Q4<double>& pi,
+                                               double& invm, V3<double>& invI) {
+        const int nbp = S.nb_pad;
+        if (P == PREC_DOUBLE) {
+            const double* st = (const double*)S.state;
+            v = v3<double>(st[b + 3 * nbp], st[b + 4 * nbp], st[b + 5 * nbp]);
+            q = q4<double>(st[b + 6 * nbp], st[b + 7 * nbp], st[b + 8 * nbp], st[b + 9 * nbp]);
+            pi = q4<double>(st[b + 10 * nbp], st[b + 11 * nbp], st[b + 12 * nbp], st[b + 13 * nbp]);
+            invm = S.invm[b];
+            invI = v3<double>(S.invI[b], S.invI[b + nbp], S.invI[b + 2 * nbp]);
+        } else {
+            const float* h = (const float*)S.state;
+            const float* l = h + 14 * nbp;
+            double x[14];
+            for (int k = 3; k < 14; k++) x[k] = (double)h[b + k * nbp] + (double)l[b + k * nbp];
+            v = v3<double>(x[3], x[4], x[5]);
+            q = q4<double>(x[6], x[7], x[8], x[9]);
+            pi = q4<double>(x[10], x[11], x[12], x[13]);
+            const float* c = S.bconst;
+            invm = (double)c[b] + (double)c[b + 7 * nbp];
+            invI = v3<double>((double)c[b + nbp] + (double)c[b + 8 * nbp], (double)c[b + 2 * nbp] + (double)c[b + 9 * nbp],
+                              (double)c[b + 3 * nbp] + (double)c[b + 10 * nbp]);
+        }
+    }
+};
+
 template <int P>
 __global__ void __launch_bounds__(kKEThreads) kinetic_kernel(DevSys S, DevBuf B, KEScratch K) {
     using V4 = typename Tr<P>::V4;
     __shared__ double s_t[kKEThreads], s_r[kKEThreads];
     __shared__ bool s_last;
-    const int nbp = S.nb_pad;
-    const double* st = S.state;
     double kt = 0.0, kr = 0.0;
     const int gsize = gridDim.x * blockDim.x;
     for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < S.nb; b += gsize) {
-        V3<double> v = v3<double>(st[b + 3 * nbp], st[b + 4 * nbp], st[b + 5 * nbp]);
-        Q4<double> q = q4<double>(st[b + 6 * nbp], st[b + 7 * nbp], st[b + 8 * nbp], st[b + 9 * nbp]);
-        Q4<double> pi = q4<double>(st[b + 10 * nbp], st[b + 11 * nbp], st[b + 12 * nbp], st[b + 13 * nbp]);
-        V3<double> invI = v3<double>(S.invI[b], S.invI[b + nbp], S.invI[b + 2 * nbp]);
+        V3<double> v, invI;
+        Q4<double> q, pi;
+        double invm;
+        BodyRead<P>::get(S, b, v, q, pi, invm, invI);
         V3<double> L = qBt(q, pi) * 0.5;
-        kt += dot(v, v) / S.invm[b];
+        kt += dot(v, v) / invm;
         kr += dot(L, mul(invI, L));
     }
     const V4* vel = (const V4*)B.velm;
@@ -409,19 +620,26 @@ size_t step_smem_bytes(int prec) {
     }
 }
 
+template <int P, int KIND, bool EXACT> struct StepKernel {
+    static constexpr auto fn() { return step_kernel_f<P, KIND, EXACT>; }
+};
+template <int KIND, bool EXACT> struct StepKernel<PREC_DOUBLE, KIND, EXACT> {
+    static constexpr auto fn() { return step_kernel_d<KIND, EXACT>; }
+};
+
 template <int P, int KIND, bool EXACT>
 static int launch_step_t(const DevSys& s, const DevBuf& b, double dt, cudaStream_t stream) {
     static bool configured = false;
     const size_t smem = step_smem<P>();
+    auto kernel = StepKernel<P, KIND, EXACT>::fn();
     if (!configured) {
-        if (cudaFuncSetAttribute(step_kernel<P, KIND, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return -1;
         configured = true;
     }
     const int grid = s.n_body_tiles + s.n_free_tiles;
     if (grid == 0) return 0;
-    step_kernel<P, KIND, EXACT><<<grid, kThreads, smem, stream>>>(s, b, dt);
+    kernel<<<grid, kThreads, smem, stream>>>(s, b, dt);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
@@ -521,7 +739,7 @@ __global__ void __launch_bounds__(kKEThreads) kinetic_static_kernel(DevSys S, De
     double* partial = scratch;
     unsigned int* count = (unsigned int*)(scratch + 2 * kStaticKEMaxBlocks);
     const int nbp = S.nb_pad;
-    const double* st = S.state;
+    const double* st = (const double*)S.state;
     const int first = blockIdx.x * kStaticKEItemsPerBlock;
     const int last = first + kStaticKEItemsPerBlock;
     double kt = 0.0, kr = 0.0;

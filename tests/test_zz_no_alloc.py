@@ -26,8 +26,10 @@ def setup():
     build.build_library()
     lib = _lib.load()
     s = W.mixed_system(n_bodies=5000, n_free=700, fractions=(0.6, 0.25, 0.15), seed=31)
-    k = kernel.IntegratorKernel(s.masses, s.body_indices, rotation_mode=0, precision="mixed")
-    buf = kernel.DeviceBuffers(s.num_atoms, precision="mixed")
+    # Double precision: the handle keeps its state and constants in FP64, exactly the arrays the
+    # caller hands to the allocation-free entry point below.
+    k = kernel.IntegratorKernel(s.masses, s.body_indices, rotation_mode=0, precision="double")
+    buf = kernel.DeviceBuffers(s.num_atoms, precision="double")
     buf.set_positions(s.positions)
     buf.set_velocities(s.velocities, s.masses)
     buf.set_forces(W.gaussian_forces(s.num_atoms, seed=5, sd=50.0))
@@ -69,7 +71,7 @@ def _call(S, out, nb=None, nf=None):
         ctypes.cast(S["state"].data_ptr(), dp), S["nb"] if nb is None else nb, S["nb"],
         ctypes.cast(S["invm"].data_ptr(), dp), ctypes.cast(S["invI"].data_ptr(), dp),
         ctypes.c_void_p(S["buf"].velm.data_ptr()), ctypes.cast(S["free"].data_ptr(), ip),
-        S["nf"] if nf is None else nf, 1, stream, ctypes.cast(out.data_ptr(), dp))
+        S["nf"] if nf is None else nf, 2, stream, ctypes.cast(out.data_ptr(), dp))
 
 
 def test_static_scratch_matches_allocating_entry_point_twice(setup):
