@@ -111,14 +111,20 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(key):
-    """DRAM bytes per launch of the step kernel from the committed ncu summary, if any."""
+def ncu_traffic(mode, precision, bodies):
+    """DRAM bytes of one fused step launch from the committed ncu summary (profiles/traffic.json),
+    captured on a smaller case of the same mix and scaled to `bodies` (traffic is proportional to
+    the number of bodies, atoms and free atoms, which scale together). None when no capture of this
+    mode/precision is committed."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
-    return d.get(key)
+    key = f"fused_mode{mode}_{precision}_400k_bytes_per_launch"
+    if key not in d:
+        return None
+    return d[key] * bodies / d["bodies"]
 
 
 class ClockSampler:
@@ -271,7 +277,7 @@ def run_gpu(args, world, rank, local):
     per_launch = t_dev / args.steps
     peak, peak_kind = peaks()
     achieved = bytes_step / per_launch / 1e9
-    traffic = ncu_traffic(f"fused_mode{args.mode}_{args.precision}")
+    traffic = ncu_traffic(args.mode, args.precision, nb)
 
     # e2e through the host-buffer C ABI (pinned host arrays, copies inside the timed region)
     x_h = torch.empty((s.num_atoms, 3), dtype=torch.float64).pin_memory().numpy()
