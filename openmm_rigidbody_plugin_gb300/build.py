@@ -30,7 +30,10 @@ def _compile(src, verbose):
     cmd = [nvcc(), "-c", os.path.join(CSRC, src), "-o", obj, "-std=c++17", "-O3", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-Wall"]
     if src.endswith(".cu"):
-        cmd += ARCH + ["-lineinfo", "--expt-relaxed-constexpr"]
+        # FP32 division and square root need not be IEEE-exact anywhere on the single/mixed path
+        # (rotation increments and series; the float-float sums use explicit round-to-nearest
+        # adds); FP64 code is unaffected by these flags.
+        cmd += ARCH + ["-lineinfo", "--expt-relaxed-constexpr", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
         if verbose:
             cmd += ["-Xptxas", "-v"]
     else:

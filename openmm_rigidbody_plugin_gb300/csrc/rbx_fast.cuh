@@ -14,7 +14,8 @@
 //    (sn, cn, dn of u0 + h from their values at u0, which the current state fixes, and of the
 //    small argument h = wp dt); the rotation is r = e(phi) (x) mu, with mu the minimal rotation
 //    taking L_hat(t) back to L_hat(0) and phi the angle about L_hat(0), whose rate is
-//    phi' = omega . (n + n0) / (1 + n . n0), integrated by 5-point Gauss-Legendre quadrature.
+//    phi' = omega . (n + n0) / (1 + n . n0), integrated by 4-point Gauss-Legendre quadrature
+//    (exact to ~1e-9 relative for |wp dt| <= 0.3; thermal water at 2 fs has |wp dt| <= 0.11).
 //    This evaluates the same solution as the closed form of openmmapi/src/RigidBody.cpp:241-308
 //    (agreement 2e-12 in FP64) without its third-kind elliptic integrals, and with no gauge
 //    singularity.
@@ -42,6 +43,20 @@ __device__ __forceinline__ ff ff_add(ff a, float b) {
     float hi = __fadd_rn(s, e);
     float lo = __fsub_rn(e, __fsub_rn(hi, s));
     return ff{hi, lo};
+}
+
+// a + b without the final renormalisation: the rounding error of hi + b is added to lo, so
+// hi + lo stays exact to float-float accuracy while |lo| may exceed half an ulp of hi; a chain of
+// these is closed by ff_norm before the value is stored.
+__device__ __forceinline__ ff ff_acc(ff a, float b) {
+    float s = __fadd_rn(a.hi, b);
+    float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return ff{s, __fadd_rn(a.lo, e)};
+}
+__device__ __forceinline__ ff ff_norm(ff a) {
+    float hi = __fadd_rn(a.hi, a.lo);
+    return ff{hi, __fsub_rn(a.lo, __fsub_rn(hi, a.hi))};
 }
 
 // Split s + e (|e| small against s) into the OpenMM position pair posq = hi, correction = lo.
@@ -233,14 +248,13 @@ __device__ __forceinline__ Q4<float> dq_exact_asymmetric(V3<float> Iw, const Rot
         float dd = (d0 * dm1 - m * s0 * c0 * sh * (1.0f + cm1) + d0 * ms0s0 * sh2) * invD;
         return case1 ? v3<float>(Ia.x * dc, Ia.y * ds, Ia.z * dd) : v3<float>(Ia.x * dd, Ia.y * ds, Ia.z * dc);
     };
-    // precession angle about L(0): phi = int omega . (n + n0) / (1 + n . n0) dt, 5-point
+    // precession angle about L(0): phi = int omega . (n + n0) / (1 + n . n0) dt, 4-point
     // Gauss-Legendre nodes and weights on [0, dt]
-    const float glx[5] = {-0.9061798459386640f, -0.5384693101056831f, 0.0f, 0.5384693101056831f, 0.9061798459386640f};
-    const float glw[5] = {0.2369268850561891f, 0.4786286704993665f, 0.5688888888888889f, 0.4786286704993665f,
-                          0.2369268850561891f};
+    const float glx[4] = {-0.8611363115940526f, -0.3399810435848563f, 0.3399810435848563f, 0.8611363115940526f};
+    const float glw[4] = {0.3478548451374538f, 0.6521451548625461f, 0.6521451548625461f, 0.3478548451374538f};
     float phi = 0.0f;
 #pragma unroll
-    for (int i = 0; i < 5; i++) {
+    for (int i = 0; i < 4; i++) {
         float t = 0.5f * dt * (1.0f + glx[i]);
         V3<float> Lt = Iw + dL(t);
         V3<float> n = Lt * rsqrtf(dot(Lt, Lt));

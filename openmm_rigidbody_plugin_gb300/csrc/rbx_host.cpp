@@ -50,11 +50,14 @@ template <class T> struct DevArray {
         p = nullptr;
         n = 0;
     }
+    // The allocation is rounded up to a multiple of 256 bytes, so that bulk L2 prefetches of any
+    // element range, widened to 16-byte boundaries, stay inside it.
     cudaError_t alloc(size_t count) {
         release();
         n = count;
         if (count == 0) return cudaSuccess;
-        return cudaMalloc((void**)&p, count * sizeof(T));
+        const size_t bytes = ((count * sizeof(T) + 255) / 256) * 256;
+        return cudaMalloc((void**)&p, bytes);
     }
 };
 
@@ -89,7 +92,7 @@ struct rbx_integrator {
 
     DevArray<double> d_state, d_invm, d_invI;  // d_state holds FP64 rows or float-float rows
     DevArray<float> d_bconst;                   // single/mixed: 11 rows (see kBconstRows)
-    DevArray<int> d_atom0, d_atom_loc, d_free_loc, d_tiles;
+    DevArray<int> d_atom0, d_atom_loc, d_free_loc, d_tiles, d_tile_loc0;
     DevArray<uint8_t> d_cls;
     DevArray<unsigned char> d_fixed;  // float or double SoA
     DevArray<double> d_ke_partial, d_ke_out;
@@ -110,6 +113,7 @@ struct rbx_integrator {
         s.state = d_state.p; s.invm = d_invm.p; s.invI = d_invI.p; s.bconst = d_bconst.p;
         s.atom0 = d_atom0.p; s.cls = d_cls.p;
         s.d = d_fixed.p; s.atom_loc = d_atom_loc.p; s.free_loc = d_free_loc.p; s.tile_body0 = d_tiles.p;
+        s.tile_loc0 = d_tile_loc0.p;
         return s;
     }
     ~rbx_integrator() {
@@ -338,7 +342,18 @@ int upload_maps(rbx_integrator* h) {
     std::vector<int> atom_loc(h->nba), free_loc(h->nf);
     for (int k = 0; k < h->nba; k++) atom_loc[k] = h->location[h->body_atoms[k]];
     for (int j = 0; j < h->nf; j++) free_loc[j] = h->location[h->free_atoms[j]];
+    // Per body tile: the first device slot when the tile's atoms occupy consecutive slots (its
+    // force and position ranges can then be prefetched in bulk), otherwise -1.
+    std::vector<int> tile_loc0(std::max(h->n_body_tiles, 1), -1);
+    for (int t = 0; t < h->n_body_tiles; t++) {
+        const int a0 = h->body_first[h->tile_body0[t]], a1 = h->body_first[h->tile_body0[t + 1]];
+        bool contiguous = a1 > a0;
+        for (int k = a0 + 1; contiguous && k < a1; k++) contiguous = atom_loc[k] == atom_loc[k - 1] + 1;
+        tile_loc0[t] = contiguous ? atom_loc[a0] : -1;
+    }
     int rc = upload(h->d_atom_loc, atom_loc);
+    if (rc) return rc;
+    rc = upload(h->d_tile_loc0, tile_loc0);
     if (rc) return rc;
     rc = upload(h->d_free_loc, free_loc);
     if (rc) return rc;
@@ -450,7 +465,7 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
             delete h;
             return fail(RBX_ERR_UNSUPPORTED, "a rigid body of %d atoms exceeds the %d-atom tile of this build", n0, TA);
         }
-        while (b < nb && cnt < kTileBodies && atoms + (h->body_first[b + 1] - h->body_first[b]) <= TA) {
+        while (b < nb && cnt < tile_bodies(precision) && atoms + (h->body_first[b + 1] - h->body_first[b]) <= TA) {
             atoms += h->body_first[b + 1] - h->body_first[b];
             cnt++;
             b++;
@@ -458,7 +473,7 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
         h->tile_body0.push_back(b);
     }
     h->n_body_tiles = (int)h->tile_body0.size() - 1;
-    h->n_free_tiles = (h->nf + kFreePerTile - 1) / kFreePerTile;
+    h->n_free_tiles = (h->nf + free_per_tile(precision) - 1) / free_per_tile(precision);
     h->nb_pad = ((std::max(nb, 1) + 31) / 32) * 32;
     h->nba_pad = ((std::max(h->nba, 1) + 31) / 32) * 32;
     h->I.assign((size_t)nb * 3, 0.0);

@@ -23,14 +23,20 @@ namespace rbx {
 enum Precision : int { PREC_SINGLE = 0, PREC_MIXED = 1, PREC_DOUBLE = 2 };
 enum StepKind : int { STEP_PART1 = 0, STEP_PART2 = 1, STEP_FUSED = 2 };
 
-constexpr int kThreads = 256;       // threads per CTA of the step kernels
-constexpr int kTileBodies = 256;    // max bodies per tile (one body per thread in the body phase)
-constexpr int kTileAtomsF = 1024;   // max body atoms per tile, single/mixed
-constexpr int kTileAtomsD = 512;    // max body atoms per tile, double
-constexpr int kFreePerTile = 256;   // free atoms per free-atom tile
+// Double precision: one 256-thread CTA per tile of at most 256 bodies / 512 body atoms.
+constexpr int kThreads = 256;
+constexpr int kTileBodies = 256;
+constexpr int kTileAtomsD = 512;
+// Single/mixed precision: one 256-thread CTA per tile of at most 256 bodies / 1024 body atoms.
+constexpr int kThreadsF = 256;
+constexpr int kTileBodiesF = 256;
+constexpr int kTileAtomsF = 1024;
 constexpr int kBconstRows = 11;     // rows of the FP32 body-constant table (single/mixed)
 
 inline int tile_atoms(int prec) { return prec == PREC_DOUBLE ? kTileAtomsD : kTileAtomsF; }
+inline int tile_bodies(int prec) { return prec == PREC_DOUBLE ? kTileBodies : kTileBodiesF; }
+// Free atoms per free-atom tile: one per thread of the precision's step kernel.
+inline int free_per_tile(int prec) { return prec == PREC_DOUBLE ? kThreads : kThreadsF; }
 
 struct DevSys {
     int nb, nf, nba, nb_pad, nba_pad;
@@ -46,6 +52,7 @@ struct DevSys {
     const int* atom_loc;
     const int* free_loc;
     const int* tile_body0;
+    const int* tile_loc0;  // first device slot of a body tile whose atom slots are consecutive, else -1
 };
 
 struct DevBuf {

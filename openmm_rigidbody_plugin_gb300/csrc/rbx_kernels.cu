@@ -45,7 +45,6 @@ template <> struct Tr<PREC_SINGLE> {
     using P4 = float4; // posq element
     using V4 = float4; // velm element
     static constexpr bool kCorr = false;
-    static constexpr int kTA = kTileAtomsF;
 };
 template <> struct Tr<PREC_MIXED> {
     using A = float;
@@ -54,7 +53,6 @@ template <> struct Tr<PREC_MIXED> {
     using P4 = float4;
     using V4 = dq4;
     static constexpr bool kCorr = true;
-    static constexpr int kTA = kTileAtomsF;
 };
 template <> struct Tr<PREC_DOUBLE> {
     using A = double;
@@ -63,7 +61,6 @@ template <> struct Tr<PREC_DOUBLE> {
     using P4 = dq4;
     using V4 = dq4;
     static constexpr bool kCorr = false;
-    static constexpr int kTA = kTileAtomsD;
 };
 
 // Fixed-point force (scale 2^32) to floating point.
@@ -129,19 +126,19 @@ template <> struct PosIO<PREC_DOUBLE> {
 };
 
 
-template <int P> __host__ __device__ constexpr size_t step_smem() {
-    using A = typename Tr<P>::A;
-    constexpr int TA = Tr<P>::kTA, TB = kTileBodies;
-    // sF, sT, sX: 3*TA each (A); sQ: 4*TB (A); sRb: 3*TB (double); sW: 3*TB (A); sBody: TA (uint16)
-    return (size_t)3 * 3 * TA * sizeof(A) + 4 * TB * sizeof(A) + 3 * TB * sizeof(double) + 3 * TB * sizeof(A) +
-           TA * sizeof(unsigned short) + 64;
+// Shared memory of the double-precision step kernel: sF, sT, sX 3*TA each; sQ 4*TB; sRb 3*TB
+// (double); sW 3*TB; sBody TA (uint16).
+constexpr size_t step_smem_d() {
+    constexpr int TA = kTileAtomsD, TB = kTileBodies;
+    return (size_t)3 * 3 * TA * sizeof(double) + 4 * TB * sizeof(double) + 3 * TB * sizeof(double) +
+           3 * TB * sizeof(double) + TA * sizeof(unsigned short) + 64;
 }
 
 template <int P, int KIND>
 __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B, double dt, int ft) {
     using T = typename Tr<P>::R;  // free-atom velocity/position arithmetic
     using V4 = typename Tr<P>::V4;
-    const int j = ft * kFreePerTile + (int)threadIdx.x;
+    const int j = ft * (int)blockDim.x + (int)threadIdx.x;
     if (j >= S.nf) return;
     const int loc = __ldg(S.free_loc + j);
     V4* vel = (V4*)B.velm;
@@ -182,7 +179,7 @@ template <class A> struct StepSmem {
 // gathers overlap.
 template <int P, int KIND, class A, class D>
 __device__ __forceinline__ void atom_forces(const DevSys& S, const DevBuf& B, const StepSmem<A>& sm, int a0, int nat) {
-    constexpr int APT = Tr<P>::kTA / kThreads;
+    constexpr int APT = kTileAtomsD / kThreads;
     const D* __restrict__ dg = (const D*)S.d;
     int loc[APT];
     V3<A> F[APT], d[APT];
@@ -215,8 +212,6 @@ __device__ __forceinline__ void atom_forces(const DevSys& S, const DevBuf& B, co
         }
     }
 }
-
-__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
 
 // Fixed-order sum of the tile-local atoms [s, e) of one body.
 template <class A>
@@ -254,7 +249,7 @@ __device__ __forceinline__ void atom_velocities(const DevSys& S, const DevBuf& B
 template <int KIND, bool EXACT>
 __global__ void __launch_bounds__(kThreads) step_kernel_d(DevSys S, DevBuf B, double dt) {
     constexpr int P = PREC_DOUBLE;
-    constexpr int TA = Tr<P>::kTA, TB = kTileBodies;
+    constexpr int TA = kTileAtomsD, TB = kTileBodies;
     if ((int)blockIdx.x >= S.n_body_tiles) {
         free_atom_tile<P, KIND>(S, B, dt, (int)blockIdx.x - S.n_body_tiles);
         return;
@@ -333,54 +328,109 @@ __global__ void __launch_bounds__(kThreads) step_kernel_d(DevSys S, DevBuf B, do
 
 // ------------------------------------------------------------------------------------------
 // Single and mixed precision: FP32 arithmetic, float-float body state, rotation increments.
+// One 256-thread CTA per tile (<= 256 bodies, <= 1024 body atoms), 3 CTAs per SM. Each body's
+// rotation matrix is formed once per phase and kept in shared memory, so the per-atom rebuild
+// delta = At(q) d costs 9 FMAs.
 // ------------------------------------------------------------------------------------------
+struct FSmem {
+    static constexpr int TA = kTileAtomsF, TB = kTileBodiesF;
+    static constexpr int SF = 0;              // 3 x TA: F
+    static constexpr int ST = SF + 3 * TA;    // 3 x TA: torque
+    static constexpr int SX = ST + 3 * TA;    // 3 x TA: d (part1, fused) or delta (part2)
+    static constexpr int SM = SX + 3 * TA;    // 9 x TB: rotation matrix At(q), row-major per body
+    static constexpr int SR = SM + 9 * TB;    // 6 x TB: COM (hi, lo) or COM velocity (double)
+    static constexpr int SW = SR + 6 * TB;    // 3 x TB: space-frame omega (part2)
+    static constexpr int SB = SW + 3 * TB;    // TA ushort: atom -> tile body
+    static constexpr int WORDS = SB + TA / 2;
+};
+
+// At(q) as a row-major 3x3 matrix (homogeneous quadratic form, equal to Ct(q, B(q, .))).
+__device__ __forceinline__ void rotation_matrix(Q4<float> q, float* m) {
+    const float ww = q.w * q.w, xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z;
+    const float xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z, wx = q.w * q.x, wy = q.w * q.y, wz = q.w * q.z;
+    m[0] = ww + xx - yy - zz; m[1] = 2.0f * (xy - wz); m[2] = 2.0f * (xz + wy);
+    m[3] = 2.0f * (xy + wz); m[4] = ww - xx + yy - zz; m[5] = 2.0f * (yz - wx);
+    m[6] = 2.0f * (xz - wy); m[7] = 2.0f * (yz + wx); m[8] = ww - xx - yy + zz;
+}
+__device__ __forceinline__ V3<float> mat_vec(const float* m, V3<float> d) {
+    return v3<float>(fmaf(m[0], d.x, fmaf(m[1], d.y, m[2] * d.z)), fmaf(m[3], d.x, fmaf(m[4], d.y, m[5] * d.z)),
+                     fmaf(m[6], d.x, fmaf(m[7], d.y, m[8] * d.z)));
+}
+
 template <int P, int KIND, bool EXACT>
-__global__ void __launch_bounds__(kThreads, 4) step_kernel_f(DevSys S, DevBuf B, double dt_d) {
-    constexpr int TA = Tr<P>::kTA, TB = kTileBodies;
+__global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B, double dt_d) {
+    constexpr int TA = kTileAtomsF;
+    constexpr int APT = TA / kThreadsF;
     if ((int)blockIdx.x >= S.n_body_tiles) {
         free_atom_tile<P, KIND>(S, B, dt_d, (int)blockIdx.x - S.n_body_tiles);
         return;
     }
-    extern __shared__ __align__(16) unsigned char smem[];
-    StepSmem<float> sm;
-    sm.carve<TA, TB>(smem);
+    extern __shared__ __align__(16) float fsm[];
+    float* sF = fsm + FSmem::SF;
+    float* sT = fsm + FSmem::ST;
+    float* sX = fsm + FSmem::SX;
+    float* sM = fsm + FSmem::SM;
+    float* sR = fsm + FSmem::SR;
+    float* sW = fsm + FSmem::SW;
+    unsigned short* sBody = (unsigned short*)(fsm + FSmem::SB);
     const int tid = threadIdx.x;
     const int b0 = __ldg(S.tile_body0 + blockIdx.x), b1 = __ldg(S.tile_body0 + blockIdx.x + 1);
     const int nbt = b1 - b0;
     const int a0 = __ldg(S.atom0 + b0), nat = __ldg(S.atom0 + b1) - a0;
     const int nbp = S.nb_pad;
-    float* __restrict__ hi = (float*)S.state;  // rows 0..13
-    float* __restrict__ lo = hi + 14 * nbp;    // rows 14..27
+    float* __restrict__ ghi = (float*)S.state;  // state rows 0..13 (hi)
+    float* __restrict__ glo = ghi + 14 * nbp;   // rows 14..27 (lo)
     const float dt = (float)dt_d;
 
-    // Phase 0: orientation into shared memory, the rest of the body record prefetched into L2
-    // (loaded after the atom phase, keeping registers free for the atom gathers).
+    // Phase 0: rotation matrix of the current orientation; atoms -> tile-local body
     if (tid < nbt) {
         const int b = b0 + tid;
-#pragma unroll
-        for (int c = 0; c < 4; c++) sm.sQ[4 * tid + c] = hi[b + (6 + c) * nbp];
-#pragma unroll
-        for (int c = 0; c < 14; c++) {
-            if (c < 6 || c > 9) prefetch_l2(hi + b + c * nbp);
-            prefetch_l2(lo + b + c * nbp);
-        }
-#pragma unroll
-        for (int c = 0; c < kBconstRows; c++) prefetch_l2(S.bconst + b + c * nbp);
-        const int s = __ldg(S.atom0 + b) - a0, e = __ldg(S.atom0 + b + 1) - a0;
-        for (int j = s; j < e; j++) sm.sBody[j] = (unsigned short)tid;
+        rotation_matrix(q4<float>(ghi[b + 6 * nbp], ghi[b + 7 * nbp], ghi[b + 8 * nbp], ghi[b + 9 * nbp]), sM + 9 * tid);
+        const int s0 = __ldg(S.atom0 + b) - a0, e0 = __ldg(S.atom0 + b + 1) - a0;
+        for (int j = s0; j < e0; j++) sBody[j] = (unsigned short)tid;
     }
     __syncthreads();
-    atom_forces<P, KIND, float, float>(S, B, sm, a0, nat);
+
+    // Phase 1: per-atom force, displacement from the COM, torque (all loads issued first)
+    {
+        const float* __restrict__ dg = (const float*)S.d;
+        int loc[APT];
+        V3<float> F[APT], d[APT];
+#pragma unroll
+        for (int i = 0; i < APT; i++) {
+            const int a = tid + i * kThreadsF;
+            loc[i] = a < nat ? __ldg(S.atom_loc + a0 + a) : 0;
+        }
+#pragma unroll
+        for (int i = 0; i < APT; i++) {
+            const int a = tid + i * kThreadsF;
+            if (a < nat) {
+                const int k = a0 + a;
+                d[i] = v3<float>(__ldg(dg + k), __ldg(dg + k + S.nba_pad), __ldg(dg + k + 2 * S.nba_pad));
+                F[i] = load_force<float>(B.force, loc[i], B.stride);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < APT; i++) {
+            const int a = tid + i * kThreadsF;
+            if (a < nat) {
+                const V3<float> delta = mat_vec(sM + 9 * sBody[a], d[i]);
+                const V3<float> tau = cross(delta, F[i]);
+                sF[3 * a] = F[i].x; sF[3 * a + 1] = F[i].y; sF[3 * a + 2] = F[i].z;
+                sT[3 * a] = tau.x; sT[3 * a + 1] = tau.y; sT[3 * a + 2] = tau.z;
+                const V3<float> x = KIND == STEP_PART2 ? delta : d[i];
+                sX[3 * a] = x.x; sX[3 * a + 1] = x.y; sX[3 * a + 2] = x.z;
+            }
+        }
+    }
     __syncthreads();
 
-    // Phase 2: kicks, drift and rotation on the float-float state.
+    // Phase 2: kicks, drift and rotation on the float-float state
     if (tid < nbt) {
         const int b = b0 + tid;
         ff x[14];
 #pragma unroll
-        for (int c = 0; c < 14; c++) x[c] = ff{hi[b + c * nbp], lo[b + c * nbp]};
-        V3<float> Fa, Ta;
-        body_sums(sm, __ldg(S.atom0 + b) - a0, __ldg(S.atom0 + b + 1) - a0, Fa, Ta);
+        for (int c = 0; c < 14; c++) x[c] = ff{ghi[b + c * nbp], glo[b + c * nbp]};
         const float* bc = S.bconst;
         const float invm = __ldg(bc + b), invm_lo = __ldg(bc + b + 7 * nbp);
         Rotor R;
@@ -389,82 +439,99 @@ __global__ void __launch_bounds__(kThreads, 4) step_kernel_f(DevSys S, DevBuf B,
         R.g12 = __ldg(bc + b + 5 * nbp);
         R.g02 = __ldg(bc + b + 6 * nbp);
         R.invI_lo = v3<float>(__ldg(bc + b + 8 * nbp), __ldg(bc + b + 9 * nbp), __ldg(bc + b + 10 * nbp));
-        const Q4<float> qh = q4<float>(x[6].hi, x[7].hi, x[8].hi, x[9].hi);
-        const Q4<float> Ctau = qC(qh, Ta) * dt;              // pi kick, full dt (RigidBodySystem.cpp:179)
-        const float hdt = 0.5f * dt;                         // COM velocity half kick, 1/m as hi + lo
-        const V3<float> dv = v3<float>(fmaf(Fa.x, invm_lo * hdt, Fa.x * (invm * hdt)),
-                                       fmaf(Fa.y, invm_lo * hdt, Fa.y * (invm * hdt)),
-                                       fmaf(Fa.z, invm_lo * hdt, Fa.z * (invm * hdt)));
-        const int kicks = KIND == STEP_FUSED ? 2 : 1;
-        for (int kk = 0; kk < kicks; kk++) {
-            x[3] = ff_add(x[3], dv.x); x[4] = ff_add(x[4], dv.y); x[5] = ff_add(x[5], dv.z);
-            x[10] = ff_add(x[10], Ctau.w); x[11] = ff_add(x[11], Ctau.x);
-            x[12] = ff_add(x[12], Ctau.y); x[13] = ff_add(x[13], Ctau.z);
+        V3<float> Fa = v3<float>(0.f, 0.f, 0.f), Ta = Fa;
+        {
+            const int s0 = __ldg(S.atom0 + b) - a0, e0 = __ldg(S.atom0 + b + 1) - a0;
+            for (int j = s0; j < e0; j++) {
+                Fa = Fa + v3<float>(sF[3 * j], sF[3 * j + 1], sF[3 * j + 2]);
+                Ta = Ta + v3<float>(sT[3 * j], sT[3 * j + 1], sT[3 * j + 2]);
+            }
         }
+        const Q4<float> qh = q4<float>(x[6].hi, x[7].hi, x[8].hi, x[9].hi);
+        // half kicks: COM velocity by F/m dt/2 (1/m as hi + lo), pi by C(q, tau) dt
+        // (RigidBodySystem.cpp:178-179, :200-201); the fused step applies both halves at once
+        const float kick = KIND == STEP_FUSED ? dt : 0.5f * dt;
+        const float piscale = KIND == STEP_FUSED ? 2.0f * dt : dt;
+        const Q4<float> Ctau = qC(qh, Ta) * piscale;
+        x[3] = ff_acc(x[3], fmaf(Fa.x, invm_lo * kick, Fa.x * (invm * kick)));
+        x[4] = ff_acc(x[4], fmaf(Fa.y, invm_lo * kick, Fa.y * (invm * kick)));
+        x[5] = ff_acc(x[5], fmaf(Fa.z, invm_lo * kick, Fa.z * (invm * kick)));
+        x[10] = ff_acc(x[10], Ctau.w); x[11] = ff_acc(x[11], Ctau.x);
+        x[12] = ff_acc(x[12], Ctau.y); x[13] = ff_acc(x[13], Ctau.z);
         const Q4<float> ph = q4<float>(x[10].hi, x[11].hi, x[12].hi, x[13].hi);
         if (KIND == STEP_PART2) {
-            V3<float> ws = rotate_to_space(qh, mul(R.invI, qBt(qh, ph)) * 0.5f);
-            sm.sRb[3 * tid] = (double)x[3].hi + (double)x[3].lo;
-            sm.sRb[3 * tid + 1] = (double)x[4].hi + (double)x[4].lo;
-            sm.sRb[3 * tid + 2] = (double)x[5].hi + (double)x[5].lo;
-            sm.sW[3 * tid] = ws.x; sm.sW[3 * tid + 1] = ws.y; sm.sW[3 * tid + 2] = ws.z;
+            const V3<float> ws = rotate_to_space(qh, mul(R.invI, qBt(qh, ph)) * 0.5f);
+            double* v = (double*)(sR + 6 * tid);
+            v[0] = (double)x[3].hi + (double)x[3].lo;
+            v[1] = (double)x[4].hi + (double)x[4].lo;
+            v[2] = (double)x[5].hi + (double)x[5].lo;
+            sW[3 * tid] = ws.x; sW[3 * tid + 1] = ws.y; sW[3 * tid + 2] = ws.z;
         } else {
-            // drift
 #pragma unroll
-            for (int c = 0; c < 3; c++) x[c] = ff_add(x[c], fmaf(x[3 + c].hi, dt, x[3 + c].lo * dt));
-            // free rotation as an increment of q and pi
+            for (int c = 0; c < 3; c++) x[c] = ff_acc(x[c], fmaf(x[3 + c].hi, dt, x[3 + c].lo * dt));  // drift
             const V3<float> L = qBt(qh, ph) * 0.5f;
             Q4<float> dr;
             if (EXACT) dr = dq_exact(__ldg(S.cls + b), L, R, dt);
             else dr = nosquish_increment(L, R, R.invI.z != 0.0f, dt, S.rot_n);
             const Q4<float> dq = qmul(qh, dr), dp = qmul(ph, dr);
-            x[6] = ff_add(x[6], dq.w); x[7] = ff_add(x[7], dq.x); x[8] = ff_add(x[8], dq.y); x[9] = ff_add(x[9], dq.z);
-            x[10] = ff_add(x[10], dp.w); x[11] = ff_add(x[11], dp.x);
-            x[12] = ff_add(x[12], dp.y); x[13] = ff_add(x[13], dp.z);
+            x[6] = ff_acc(x[6], dq.w); x[7] = ff_acc(x[7], dq.x); x[8] = ff_acc(x[8], dq.y); x[9] = ff_acc(x[9], dq.z);
+            x[10] = ff_acc(x[10], dp.w); x[11] = ff_acc(x[11], dp.x);
+            x[12] = ff_acc(x[12], dp.y); x[13] = ff_acc(x[13], dp.z);
             // renormalise q: eps = |q|^2 - 1 from exact squares, q <- q (1 - eps/2)
+#pragma unroll
+            for (int c = 6; c < 10; c++) x[c] = ff_norm(x[c]);
             ff n2 = ff{0.0f, 0.0f};
             float tail = 0.0f;
 #pragma unroll
             for (int c = 6; c < 10; c++) {
-                float p = x[c].hi * x[c].hi;
+                const float p = x[c].hi * x[c].hi;
                 tail += fmaf(x[c].hi, x[c].hi, -p) + 2.0f * x[c].hi * x[c].lo;
-                n2 = ff_add(n2, p);
+                n2 = ff_acc(n2, p);
             }
             const float eps = ((n2.hi - 1.0f) + n2.lo) + tail;
 #pragma unroll
-            for (int c = 6; c < 10; c++) x[c] = ff_add(x[c], -0.5f * eps * x[c].hi);
+            for (int c = 6; c < 10; c++) x[c] = ff_acc(x[c], -0.5f * eps * x[c].hi);
 #pragma unroll
-            for (int c = 0; c < 3; c++) {  // COM as float-float pairs in the double slots
-                ((float*)(sm.sRb + 3 * tid))[2 * c] = x[c].hi;
-                ((float*)(sm.sRb + 3 * tid))[2 * c + 1] = x[c].lo;
+            for (int c = 0; c < 3; c++) {
+                x[c] = ff_norm(x[c]);
+                sR[6 * tid + 2 * c] = x[c].hi;
+                sR[6 * tid + 2 * c + 1] = x[c].lo;
             }
-#pragma unroll
-            for (int c = 0; c < 4; c++) sm.sQ[4 * tid + c] = x[6 + c].hi;
+            rotation_matrix(q4<float>(x[6].hi, x[7].hi, x[8].hi, x[9].hi), sM + 9 * tid);
         }
 #pragma unroll
         for (int c = 0; c < 14; c++) {
-            hi[b + c * nbp] = x[c].hi;
-            lo[b + c * nbp] = x[c].lo;
+            const ff y = ff_norm(x[c]);
+            ghi[b + c * nbp] = y.hi;
+            glo[b + c * nbp] = y.lo;
         }
     }
     __syncthreads();
 
-    // Phase 3
-    if (KIND == STEP_PART2) {
-        atom_velocities<P, float>(S, B, sm, a0, nat);
-    } else {
-        for (int a = tid; a < nat; a += kThreads) {
-            const int t = sm.sBody[a];
-            const int loc = __ldg(S.atom_loc + a0 + a);
-            Q4<float> q = q4<float>(sm.sQ[4 * t], sm.sQ[4 * t + 1], sm.sQ[4 * t + 2], sm.sQ[4 * t + 3]);
-            V3<float> delta = rotate_to_space(q, v3<float>(sm.sX[3 * a], sm.sX[3 * a + 1], sm.sX[3 * a + 2]));
-            const float* rf = (const float*)(sm.sRb + 3 * t);
-            // posq.w (the charge) is left untouched: x, y written as one 8-byte store, z as 4 bytes
+    // Phase 3: positions (part1, fused) or velocities (part2)
+    for (int a = tid; a < nat; a += kThreadsF) {
+        const int t = sBody[a];
+        const int loc = __ldg(S.atom_loc + a0 + a);
+        const V3<float> x = v3<float>(sX[3 * a], sX[3 * a + 1], sX[3 * a + 2]);
+        if (KIND == STEP_PART2) {
+            using V4 = typename Tr<P>::V4;
+            const V3<float> rel = cross(v3<float>(sW[3 * t], sW[3 * t + 1], sW[3 * t + 2]), x);
+            const double* v = (const double*)(sR + 6 * t);
+            V4* vel = (V4*)B.velm;
+            V4 vm = vel[loc];
+            vm.x = v[0] + (double)rel.x;
+            vm.y = v[1] + (double)rel.y;
+            vm.z = v[2] + (double)rel.z;
+            vel[loc] = vm;
+        } else {
+            const V3<float> delta = mat_vec(sM + 9 * t, x);
+            const float* rf = sR + 6 * t;
+            // posq.w (the charge) is left untouched: x, y in one 8-byte store, z in 4 bytes
             float* pq = (float*)B.posq + 4 * (size_t)loc;
             if (P == PREC_MIXED) {
-                ff px = ff_add(ff{rf[0], rf[1]}, delta.x);
-                ff py = ff_add(ff{rf[2], rf[3]}, delta.y);
-                ff pz = ff_add(ff{rf[4], rf[5]}, delta.z);
+                const ff px = ff_add(ff{rf[0], rf[1]}, delta.x);
+                const ff py = ff_add(ff{rf[2], rf[3]}, delta.y);
+                const ff pz = ff_add(ff{rf[4], rf[5]}, delta.z);
                 *(float2*)pq = make_float2(px.hi, py.hi);
                 pq[2] = pz.hi;
                 ((float4*)B.corr)[loc] = make_float4(px.lo, py.lo, pz.lo, 0.0f);
@@ -612,13 +679,9 @@ __global__ void store_positions_kernel(DevBuf B, const int* __restrict__ loc, in
 // ------------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------------
-size_t step_smem_bytes(int prec) {
-    switch (prec) {
-        case PREC_SINGLE: return step_smem<PREC_SINGLE>();
-        case PREC_MIXED: return step_smem<PREC_MIXED>();
-        default: return step_smem<PREC_DOUBLE>();
-    }
-}
+constexpr size_t step_smem_f() { return (size_t)FSmem::WORDS * 4; }
+
+size_t step_smem_bytes(int prec) { return prec == PREC_DOUBLE ? step_smem_d() : step_smem_f(); }
 
 template <int P, int KIND, bool EXACT> struct StepKernel {
     static constexpr auto fn() { return step_kernel_f<P, KIND, EXACT>; }
@@ -630,16 +693,26 @@ template <int KIND, bool EXACT> struct StepKernel<PREC_DOUBLE, KIND, EXACT> {
 template <int P, int KIND, bool EXACT>
 static int launch_step_t(const DevSys& s, const DevBuf& b, double dt, cudaStream_t stream) {
     static bool configured = false;
-    const size_t smem = step_smem<P>();
+    static int wave = 0;  // resident CTAs of one full wave (float kernels are persistent)
+    const size_t smem = P == PREC_DOUBLE ? step_smem_d() : step_smem_f();
+    const int threads = P == PREC_DOUBLE ? kThreads : kThreadsF;
     auto kernel = StepKernel<P, KIND, EXACT>::fn();
     if (!configured) {
         if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
             return -1;
+        int dev = 0, sms = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess)
+            return -1;
+        wave = sms * (per_sm > 0 ? per_sm : 1);
         configured = true;
     }
-    const int grid = s.n_body_tiles + s.n_free_tiles;
-    if (grid == 0) return 0;
-    kernel<<<grid, kThreads, smem, stream>>>(s, b, dt);
+    const int tiles = s.n_body_tiles + s.n_free_tiles;
+    if (tiles == 0) return 0;
+    const int grid = tiles;
+    (void)wave;
+    kernel<<<grid, threads, smem, stream>>>(s, b, dt);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
