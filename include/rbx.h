@@ -73,7 +73,10 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
 int rbx_destroy(rbx_integrator* h);
 
 /* Map user atom i -> device slot location[i] (OpenMM atom reordering; replaces the
- * ReorderListener's atomLocation rebuild, CudaRigidBodyKernels.cpp:69-113). */
+ * ReorderListener's atomLocation rebuild, CudaRigidBodyKernels.cpp:69-113). The library keeps
+ * its device arrays with bodies ordered by the lowest slot of their atoms (so that a CTA's
+ * atoms occupy a narrow slot range); this call re-plans that order and moves the device body
+ * state to it exactly, at a host cost of O(n log n) plus one copy of the body state each way. */
 int rbx_set_atom_locations(rbx_integrator* h, const int* location);
 
 /*
@@ -115,11 +118,12 @@ int rbx_integrate_fused(rbx_integrator* h, void* stream, const rbx_buffers* buf,
 int rbx_kinetic_energies(rbx_integrator* h, void* stream, const rbx_buffers* buf, double* out2);
 
 /*
- * Body state exchange for tests and checkpoints, host arrays in the library's body order
- * (bodies sorted by atom count, ties in order of first appearance):
+ * Body state exchange for tests and checkpoints, host arrays with bodies in the reference's
+ * order (ascending body index, as RigidBodySystem numbers them; RigidBodySystem.cpp:28-49):
  *   state [num_bodies*14]: r[3], v[3], q[4], pi[4] per body (v = centre-of-mass velocity)
  *   geometry [num_bodies*3] principal moments I (descending; I[2] = 0 for a linear body)
- * rbx_get_body_atoms gives, for body-atom k in the library order, the user atom index.
+ * rbx_get_body_atoms gives the first body atom of each body [nb+1] and, for body-atom k, the
+ * user atom index [nba], in the same order; body_fixed follows that atom order.
  */
 int rbx_get_body_state(rbx_integrator* h, double* state);
 int rbx_set_body_state(rbx_integrator* h, const double* state);

@@ -81,18 +81,27 @@ struct rbx_integrator {
     int last_launches = 0;
     std::vector<double> masses;
     std::vector<int> location;          // user atom -> device slot
-    std::vector<int> free_atoms;        // user index of each free atom
-    std::vector<int> body_first;        // [nb+1] first body atom (library order)
-    std::vector<int> body_atoms;        // [nba] user index of each body atom
-    std::vector<int> tile_body0;        // [n_body_tiles+1]
-    std::vector<double> I;              // [nb*3] principal moments (host copy)
-    std::vector<double> dfix;           // [nba*3] body-frame positions (host copy)
+    std::vector<int> free_atoms;        // user index of each free atom, in device-slot order
+    // Bodies in the reference's order (ascending body index, RigidBodySystem.cpp:28-49); every
+    // host copy of per-body data is kept in this order.
+    std::vector<int> ref_first;         // [nb+1] first body atom of each body
+    std::vector<int> ref_atoms;         // [nba] user index of each body atom
+    std::vector<double> I;              // [nb*3] principal moments
+    std::vector<double> dfix;           // [nba*3] body-frame positions, ref_atoms order
+    std::vector<double> invm, invI;     // [nb], [nb*3]
     std::vector<uint8_t> cls;           // [nb]
     std::vector<int> dof;               // [nb]
+    // Library order, the order of every device array: bodies by the lowest device slot of their
+    // atoms, so that a tile's atoms occupy a narrow slot range. Re-planned when slots change.
+    std::vector<int> lib_body;          // [nb] library position -> reference body
+    std::vector<int> lib_pos;           // [nb] reference body -> library position
+    std::vector<int> body_first;        // [nb+1] first body atom (library order)
+    std::vector<int> body_atoms;        // [nba] user index of each body atom (library order)
+    std::vector<int> tile_body0;        // [n_body_tiles+1]
 
     DevArray<double> d_state, d_invm, d_invI;  // d_state holds FP64 rows or float-float rows
     DevArray<float> d_bconst;                   // single/mixed: 11 rows (see kBconstRows)
-    DevArray<int> d_atom0, d_atom_loc, d_free_loc, d_tiles, d_tile_loc0;
+    DevArray<int> d_atom0, d_atom_loc, d_free_loc, d_tiles;
     DevArray<uint8_t> d_cls;
     DevArray<unsigned char> d_fixed;  // float or double SoA
     DevArray<double> d_ke_partial, d_ke_out;
@@ -113,7 +122,6 @@ struct rbx_integrator {
         s.state = d_state.p; s.invm = d_invm.p; s.invI = d_invI.p; s.bconst = d_bconst.p;
         s.atom0 = d_atom0.p; s.cls = d_cls.p;
         s.d = d_fixed.p; s.atom_loc = d_atom_loc.p; s.free_loc = d_free_loc.p; s.tile_body0 = d_tiles.p;
-        s.tile_loc0 = d_tile_loc0.p;
         return s;
     }
     ~rbx_integrator() {
@@ -338,26 +346,103 @@ template <class T> int upload(DevArray<T>& a, const std::vector<T>& h) {
     return RBX_OK;
 }
 
-int upload_maps(rbx_integrator* h) {
+// Library order and tiles. Bodies are ordered by the lowest device slot of their atoms (stable,
+// ties by body index) and free atoms by their slot, so that consecutive threads of a tile touch
+// neighbouring slots of the force, position and velocity buffers. A tile is a run of
+// consecutive bodies under the per-CTA body and atom limits (rbx_create has rejected any body
+// larger than one tile).
+void plan_order(rbx_integrator* h) {
+    const int nb = h->nb;
+    std::vector<int> key(nb);
+    for (int b = 0; b < nb; b++) {
+        int k = h->location[h->ref_atoms[h->ref_first[b]]];
+        for (int a = h->ref_first[b] + 1; a < h->ref_first[b + 1]; a++) k = std::min(k, h->location[h->ref_atoms[a]]);
+        key[b] = k;
+    }
+    h->lib_body.resize(nb);
+    for (int b = 0; b < nb; b++) h->lib_body[b] = b;
+    std::stable_sort(h->lib_body.begin(), h->lib_body.end(), [&](int a, int b) { return key[a] < key[b]; });
+    h->lib_pos.resize(nb);
+    h->body_first.assign(1, 0);
+    h->body_atoms.clear();
+    for (int L = 0; L < nb; L++) {
+        const int b = h->lib_body[L];
+        h->lib_pos[b] = L;
+        for (int a = h->ref_first[b]; a < h->ref_first[b + 1]; a++) h->body_atoms.push_back(h->ref_atoms[a]);
+        h->body_first.push_back((int)h->body_atoms.size());
+    }
+    std::stable_sort(h->free_atoms.begin(), h->free_atoms.end(),
+                     [&](int a, int b) { return h->location[a] < h->location[b]; });
+    const int TA = tile_atoms(h->prec), TB = tile_bodies(h->prec);
+    h->tile_body0.assign(1, 0);
+    for (int b = 0; b < nb;) {
+        int atoms = 0, cnt = 0;
+        while (b < nb && cnt < TB && atoms + (h->body_first[b + 1] - h->body_first[b]) <= TA) {
+            atoms += h->body_first[b + 1] - h->body_first[b];
+            cnt++;
+            b++;
+        }
+        h->tile_body0.push_back(b);
+    }
+    h->n_body_tiles = (int)h->tile_body0.size() - 1;
+    h->n_free_tiles = (h->nf + free_per_tile(h->prec) - 1) / free_per_tile(h->prec);
+}
+
+// Device copies of the library order: first atom of each body, tiles and device slots.
+int upload_layout(rbx_integrator* h) {
     std::vector<int> atom_loc(h->nba), free_loc(h->nf);
     for (int k = 0; k < h->nba; k++) atom_loc[k] = h->location[h->body_atoms[k]];
     for (int j = 0; j < h->nf; j++) free_loc[j] = h->location[h->free_atoms[j]];
-    // Per body tile: the first device slot when the tile's atoms occupy consecutive slots (its
-    // force and position ranges can then be prefetched in bulk), otherwise -1.
-    std::vector<int> tile_loc0(std::max(h->n_body_tiles, 1), -1);
-    for (int t = 0; t < h->n_body_tiles; t++) {
-        const int a0 = h->body_first[h->tile_body0[t]], a1 = h->body_first[h->tile_body0[t + 1]];
-        bool contiguous = a1 > a0;
-        for (int k = a0 + 1; contiguous && k < a1; k++) contiguous = atom_loc[k] == atom_loc[k - 1] + 1;
-        tile_loc0[t] = contiguous ? atom_loc[a0] : -1;
+    int rc = upload(h->d_atom0, h->body_first);
+    if (!rc) rc = upload(h->d_tiles, h->tile_body0);
+    if (!rc) rc = upload(h->d_atom_loc, atom_loc);
+    if (!rc) rc = upload(h->d_free_loc, free_loc);
+    if (!rc) rc = upload(h->c_loc, h->location);
+    return rc;
+}
+
+// Device copies of the body constants in the library order: 1/m and 1/I (FP64 for double;
+// float-float for single and mixed, with the moment gaps formed in FP64 so that they keep their
+// relative accuracy for nearly degenerate tops), rotation classes and body-frame positions.
+int upload_bodies(rbx_integrator* h) {
+    const int nb = h->nb, nbp = h->nb_pad, nbap = h->nba_pad;
+    if (h->prec == PREC_DOUBLE) {
+        std::vector<double> invm(std::max(nb, 1), 0.0), invI((size_t)3 * nbp, 0.0);
+        for (int L = 0; L < nb; L++) {
+            const int b = h->lib_body[L];
+            invm[L] = h->invm[b];
+            for (int k = 0; k < 3; k++) invI[L + (size_t)k * nbp] = h->invI[3 * b + k];
+        }
+        CUDA_TRY(cudaMemcpy(h->d_invm.p, invm.data(), invm.size() * sizeof(double), cudaMemcpyHostToDevice));
+        CUDA_TRY(cudaMemcpy(h->d_invI.p, invI.data(), invI.size() * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> bconst((size_t)kBconstRows * nbp, 0.0f);
+        for (int L = 0; L < nb; L++) {
+            const int b = h->lib_body[L];
+            const double* I = &h->I[3 * b];
+            const double cst[7] = {h->invm[b], h->invI[3 * b], h->invI[3 * b + 1], h->invI[3 * b + 2],
+                                   I[0] - I[1], I[1] - I[2], I[0] - I[2]};
+            for (int k = 0; k < 7; k++) bconst[L + (size_t)k * nbp] = (float)cst[k];
+            for (int k = 0; k < 4; k++) bconst[L + (size_t)(7 + k) * nbp] = (float)(cst[k] - (double)(float)cst[k]);
+        }
+        CUDA_TRY(cudaMemcpy(h->d_bconst.p, bconst.data(), bconst.size() * sizeof(float), cudaMemcpyHostToDevice));
     }
-    int rc = upload(h->d_atom_loc, atom_loc);
-    if (rc) return rc;
-    rc = upload(h->d_tile_loc0, tile_loc0);
-    if (rc) return rc;
-    rc = upload(h->d_free_loc, free_loc);
-    if (rc) return rc;
-    return upload(h->c_loc, h->location);
+    std::vector<uint8_t> cls(std::max(nb, 1), 0);
+    for (int L = 0; L < nb; L++) cls[L] = h->cls[h->lib_body[L]];
+    CUDA_TRY(cudaMemcpy(h->d_cls.p, cls.data(), cls.size(), cudaMemcpyHostToDevice));
+    std::vector<double> d((size_t)3 * nbap, 0.0);
+    for (int L = 0; L < nb; L++) {
+        const int b = h->lib_body[L];
+        for (int j = 0; j < h->ref_first[b + 1] - h->ref_first[b]; j++)
+            for (int c = 0; c < 3; c++) d[h->body_first[L] + j + (size_t)c * nbap] = h->dfix[3 * (size_t)(h->ref_first[b] + j) + c];
+    }
+    if (h->prec == PREC_DOUBLE) {
+        CUDA_TRY(cudaMemcpy(h->d_fixed.p, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> f(d.begin(), d.end());
+        CUDA_TRY(cudaMemcpy(h->d_fixed.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    return RBX_OK;
 }
 
 int check(const rbx_integrator* h) {
@@ -443,49 +528,32 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
         if (in_body) members[compact[id]].push_back(i);
         else h->free_atoms.push_back(i);
     }
-    // Library order: bodies by ascending size, ties by compacted id (stable).
-    std::vector<int> order(nb);
-    for (int b = 0; b < nb; b++) order[b] = b;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return members[a].size() < members[b].size(); });
     h->nb = nb;
     h->nf = (int)h->free_atoms.size();
-    h->body_first.assign(1, 0);
-    for (int b : order) {
-        for (int i : members[b]) h->body_atoms.push_back(i);
-        h->body_first.push_back((int)h->body_atoms.size());
-    }
-    h->nba = (int)h->body_atoms.size();
-    // Tiles of consecutive bodies under the per-CTA body and atom limits.
-    const int TA = tile_atoms(precision);
-    h->tile_body0.assign(1, 0);
-    for (int b = 0; b < nb;) {
-        int atoms = 0, cnt = 0;
-        int n0 = h->body_first[b + 1] - h->body_first[b];
-        if (n0 > TA) {
+    h->ref_first.assign(1, 0);
+    for (int b = 0; b < nb; b++) {
+        if ((int)members[b].size() > tile_atoms(precision)) {
             delete h;
-            return fail(RBX_ERR_UNSUPPORTED, "a rigid body of %d atoms exceeds the %d-atom tile of this build", n0, TA);
+            return fail(RBX_ERR_UNSUPPORTED, "a rigid body of %d atoms exceeds the %d-atom tile of this build",
+                        (int)members[b].size(), tile_atoms(precision));
         }
-        while (b < nb && cnt < tile_bodies(precision) && atoms + (h->body_first[b + 1] - h->body_first[b]) <= TA) {
-            atoms += h->body_first[b + 1] - h->body_first[b];
-            cnt++;
-            b++;
-        }
-        h->tile_body0.push_back(b);
+        for (int i : members[b]) h->ref_atoms.push_back(i);
+        h->ref_first.push_back((int)h->ref_atoms.size());
     }
-    h->n_body_tiles = (int)h->tile_body0.size() - 1;
-    h->n_free_tiles = (h->nf + free_per_tile(precision) - 1) / free_per_tile(precision);
+    h->nba = (int)h->ref_atoms.size();
+    plan_order(h);
     h->nb_pad = ((std::max(nb, 1) + 31) / 32) * 32;
     h->nba_pad = ((std::max(h->nba, 1) + 31) / 32) * 32;
     h->I.assign((size_t)nb * 3, 0.0);
     h->dfix.assign((size_t)h->nba * 3, 0.0);
+    h->invm.assign(nb, 0.0);
+    h->invI.assign((size_t)nb * 3, 0.0);
     h->cls.assign(nb, 0);
     h->dof.assign(nb, 6);
 
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) { delete h; return fail(RBX_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); }
-    int rc = upload(h->d_atom0, h->body_first);
-    if (!rc) rc = upload(h->d_tiles, h->tile_body0);
-    if (!rc) rc = upload_maps(h);
+    int rc = upload_layout(h);
     if (!rc && h->d_state.alloc((size_t)14 * h->nb_pad) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc body state");
     if (precision == PREC_DOUBLE) {
         if (!rc && h->d_invm.alloc(std::max(nb, 1)) != cudaSuccess) rc = fail(RBX_ERR_CUDA, "cudaMalloc invm");
@@ -534,7 +602,20 @@ int rbx_set_atom_locations(rbx_integrator* h, const int* location) {
     h->location.assign(location, location + h->natoms);
     h->max_location = *std::max_element(h->location.begin(), h->location.end());
     CUDA_TRY(cudaSetDevice(h->device));
-    return upload_maps(h);
+    // Re-plan the library order for the new slots and carry the body state (and constants)
+    // over to it; the raw rows are permuted, so the float-float state moves bit for bit.
+    const std::vector<int> old_pos = h->lib_pos;
+    plan_order(h);
+    if ((rc = upload_layout(h))) return rc;
+    if (!h->have_state || h->nb == 0 || old_pos == h->lib_pos) return RBX_OK;
+    const size_t rows = h->prec == PREC_DOUBLE ? 14 : 28, es = h->prec == PREC_DOUBLE ? 8 : 4, nbp = h->nb_pad;
+    std::vector<unsigned char> in(rows * nbp * es), out(rows * nbp * es, 0);
+    CUDA_TRY(cudaMemcpy(in.data(), h->d_state.p, in.size(), cudaMemcpyDeviceToHost));
+    for (size_t r = 0; r < rows; r++)
+        for (int L = 0; L < h->nb; L++)
+            std::memcpy(&out[(r * nbp + L) * es], &in[(r * nbp + old_pos[h->lib_body[L]]) * es], es);
+    CUDA_TRY(cudaMemcpy(h->d_state.p, out.data(), out.size(), cudaMemcpyHostToDevice));
+    return upload_bodies(h);
 }
 
 // Body state rows (14 per body, library order) -> device layout of the integrator's precision:
@@ -573,50 +654,27 @@ int rbx_upload_state(rbx_integrator* h, const double* positions, const double* v
     if (rc) return rc;
     if (!positions || !velocities) return fail(RBX_ERR_INVALID_ARGUMENT, "null positions or velocities");
     const int nb = h->nb, nbp = h->nb_pad;
-    std::vector<double> state((size_t)14 * nbp, 0.0), invm(std::max(nb, 1), 0.0), invI((size_t)3 * nbp, 0.0);
-    std::vector<float> bconst((size_t)kBconstRows * nbp, 0.0f);
-    h->ndof = h->nf;
+    std::vector<double> state((size_t)14 * nbp, 0.0);
+    int ndof = h->nf;
     for (int b = 0; b < nb; b++) {
-        const int f = h->body_first[b], N = h->body_first[b + 1] - f;
+        const int f = h->ref_first[b], N = h->ref_first[b + 1] - f;
         BodySetup s;
-        build_body(&h->body_atoms[f], N, h->masses.data(), positions, velocities, &h->dfix[3 * (size_t)f], s);
-        for (int k = 0; k < 3; k++) { h->I[3 * b + k] = s.I[k]; invI[b + (size_t)k * nbp] = s.invI[k]; }
+        build_body(&h->ref_atoms[f], N, h->masses.data(), positions, velocities, &h->dfix[3 * (size_t)f], s);
+        for (int k = 0; k < 3; k++) { h->I[3 * b + k] = s.I[k]; h->invI[3 * b + k] = s.invI[k]; }
+        h->invm[b] = s.invm;
         h->cls[b] = s.cls;
         h->dof[b] = s.dof;
-        h->ndof += s.dof;
-        invm[b] = s.invm;
-        // FP32 constants: 1/m and 1/I as float-float (rows 0-3 hi, 7-10 lo); the moment gaps are
-        // formed in FP64 so that they keep their relative accuracy for nearly degenerate tops.
-        const double gaps[3] = {s.I[0] - s.I[1], s.I[1] - s.I[2], s.I[0] - s.I[2]};
-        const double cst[7] = {s.invm, s.invI[0], s.invI[1], s.invI[2], gaps[0], gaps[1], gaps[2]};
-        for (int k = 0; k < 7; k++) bconst[b + (size_t)k * nbp] = (float)cst[k];
-        for (int k = 0; k < 4; k++) bconst[b + (size_t)(7 + k) * nbp] = (float)(cst[k] - (double)(float)cst[k]);
+        ndof += s.dof;
         double row[14] = {s.r.x, s.r.y, s.r.z, s.v.x, s.v.y, s.v.z, s.q.w, s.q.x, s.q.y, s.q.z, s.pi.w, s.pi.x, s.pi.y, s.pi.z};
-        for (int k = 0; k < 14; k++) state[b + (size_t)k * nbp] = row[k];
-        for (int k = 0; k < 14; k++)
+        for (int k = 0; k < 14; k++) {
             if (!std::isfinite(row[k])) return fail(RBX_ERR_NUMERIC, "non-finite rigid-body state for body %d", b);
+            state[h->lib_pos[b] + (size_t)k * nbp] = row[k];
+        }
     }
+    h->ndof = ndof;
     CUDA_TRY(cudaSetDevice(h->device));
     if ((rc = put_state(h, state))) return rc;
-    if (h->prec == PREC_DOUBLE) {
-        CUDA_TRY(cudaMemcpy(h->d_invm.p, invm.data(), invm.size() * sizeof(double), cudaMemcpyHostToDevice));
-        CUDA_TRY(cudaMemcpy(h->d_invI.p, invI.data(), invI.size() * sizeof(double), cudaMemcpyHostToDevice));
-    } else {
-        CUDA_TRY(cudaMemcpy(h->d_bconst.p, bconst.data(), bconst.size() * sizeof(float), cudaMemcpyHostToDevice));
-    }
-    if (nb) CUDA_TRY(cudaMemcpy(h->d_cls.p, h->cls.data(), nb, cudaMemcpyHostToDevice));
-    const int nbap = h->nba_pad;
-    if (h->prec == PREC_DOUBLE) {
-        std::vector<double> d((size_t)3 * nbap, 0.0);
-        for (int k = 0; k < h->nba; k++)
-            for (int c = 0; c < 3; c++) d[k + (size_t)c * nbap] = h->dfix[3 * (size_t)k + c];
-        CUDA_TRY(cudaMemcpy(h->d_fixed.p, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
-    } else {
-        std::vector<float> d((size_t)3 * nbap, 0.0f);
-        for (int k = 0; k < h->nba; k++)
-            for (int c = 0; c < 3; c++) d[k + (size_t)c * nbap] = (float)h->dfix[3 * (size_t)k + c];
-        CUDA_TRY(cudaMemcpy(h->d_fixed.p, d.data(), d.size() * sizeof(float), cudaMemcpyHostToDevice));
-    }
+    if ((rc = upload_bodies(h))) return rc;
     h->have_state = true;
     return RBX_OK;
 }
@@ -667,7 +725,7 @@ int rbx_get_body_state(rbx_integrator* h, double* state) {
     CUDA_TRY(cudaSetDevice(h->device));
     if ((rc = get_state(h, s))) return rc;
     for (int b = 0; b < h->nb; b++)
-        for (int k = 0; k < 14; k++) state[14 * (size_t)b + k] = s[b + (size_t)k * h->nb_pad];
+        for (int k = 0; k < 14; k++) state[14 * (size_t)b + k] = s[h->lib_pos[b] + (size_t)k * h->nb_pad];
     return RBX_OK;
 }
 
@@ -677,7 +735,7 @@ int rbx_set_body_state(rbx_integrator* h, const double* state) {
     if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body geometry: call rbx_upload_state first");
     std::vector<double> s((size_t)14 * h->nb_pad, 0.0);
     for (int b = 0; b < h->nb; b++)
-        for (int k = 0; k < 14; k++) s[b + (size_t)k * h->nb_pad] = state[14 * (size_t)b + k];
+        for (int k = 0; k < 14; k++) s[h->lib_pos[b] + (size_t)k * h->nb_pad] = state[14 * (size_t)b + k];
     CUDA_TRY(cudaSetDevice(h->device));
     return put_state(h, s);
 }
@@ -694,8 +752,8 @@ int rbx_get_body_geometry(rbx_integrator* h, double* moments, double* body_fixed
 int rbx_get_body_atoms(rbx_integrator* h, int* first_atom, int* atoms) {
     int rc = check(h);
     if (rc) return rc;
-    if (first_atom) std::memcpy(first_atom, h->body_first.data(), h->body_first.size() * sizeof(int));
-    if (atoms) std::memcpy(atoms, h->body_atoms.data(), h->body_atoms.size() * sizeof(int));
+    if (first_atom) std::memcpy(first_atom, h->ref_first.data(), h->ref_first.size() * sizeof(int));
+    if (atoms) std::memcpy(atoms, h->ref_atoms.data(), h->ref_atoms.size() * sizeof(int));
     return RBX_OK;
 }
 

@@ -8,7 +8,7 @@
 //   constants    double: invm [nb] + invI FP64 SoA 3 x nb_pad                   (32 B/body)
 //                single/mixed: FP32 SoA 11 x nb_pad: invm, invI.xyz, I0-I1, I1-I2, I0-I2, then
 //                the low parts of invm and invI.xyz (float-float)                  (44 B/body)
-//   atom0        int [nb+1]: first body atom of each body, bodies sorted by size  (4 B/body)
+//   atom0        int [nb+1]: first body atom of each body (library order)       (4 B/body)
 //   cls          uint8 [nb]: rotation class (rbx::RotClass)                      (1 B/body)
 //   d            body-frame atom positions, SoA 3 x nba_pad, float (single/mixed) or double
 //   atom_loc     int [nba]: device slot of each body atom (library order)
@@ -52,7 +52,6 @@ struct DevSys {
     const int* atom_loc;
     const int* free_loc;
     const int* tile_body0;
-    const int* tile_loc0;  // first device slot of a body tile whose atom slots are consecutive, else -1
 };
 
 struct DevBuf {

@@ -3,8 +3,8 @@
 // The step kernels serve the three step kinds (part1, part2, fused part2+part1) of the plugin's
 // integrateRigidBodyPart1/Part2 and freeAtomsDelta (platforms/cuda/src/kernels/
 // rigidbodyintegrator.cu:270-396). A CTA owns one tile: a run of bodies whose atoms are
-// contiguous in the library's body-atom order (bodies sorted by size so that a tile holds bodies
-// of one kind). Four phases, separated by __syncthreads:
+// contiguous in the library's body-atom order (bodies ordered by the lowest device slot of their
+// atoms, so that a tile's atoms occupy a narrow slot range). Four phases, separated by __syncthreads:
 //   0. one thread per body loads its state and stages its orientation, and marks its atoms
 //      with the tile-local body index in shared memory;
 //   1. one thread per atom gathers the fixed-point force, rebuilds the COM displacement

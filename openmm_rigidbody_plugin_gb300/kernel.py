@@ -83,6 +83,19 @@ class DeviceBuffers:
         for c in range(3):
             self.force[loc + c * self.stride] = fx[:, c]
 
+    def relocate(self, location):
+        """Move every atom's slot contents to its new slot, as OpenMM's atom reordering does
+        (posq, posqCorrection, velm and the three force components move together)."""
+        import torch
+        old = self._loc()
+        new = torch.as_tensor(np.asarray(location, dtype=np.int64), device=self.posq.device)
+        for a in (self.posq, self.corr, self.velm):
+            if a is not None:
+                a[new] = a[old].clone()
+        for c in range(3):
+            self.force[new + c * self.stride] = self.force[old + c * self.stride].clone()
+        self.location = np.asarray(location, dtype=np.int64)
+
     def get_positions(self):
         import torch
         loc = self._loc()

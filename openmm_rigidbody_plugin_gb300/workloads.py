@@ -152,17 +152,21 @@ def water_box(n_waters=512, seed=1, temperature=300.0, box=None):
 
 
 def mixed_system(n_bodies=1_000_000, n_free=100_000, fractions=(0.7, 0.2, 0.1), seed=3,
-                 temperature=300.0):
-    """Waters, tetrahedra and planar rings in the given fractions plus free LJ atoms."""
+                 temperature=300.0, grouped=False):
+    """Waters, tetrahedra and planar rings in the given fractions plus free LJ atoms.
+
+    The molecules sit on seeded random lattice sites either way; `grouped` lists them in the
+    atom order by kind (waters, tetrahedra, rings, then free atoms, as a PDB file usually lists
+    residues), otherwise the kinds are interleaved in a seeded random order."""
     rng = np.random.default_rng(seed)
     nw = int(round(fractions[0] * n_bodies))
     nt = int(round(fractions[1] * n_bodies))
     nr = n_bodies - nw - nt
     kinds = ["water"] * nw + ["tetra"] * nt + ["ring"] * nr
-    return _assemble_fast(kinds, n_free, rng, temperature)
+    return _assemble_fast(kinds, n_free, rng, temperature, grouped=grouped)
 
 
-def _assemble_fast(kinds, n_free, rng, temperature, free_mass=ARGON_MASS):
+def _assemble_fast(kinds, n_free, rng, temperature, free_mass=ARGON_MASS, grouped=False):
     """Vectorised version of _assemble for millions of molecules."""
     names = ["water", "tetra", "ring"]
     kid = np.array([names.index(k) for k in kinds], dtype=np.int8) if kinds else np.zeros(0, np.int8)
@@ -174,6 +178,10 @@ def _assemble_fast(kinds, n_free, rng, temperature, free_mass=ARGON_MASS):
     sites = _lattice(nmol + n_free, box)
     order = rng.permutation(nmol + n_free)
     rot = random_rotations(rng, nmol)
+    if grouped:  # list order: molecules by kind, then free atoms; lattice sites stay random
+        site_of = order.copy()
+        order = np.arange(nmol + n_free)
+        sites = sites[np.argsort(site_of)]
     # slot -> (kind, n atoms)
     slot_kind = np.full(nmol + n_free, 3, dtype=np.int8)  # 3 = free atom
     slot_kind[:nmol] = kid
