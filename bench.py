@@ -25,7 +25,6 @@ import json
 import os
 import subprocess
 import sys
-import tempfile
 import time
 
 import numpy as np
@@ -55,8 +54,8 @@ BYTES_PER_FREE = 128
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=50)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=2000)
+    p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="rbx", choices=["rbx", "reference"])
     p.add_argument("--mode", type=int, default=0, help="rotation mode: 0 exact, n NO-SQUISH substeps")
     p.add_argument("--precision", default="mixed", choices=["single", "mixed", "double"])
@@ -64,6 +63,8 @@ def parse():
     p.add_argument("--free", type=int, default=100_000)
     p.add_argument("--e2e-steps", type=int, default=10)
     p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--reference-seconds", type=float, default=90.0,
+                   help="bound on the timed CPU work of --impl reference")
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
 
@@ -128,26 +129,42 @@ def ncu_traffic(mode, precision, bodies):
 
 
 class ClockSampler:
-    """nvidia-smi clock / throttle sampling during the timed region."""
+    """nvidia-smi clock / throttle sampling; only samples that arrive between mark_start() and
+    mark_end() (the timed region) are summarised."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
+    def __init__(self, gpu_index, period_ms=50):
         self.gpu = gpu_index
+        self.period_ms = period_ms
         self.proc = None
-        self.file = None
+        self.thread = None
+        self.lines = []  # (host time, csv line)
+        self.t0 = self.t1 = None
+
+    def _reader(self):
+        for line in self.proc.stdout:
+            self.lines.append((time.perf_counter(), line))
 
     def __enter__(self):
+        import threading
         try:
-            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=self.file, stderr=subprocess.DEVNULL)
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period_ms)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._reader, daemon=True)
+            self.thread.start()
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
+
+    def mark_start(self):
+        self.t0 = time.perf_counter()
+
+    def mark_end(self):
+        self.t1 = time.perf_counter()
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -156,15 +173,18 @@ class ClockSampler:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            self.thread.join(timeout=5)
 
     def summary(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.file.flush()
-        self.file.seek(0)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in self.file.read().splitlines():
+        t0 = self.t0 if self.t0 is not None else -np.inf
+        t1 = self.t1 if self.t1 is not None else np.inf
+        for t, line in self.lines:
+            if not t0 <= t <= t1:
+                continue
             parts = [x.strip() for x in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -176,9 +196,8 @@ class ClockSampler:
             for n, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
-        os.unlink(self.file.name)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "period_ms": self.period_ms}
 
 
 def cpu_baseline(s, F, args, seconds):
@@ -188,14 +207,14 @@ def cpu_baseline(s, F, args, seconds):
     oracle.build()
     from openmm_rigidbody_plugin_gb300 import workloads as W
     threads = os.cpu_count() or 1
-    frac = 0.05
-    sub = W.mixed_system(n_bodies=int(args.bodies * frac), n_free=int(args.free * frac), seed=3)
+    frac = 0.2  # a sample of 200,000 bodies at the default size: larger than the host caches
+    sub = W.mixed_system(n_bodies=max(1000, int(args.bodies * frac)), n_free=int(args.free * frac), seed=3)
     Fs = W.gaussian_forces(sub.num_atoms, seed=5)
     o = oracle.Oracle(sub.masses, sub.body_indices, mode=args.mode, robust=True)
     o.setup(sub.positions, sub.velocities, Fs)
     o.run_fixed_force(0.002, Fs, 1, threads)
     t = o.run_fixed_force(0.002, Fs, 1, threads)
-    steps = max(1, min(1000, int(seconds / max(t, 1e-6))))
+    steps = max(1, min(20000, int(seconds / max(t, 1e-6))))
     t = o.run_fixed_force(0.002, Fs, steps, threads)
     nb = o.num_bodies
     return {"value": nb * steps / t, "unit": UNIT, "cores": threads, "kind": "port",
@@ -204,16 +223,30 @@ def cpu_baseline(s, F, args, seconds):
 
 
 def run_reference(args, world, rank):
-    """CPU implementation of the step on the host cores (rank 0 only)."""
+    """CPU implementation of the step on the host cores (rank 0 only). Each step integrates the
+    full workload unless --steps of them would take longer than --reference-seconds; then each
+    step integrates a seeded sample of the same mix, sized to fit that time."""
     if rank != 0:
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
-    s, F = build_workload(args)
+    from openmm_rigidbody_plugin_gb300 import workloads as W
     threads = os.cpu_count() or 1
+    s, F = build_workload(args)
     o = oracle.Oracle(s.masses, s.body_indices, mode=args.mode, robust=True)
     o.setup(s.positions, s.velocities, F)
+    t1 = o.run_fixed_force(0.002, F, 1, threads)
+    sample = "full workload"
+    if args.steps * t1 > args.reference_seconds:
+        frac = args.reference_seconds / (args.steps * t1)
+        nb_s = max(1000, int(args.bodies * frac))
+        s = W.mixed_system(n_bodies=nb_s, n_free=int(args.free * nb_s / max(args.bodies, 1)), seed=3)
+        F = W.gaussian_forces(s.num_atoms, seed=5)
+        o = oracle.Oracle(s.masses, s.body_indices, mode=args.mode, robust=True)
+        o.setup(s.positions, s.velocities, F)
+        sample = f"a {nb_s}-body sample of the same mix per step (full workload x {args.steps} steps exceeds " \
+                 f"{args.reference_seconds:.0f} s)"
     for _ in range(args.warmup):
         o.run_fixed_force(0.002, F, 1, threads)
     t = o.run_fixed_force(0.002, F, args.steps, threads)
@@ -227,7 +260,7 @@ def run_reference(args, world, rank):
                       "(robust variant: the reference's own eigen-solver and exact rotation produce NaN for the "
                       "tetrahedra and rings of this mix)"},
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                            "sample": f"full workload, {args.steps} steps, {threads} threads"},
+                            "sample": f"{sample}, {args.steps} steps, {threads} threads, {t:.1f} s"},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -258,13 +291,15 @@ def run_gpu(args, world, rank, local):
     barrier(world)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clocks:
-        time.sleep(0.3)
+        time.sleep(0.3)  # nvidia-smi start-up
         torch.cuda.synchronize()
+        clocks.mark_start()
         start.record(stream)
         for _ in range(args.steps):
             k.fused(buf, dt, stream)
         end.record(stream)
         torch.cuda.synchronize()
+        clocks.mark_end()
     launches = args.steps
     t_dev = start.elapsed_time(end) / 1e3
     t_dev = max_over_ranks(t_dev, world)
