@@ -178,6 +178,49 @@ int rbx_kinetic_energies_static(const double* body_state, int num_bodies, int bo
 /* Number of kernel launches the last integrate/kinetic/step call enqueued (for accounting). */
 int rbx_last_launch_count(const rbx_integrator* h);
 
+/*
+ * Batched systems: many independent periodic systems integrated together, with forces from the
+ * library's own cutoff Lennard-Jones + reaction-field kernel (the functional form of OpenMM's
+ * NonbondedForce with the CutoffPeriodic method; pairs of one rigid body excluded, as the
+ * plugin's ForceField helper removes them, python/forcefield.py:131-138). The reference has no
+ * batched form: each system of the reference is one Context with one integrator kernel, stepped
+ * by RigidBodyIntegrator::step (RigidBodyIntegrator.cpp:76-93) -> execute
+ * (CudaRigidBodyKernels.cpp:377-444); this handle runs that same step for every system at once.
+ *
+ *   num_systems   S; system s holds atoms [atom_offsets[s], atom_offsets[s+1]) of the arrays
+ *   box_edges     [S] cubic box edge (nm); cutoffs [S] cutoff (nm), each below box_edges[s]/2
+ *   body_indices  [N] per-system body ids (0 = free atom; equal positive ids within a system
+ *                 form one rigid body, as in rbx_create)
+ *   masses, charges (e), sigmas (nm), epsilons (kJ/mol)  [N]; Lorentz-Berthelot combination
+ *   eps_solvent   reaction-field dielectric (OpenMM's default is 78.3)
+ * Atoms live in device slots equal to their index in these arrays.
+ * rbx_batch_step runs nsteps velocity-Verlet steps of size dt on every system: forces at the
+ * current positions, part1, then (forces, fused part2+part1) x (nsteps-1), forces, part2. With
+ * rbx_batch_set_graph_steps(k > 0), runs of k (forces, fused) pairs replay one captured CUDA graph
+ * (captured on first use for a given dt; invalidated by rbx_batch_set_state).
+ * rbx_batch_energies returns [U, KE_t, KE_r] per system (kJ/mol) at the current state
+ * (synchronous). rbx_batch_get_num_dof gives each system's degrees of freedom.
+ */
+typedef struct rbx_batch rbx_batch;
+int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, const double* box_edges,
+                     const double* cutoffs, const int* body_indices, const double* masses, const double* charges,
+                     const double* sigmas, const double* epsilons, double eps_solvent, int rotation_mode,
+                     int precision, int device);
+int rbx_batch_destroy(rbx_batch* b);
+int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, const double* velocities);
+int rbx_batch_get_state(rbx_batch* b, void* stream, double* positions, double* velocities);
+int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt);
+/* Relaxation by quenched steps: nsteps times (forces capped at max_force kJ/mol/nm per atom, every
+ * momentum zeroed, part1 of size dt), then every momentum zeroed. Removes the overlaps of
+ * generated starting structures before dynamics; velocities are then reassigned by
+ * rbx_batch_set_state. Not a step of the reference, which takes its starting state as given. */
+int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double max_force);
+int rbx_batch_energies(rbx_batch* b, void* stream, double* out /* [3*S] */);
+int rbx_batch_forces(rbx_batch* b, void* stream, double* forces /* [N*3], user order */, double* energies /* [S] */);
+int rbx_batch_get_num_dof(rbx_batch* b, int* dof /* [S] */);
+int rbx_batch_set_graph_steps(rbx_batch* b, int k);
+int rbx_batch_last_launch_count(const rbx_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -55,6 +55,18 @@ SIGNATURES = [
     ("rbx_last_launch_count", ctypes.c_int, [_vp]),
     ("rbx_kinetic_energies_static", ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int, _dp, _dp, _vp, _ip, ctypes.c_int,
                                                    ctypes.c_int, _vp, _dp]),
+    ("rbx_batch_create", ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, _ip, _dp, _dp, _ip, _dp, _dp, _dp, _dp,
+                                        ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    ("rbx_batch_destroy", ctypes.c_int, [_vp]),
+    ("rbx_batch_set_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
+    ("rbx_batch_get_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
+    ("rbx_batch_step", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double]),
+    ("rbx_batch_relax", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_double]),
+    ("rbx_batch_energies", ctypes.c_int, [_vp, _vp, _dp]),
+    ("rbx_batch_forces", ctypes.c_int, [_vp, _vp, _dp, _dp]),
+    ("rbx_batch_get_num_dof", ctypes.c_int, [_vp, _ip]),
+    ("rbx_batch_set_graph_steps", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("rbx_batch_last_launch_count", ctypes.c_int, [_vp]),
 ]
 
 _lib = None

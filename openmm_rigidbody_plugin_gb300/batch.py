@@ -1,0 +1,130 @@
+"""Batched systems: many independent periodic systems stepped together (rbx_batch_* C ABI).
+
+Each system is a rigid-body system in its own cubic box; forces come from the library's cell-list
+cutoff Lennard-Jones + reaction-field kernels (the CutoffPeriodic form of OpenMM's
+NonbondedForce), and the whole set advances with one integrator launch per step. Runs of steps
+can replay a captured CUDA graph (``graph_steps``).
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+EPS_SOLVENT = 78.3
+
+
+def _d(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _i(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _stream(stream):
+    import torch
+    return ctypes.c_void_p((stream or torch.cuda.current_stream()).cuda_stream)
+
+
+class BatchedSystems:
+    """Independent systems (each with masses, body_indices, positions, velocities, box and
+    per-atom charge/sigma/epsilon) integrated as one batch on one device."""
+
+    def __init__(self, masses, body_indices, atom_offsets, boxes, cutoffs, charges, sigmas, epsilons,
+                 rotation_mode=0, precision="mixed", eps_solvent=EPS_SOLVENT, device=0):
+        self._lib = _lib.load()
+        self.masses = np.ascontiguousarray(masses, dtype=np.float64)
+        self.offsets = np.ascontiguousarray(atom_offsets, dtype=np.int32)
+        self.num_systems = len(self.offsets) - 1
+        self.num_atoms = int(self.offsets[-1])
+        cast = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+        self.boxes = cast(boxes)
+        self.cutoffs = cast(cutoffs)
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.rbx_batch_create(
+            ctypes.byref(h), self.num_systems, _i(self.offsets), _d(self.boxes), _d(self.cutoffs),
+            _i(np.ascontiguousarray(body_indices, dtype=np.int32)), _d(cast(masses)), _d(cast(charges)),
+            _d(cast(sigmas)), _d(cast(epsilons)), float(eps_solvent), int(rotation_mode),
+            _lib.PRECISIONS[precision], int(device)))
+        self._h = h
+
+    @classmethod
+    def from_systems(cls, systems, rotation_mode=0, precision="mixed", device=0, relax_steps=0, temperature=300.0,
+                     seed=0):
+        """Batch of workloads.System objects, with their species' nonbonded parameters and the
+        0.9 nm cutoff clamped to 0.49 box edges. With relax_steps > 0 the generated structures are
+        first relaxed (``relax``) and then given Maxwell-Boltzmann velocities at `temperature`."""
+        from . import workloads as W
+        q, s, e = zip(*(W.nonbonded(x) for x in systems))
+        offsets = np.concatenate([[0], np.cumsum([x.num_atoms for x in systems])])
+        b = cls(np.concatenate([x.masses for x in systems]), np.concatenate([x.body_indices for x in systems]),
+                offsets, [x.box for x in systems], [W.cutoff_for(x.box) for x in systems], np.concatenate(q),
+                np.concatenate(s), np.concatenate(e), rotation_mode=rotation_mode, precision=precision,
+                device=device)
+        b.set_state(np.concatenate([x.positions for x in systems]), np.concatenate([x.velocities for x in systems]))
+        if relax_steps > 0:
+            b.relax(relax_steps)
+            b.thermalize(temperature, seed)
+        return b
+
+    def relax(self, nsteps=300, dt=0.005, max_force=5000.0, stream=None):
+        """Quenched steps (forces capped at max_force, momenta zeroed each step) that remove the
+        overlaps of generated starting structures; leaves every momentum at zero."""
+        _lib.check(self._lib.rbx_batch_relax(self._h, _stream(stream), int(nsteps), float(dt), float(max_force)))
+
+    def thermalize(self, temperature=300.0, seed=0, stream=None):
+        """Seeded Maxwell-Boltzmann velocities at the current positions (projected onto rigid motion
+        by the state upload)."""
+        from .workloads import KB
+        x, _ = self.get_state(stream)
+        rng = np.random.default_rng(seed)
+        sd = np.sqrt(KB * temperature / np.where(self.masses > 0, self.masses, 1.0))
+        v = rng.standard_normal((self.num_atoms, 3)) * sd[:, None] * (self.masses > 0)[:, None]
+        self.set_state(x, v, stream)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            self._lib.rbx_batch_destroy(h)
+            self._h = None
+
+    def set_state(self, positions, velocities, stream=None):
+        x = np.ascontiguousarray(positions, dtype=np.float64)
+        v = np.ascontiguousarray(velocities, dtype=np.float64)
+        _lib.check(self._lib.rbx_batch_set_state(self._h, _stream(stream), _d(x), _d(v)))
+
+    def get_state(self, stream=None):
+        x = np.zeros((self.num_atoms, 3))
+        v = np.zeros((self.num_atoms, 3))
+        _lib.check(self._lib.rbx_batch_get_state(self._h, _stream(stream), _d(x), _d(v)))
+        return x, v
+
+    def step(self, nsteps, dt, stream=None):
+        _lib.check(self._lib.rbx_batch_step(self._h, _stream(stream), int(nsteps), float(dt)))
+
+    def energies(self, stream=None):
+        """[U, KE_t, KE_r] per system (kJ/mol), shape (num_systems, 3)."""
+        out = np.zeros((self.num_systems, 3))
+        _lib.check(self._lib.rbx_batch_energies(self._h, _stream(stream), _d(out)))
+        return out
+
+    def forces(self, stream=None):
+        """Forces at the current positions (user order, kJ/mol/nm) and the potential energies."""
+        f = np.zeros((self.num_atoms, 3))
+        e = np.zeros(self.num_systems)
+        _lib.check(self._lib.rbx_batch_forces(self._h, _stream(stream), _d(f), _d(e)))
+        return f, e
+
+    @property
+    def num_dof(self):
+        out = np.zeros(self.num_systems, dtype=np.int32)
+        _lib.check(self._lib.rbx_batch_get_num_dof(self._h, _i(out)))
+        return out
+
+    def set_graph_steps(self, k):
+        _lib.check(self._lib.rbx_batch_set_graph_steps(self._h, int(k)))
+
+    @property
+    def last_launch_count(self):
+        return self._lib.rbx_batch_last_launch_count(self._h)

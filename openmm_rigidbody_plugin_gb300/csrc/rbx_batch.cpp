@@ -1,0 +1,412 @@
+// rbx_batch.cpp -- batched systems: one integrator over the atoms of many independent periodic
+// systems, forces from the library's cell-list LJ + reaction-field kernels, and runs of steps
+// replayed from a captured CUDA graph. The C ABI is declared in include/rbx.h.
+//
+// Every system keeps a contiguous range of device slots, so the integrator's library order (bodies
+// by lowest slot) keeps each system's bodies and free atoms contiguous as well, which the
+// per-system kinetic-energy reduction relies on.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/rbx.h"
+#include "rbx_devarray.h"
+#include "rbx_internal.h"
+
+using namespace rbx;
+
+namespace {
+
+constexpr double kOne4PiEps0 = 138.935456;  // kJ nm / (mol e^2)
+
+#define BATCH_TRY(call)                                                                             \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess) return set_error(RBX_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+float int_bits(int v) {
+    float f;
+    std::memcpy(&f, &v, sizeof f);
+    return f;
+}
+
+template <class T> int upload_vec(DevArray<T>& a, const std::vector<T>& h) {
+    if (a.alloc(h.size()) != cudaSuccess) return set_error(RBX_ERR_CUDA, "cudaMalloc of %zu bytes failed", h.size() * sizeof(T));
+    if (!h.empty()) BATCH_TRY(cudaMemcpy(a.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return RBX_OK;
+}
+
+}  // namespace
+
+struct rbx_batch {
+    rbx_integrator* integ = nullptr;
+    int S = 0, natoms = 0, prec = PREC_MIXED, device = 0;
+    std::vector<int> offsets;
+    // force field
+    DevArray<FFSys> d_sys;
+    DevArray<int> d_iatom, d_isys, d_cell_of, d_cell_count, d_cell_start, d_cell_cursor, d_cell_list;
+    DevArray<float4> d_param, d_cpos, d_cpar;
+    DevArray<double> d_e_atom, d_energy;
+    FFDev ff{};
+    // per-system reductions
+    DevArray<int> d_body0, d_free0;
+    DevArray<double> d_ke, d_user;
+    std::vector<int> dof;
+    double* h_out = nullptr;  // pinned [3*S]
+    bool forces_valid = false;
+    int last_launches = 0;
+    // captured runs of (forces, fused step)
+    int graph_k = 0;
+    int graph_launches = 0;  // kernels in one replay of the graph
+    double graph_dt = 0.0;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+
+    void drop_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+    ~rbx_batch() {
+        drop_graph();
+        if (cap_stream) cudaStreamDestroy(cap_stream);
+        if (h_out) cudaFreeHost(h_out);
+        if (integ) rbx_destroy(integ);
+    }
+};
+
+namespace {
+
+int check(const rbx_batch* b) { return b ? RBX_OK : set_error(RBX_ERR_INVALID_ARGUMENT, "null batch handle"); }
+
+DevBuf buffers(rbx_batch* b) {
+    rbx_buffers rb;
+    rbx_context_buffers(b->integ, &rb);
+    DevBuf d;
+    d.posq = rb.posq;
+    d.corr = rb.posq_correction;
+    d.velm = rb.velm;
+    d.force = rb.force;
+    d.stride = rb.stride;
+    return d;
+}
+
+int forces(rbx_batch* b, void* stream, bool energy) {
+    const int n = launch_forces(b->ff, b->prec, buffers(b), energy, stream);
+    if (n < 0) return set_error(RBX_ERR_CUDA, "force kernels failed: %s", cudaGetErrorString(cudaGetLastError()));
+    b->last_launches += n;
+    return RBX_OK;
+}
+
+int fused(rbx_batch* b, void* stream, double dt) {
+    rbx_buffers rb;
+    rbx_context_buffers(b->integ, &rb);
+    int rc = rbx_integrate_fused(b->integ, stream, &rb, dt);
+    if (!rc) b->last_launches += 1;
+    return rc;
+}
+
+int capture(rbx_batch* b, double dt) {
+    b->drop_graph();
+    if (!b->cap_stream) BATCH_TRY(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
+    BATCH_TRY(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeRelaxed));
+    int rc = RBX_OK;
+    const int before = b->last_launches;
+    for (int i = 0; i < b->graph_k && !rc; i++) {
+        rc = forces(b, b->cap_stream, false);
+        if (!rc) rc = fused(b, b->cap_stream, dt);
+    }
+    b->graph_launches = b->last_launches - before;
+    b->last_launches = before;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->cap_stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return set_error(RBX_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        b->graph = nullptr;
+        return set_error(RBX_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+    }
+    b->graph_dt = dt;
+    return RBX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, const double* box_edges,
+                     const double* cutoffs, const int* body_indices, const double* masses, const double* charges,
+                     const double* sigmas, const double* epsilons, double eps_solvent, int rotation_mode,
+                     int precision, int device) {
+    if (!out) return set_error(RBX_ERR_INVALID_ARGUMENT, "null output pointer");
+    *out = nullptr;
+    if (num_systems <= 0 || !atom_offsets || !box_edges || !cutoffs || !body_indices || !masses || !charges ||
+        !sigmas || !epsilons)
+        return set_error(RBX_ERR_INVALID_ARGUMENT, "need num_systems > 0 and every per-system and per-atom array");
+    if (atom_offsets[0] != 0) return set_error(RBX_ERR_INVALID_ARGUMENT, "atom_offsets[0] must be 0");
+    for (int s = 0; s < num_systems; s++) {
+        if (atom_offsets[s + 1] <= atom_offsets[s]) return set_error(RBX_ERR_INVALID_ARGUMENT, "system %d has no atoms", s);
+        if (!(box_edges[s] > 0.0)) return set_error(RBX_ERR_INVALID_ARGUMENT, "system %d: box edge must be positive", s);
+        if (!(cutoffs[s] > 0.0) || !(cutoffs[s] < 0.5 * box_edges[s]))
+            return set_error(RBX_ERR_INVALID_ARGUMENT, "system %d: the cutoff must lie in (0, box/2)", s);
+    }
+    if (!(eps_solvent >= 1.0)) return set_error(RBX_ERR_INVALID_ARGUMENT, "reaction-field dielectric must be >= 1");
+    const int N = atom_offsets[num_systems];
+    rbx_batch* b = new (std::nothrow) rbx_batch();
+    if (!b) return set_error(RBX_ERR_INVALID_ARGUMENT, "out of host memory");
+    b->S = num_systems;
+    b->natoms = N;
+    b->prec = precision;
+    b->device = device;
+    b->offsets.assign(atom_offsets, atom_offsets + num_systems + 1);
+
+    // one integrator over all systems: per-system body ids made unique
+    std::vector<int> ids(N, 0);
+    long base = 0;
+    for (int s = 0; s < num_systems; s++) {
+        int mx = 0;
+        for (int i = atom_offsets[s]; i < atom_offsets[s + 1]; i++) {
+            if (body_indices[i] > 0) {
+                ids[i] = (int)(base + body_indices[i]);
+                mx = std::max(mx, body_indices[i]);
+            }
+        }
+        base += mx;
+        if (base > 2000000000L) { delete b; return set_error(RBX_ERR_INVALID_ARGUMENT, "too many bodies"); }
+    }
+    int rc = rbx_create(&b->integ, N, ids.data(), masses, rotation_mode, precision, device);
+    if (rc) { delete b; return rc; }
+
+    // force field tables: interacting atoms (charge or LJ) system by system
+    std::vector<FFSys> sys(num_systems);
+    std::vector<int> iatom, isys;
+    std::vector<float4> param;
+    int cells = 0;
+    for (int s = 0; s < num_systems; s++) {
+        FFSys& f = sys[s];
+        f.a0 = atom_offsets[s];
+        f.a1 = atom_offsets[s + 1];
+        f.i0 = (int)iatom.size();
+        for (int i = f.a0; i < f.a1; i++) {
+            if (charges[i] == 0.0 && epsilons[i] == 0.0) continue;
+            iatom.push_back(i);
+            isys.push_back(s);
+            const float qs = (float)(std::sqrt(kOne4PiEps0) * charges[i]);
+            param.push_back(make_float4(qs, (float)(0.5 * sigmas[i]), (float)std::sqrt(std::max(epsilons[i], 0.0)),
+                                        int_bits(ids[i])));
+        }
+        f.i1 = (int)iatom.size();
+        const double L = box_edges[s], rc_s = cutoffs[s];
+        int nc = (int)std::floor(L / rc_s);
+        if (nc < 3) nc = 1;
+        if (nc > 256) nc = 256;
+        f.c0 = cells;
+        f.nc = nc;
+        cells += nc * nc * nc;
+        f.L = (float)L;
+        f.invL = (float)(1.0 / L);
+        f.rc2 = (float)(rc_s * rc_s);
+        const double krf = (eps_solvent - 1.0) / ((2.0 * eps_solvent + 1.0) * rc_s * rc_s * rc_s);
+        f.krf = (float)krf;
+        f.crf = (float)(1.0 / rc_s + krf * rc_s * rc_s);
+    }
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete b; return set_error(RBX_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); }
+    const int nint = (int)iatom.size();
+    rc = upload_vec(b->d_sys, sys);
+    if (!rc) rc = upload_vec(b->d_iatom, iatom);
+    if (!rc) rc = upload_vec(b->d_isys, isys);
+    if (!rc) rc = upload_vec(b->d_param, param);
+    if (!rc && (b->d_cell_of.alloc(std::max(nint, 1)) != cudaSuccess || b->d_cell_list.alloc(std::max(nint, 1)) != cudaSuccess ||
+                b->d_cell_count.alloc(cells) != cudaSuccess || b->d_cell_start.alloc(cells + 1) != cudaSuccess ||
+                b->d_cell_cursor.alloc(cells) != cudaSuccess || b->d_cpos.alloc(std::max(nint, 1)) != cudaSuccess ||
+                b->d_cpar.alloc(std::max(nint, 1)) != cudaSuccess || b->d_e_atom.alloc(std::max(nint, 1)) != cudaSuccess ||
+                b->d_energy.alloc(num_systems) != cudaSuccess || b->d_ke.alloc(2 * (size_t)num_systems) != cudaSuccess ||
+                b->d_user.alloc(3 * (size_t)N) != cudaSuccess))
+        rc = set_error(RBX_ERR_CUDA, "cudaMalloc of force-field arrays failed");
+    if (!rc && cudaMemset(b->d_cell_count.p, 0, sizeof(int) * (size_t)cells) != cudaSuccess)
+        rc = set_error(RBX_ERR_CUDA, "cudaMemset of cell counts failed");
+    if (!rc && cudaMallocHost((void**)&b->h_out, sizeof(double) * 3 * (size_t)num_systems) != cudaSuccess)
+        rc = set_error(RBX_ERR_CUDA, "pinned allocation failed");
+    if (rc) { delete b; return rc; }
+    FFDev& D = b->ff;
+    D.S = num_systems;
+    D.n_int = nint;
+    D.n_cells = cells;
+    D.sys = b->d_sys.p;
+    D.iatom = b->d_iatom.p;
+    D.isys = b->d_isys.p;
+    D.param = b->d_param.p;
+    D.cell_of = b->d_cell_of.p;
+    D.cell_count = b->d_cell_count.p;
+    D.cell_start = b->d_cell_start.p;
+    D.cell_cursor = b->d_cell_cursor.p;
+    D.cell_list = b->d_cell_list.p;
+    D.cpos = b->d_cpos.p;
+    D.cpar = b->d_cpar.p;
+    D.e_atom = b->d_e_atom.p;
+    D.energy = b->d_energy.p;
+    // the owned OpenMM-layout buffers (forces of non-interacting atoms stay zero)
+    rbx_buffers rb;
+    if ((rc = rbx_context_buffers(b->integ, &rb))) { delete b; return rc; }
+    *out = b;
+    return RBX_OK;
+}
+
+int rbx_batch_destroy(rbx_batch* b) {
+    delete b;
+    return RBX_OK;
+}
+
+int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, const double* velocities) {
+    int rc = check(b);
+    if (rc) return rc;
+    b->drop_graph();  // the integrator re-plans its device arrays
+    if ((rc = rbx_context_set_state(b->integ, stream, positions, velocities))) return rc;
+    std::vector<int> body0, free0;
+    system_ranges(b->integ, b->offsets, body0, free0, b->dof);
+    if ((rc = upload_vec(b->d_body0, body0)) || (rc = upload_vec(b->d_free0, free0))) return rc;
+    b->forces_valid = false;
+    return RBX_OK;
+}
+
+int rbx_batch_get_state(rbx_batch* b, void* stream, double* positions, double* velocities) {
+    int rc = check(b);
+    if (rc) return rc;
+    return rbx_context_get_state(b->integ, stream, positions, velocities);
+}
+
+int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (nsteps < 1) return set_error(RBX_ERR_INVALID_ARGUMENT, "nsteps must be >= 1");
+    if (!(dt == dt) || dt == 0.0) return set_error(RBX_ERR_INVALID_ARGUMENT, "step size must be finite and non-zero");
+    if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
+    BATCH_TRY(cudaSetDevice(b->device));
+    b->last_launches = 0;
+    rbx_buffers rb;
+    rbx_context_buffers(b->integ, &rb);
+    if (!b->forces_valid && (rc = forces(b, stream, false))) return rc;
+    if ((rc = rbx_integrate_part1(b->integ, stream, &rb, dt))) return rc;
+    b->last_launches += 1;
+    int remaining = nsteps - 1;
+    if (b->graph_k > 0 && remaining >= b->graph_k) {
+        if (!b->graph || b->graph_dt != dt) {
+            if ((rc = capture(b, dt))) return rc;
+        }
+        while (remaining >= b->graph_k) {
+            BATCH_TRY(cudaGraphLaunch(b->graph, (cudaStream_t)stream));
+            b->last_launches += b->graph_launches;
+            remaining -= b->graph_k;
+        }
+    }
+    for (; remaining > 0; remaining--) {
+        if ((rc = forces(b, stream, false)) || (rc = fused(b, stream, dt))) return rc;
+    }
+    if ((rc = forces(b, stream, false))) return rc;
+    if ((rc = rbx_integrate_part2(b->integ, stream, &rb, dt))) return rc;
+    b->last_launches += 1;
+    b->forces_valid = true;
+    return RBX_OK;
+}
+
+int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double max_force) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (nsteps < 1 || !(dt > 0.0) || !(max_force > 0.0))
+        return set_error(RBX_ERR_INVALID_ARGUMENT, "relaxation needs nsteps >= 1, dt > 0 and max_force > 0");
+    if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
+    BATCH_TRY(cudaSetDevice(b->device));
+    b->last_launches = 0;
+    rbx_buffers rb;
+    rbx_context_buffers(b->integ, &rb);
+    const DevSys sys = device_system(b->integ);
+    b->ff.fcap = (float)max_force;
+    for (int n = 0; n < nsteps && !rc; n++) {
+        rc = forces(b, stream, false);
+        if (!rc && launch_zero_momenta(b->prec, sys, buffers(b), stream) < 0)
+            rc = set_error(RBX_ERR_CUDA, "momentum reset failed");
+        if (!rc) rc = rbx_integrate_part1(b->integ, stream, &rb, dt);
+        b->last_launches += 2;
+    }
+    b->ff.fcap = 0.0f;
+    if (rc) return rc;
+    if (launch_zero_momenta(b->prec, sys, buffers(b), stream) < 0) return set_error(RBX_ERR_CUDA, "momentum reset failed");
+    b->forces_valid = false;
+    return RBX_OK;
+}
+
+int rbx_batch_energies(rbx_batch* b, void* stream, double* out) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (!out) return set_error(RBX_ERR_INVALID_ARGUMENT, "null output");
+    if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
+    BATCH_TRY(cudaSetDevice(b->device));
+    b->last_launches = 0;
+    if ((rc = forces(b, stream, true))) return rc;  // same forces, plus per-system potential energy
+    b->forces_valid = true;
+    if (launch_kinetic_systems(b->prec, device_system(b->integ), buffers(b), b->d_body0.p, b->d_free0.p, b->S,
+                               b->d_ke.p, stream) < 0)
+        return set_error(RBX_ERR_CUDA, "kinetic-energy kernel failed: %s", cudaGetErrorString(cudaGetLastError()));
+    b->last_launches += 1;
+    cudaStream_t st = (cudaStream_t)stream;
+    BATCH_TRY(cudaMemcpyAsync(b->h_out, b->d_energy.p, sizeof(double) * b->S, cudaMemcpyDeviceToHost, st));
+    BATCH_TRY(cudaMemcpyAsync(b->h_out + b->S, b->d_ke.p, sizeof(double) * 2 * b->S, cudaMemcpyDeviceToHost, st));
+    BATCH_TRY(cudaStreamSynchronize(st));
+    for (int s = 0; s < b->S; s++) {
+        out[3 * s] = b->h_out[s];
+        out[3 * s + 1] = b->h_out[b->S + 2 * s];
+        out[3 * s + 2] = b->h_out[b->S + 2 * s + 1];
+    }
+    return RBX_OK;
+}
+
+int rbx_batch_forces(rbx_batch* b, void* stream, double* forces_out, double* energies) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
+    BATCH_TRY(cudaSetDevice(b->device));
+    b->last_launches = 0;
+    if ((rc = forces(b, stream, true))) return rc;
+    b->forces_valid = true;
+    cudaStream_t st = (cudaStream_t)stream;
+    const DevBuf d = buffers(b);
+    if (forces_out) {
+        if (launch_forces_to_user(d.force, d.stride, b->natoms, b->d_user.p, stream) < 0)
+            return set_error(RBX_ERR_CUDA, "force conversion failed");
+        BATCH_TRY(cudaMemcpyAsync(forces_out, b->d_user.p, sizeof(double) * 3 * (size_t)b->natoms, cudaMemcpyDeviceToHost, st));
+    }
+    if (energies) BATCH_TRY(cudaMemcpyAsync(energies, b->d_energy.p, sizeof(double) * b->S, cudaMemcpyDeviceToHost, st));
+    BATCH_TRY(cudaStreamSynchronize(st));
+    return RBX_OK;
+}
+
+int rbx_batch_get_num_dof(rbx_batch* b, int* dof) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (b->dof.empty()) return set_error(RBX_ERR_STATE, "degrees of freedom are known after rbx_batch_set_state");
+    std::copy(b->dof.begin(), b->dof.end(), dof);
+    return RBX_OK;
+}
+
+int rbx_batch_set_graph_steps(rbx_batch* b, int k) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (k < 0) return set_error(RBX_ERR_INVALID_ARGUMENT, "graph run length must be >= 0");
+    if (k != b->graph_k) b->drop_graph();
+    b->graph_k = k;
+    return RBX_OK;
+}
+
+int rbx_batch_last_launch_count(const rbx_batch* b) { return b ? b->last_launches : 0; }
+
+}  // extern "C"

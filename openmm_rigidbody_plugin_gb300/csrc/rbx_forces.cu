@@ -1,0 +1,260 @@
+// rbx_forces.cu -- cutoff Lennard-Jones + reaction-field forces for many independent periodic
+// systems, by cell lists (the force provider of the batched and served forms; the drop-in takes
+// its forces from the OpenMM Context instead).
+//
+// Functional form: OpenMM NonbondedForce, CutoffPeriodic method, as documented by OpenMM
+//   E = K q_i q_j (1/r + k_rf r^2 - c_rf) + 4 eps_ij ((sig_ij/r)^12 - (sig_ij/r)^6),  r < rc,
+// Lorentz-Berthelot combination, minimum image in a cubic box, pairs of one rigid body excluded.
+//
+// One evaluation, all systems at once:
+//   1. ff_bin      one thread per interacting atom: cell index, cell counts
+//   2. ff_scan     one block per system: exclusive scan of its cells' counts (and count reset)
+//   3. ff_scatter  one thread per interacting atom: slot in its cell (single-cell systems keep
+//                  their atom order and need no atomics)
+//   4. ff_order    one thread per cell: sorts the cell by atom index (the cell contents, and so
+//                  every force sum, are in a fixed order) and writes cell-ordered copies of the
+//                  positions and parameters, so that neighbour loads are contiguous
+//   5. ff_force    one thread per interacting atom, in cell order: all pairs within the cutoff
+//                  over the 27 neighbour cells (or the whole box of a single-cell system), no
+//                  atomics; forces written as OpenMM fixed point (2^32) to the atom's slot
+//   6. ff_energy   (energy evaluations only) one block per system: fixed-order FP64 sum.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "rbx_internal.h"
+
+namespace rbx {
+
+namespace {
+
+__device__ __forceinline__ float3 atom_position(const DevBuf& B, int prec, int slot) {
+    if (prec == PREC_DOUBLE) {
+        const double* p = (const double*)B.posq + 4 * (size_t)slot;
+        return make_float3((float)p[0], (float)p[1], (float)p[2]);
+    }
+    const float4 p = ((const float4*)B.posq)[slot];
+    if (prec == PREC_MIXED) {
+        const float4 c = ((const float4*)B.corr)[slot];
+        return make_float3(p.x + c.x, p.y + c.y, p.z + c.z);
+    }
+    return make_float3(p.x, p.y, p.z);
+}
+
+__device__ __forceinline__ int wrap_cell(float x, float invL, int nc) {
+    float f = x * invL;
+    f -= floorf(f);
+    int c = (int)(f * (float)nc);
+    return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
+}
+
+__global__ void ff_bin(FFDev D, DevBuf B, int prec) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= D.n_int) return;
+    const FFSys S = D.sys[D.isys[k]];
+    if (S.nc == 1) {
+        D.cell_of[k] = S.c0;
+        return;
+    }
+    const float3 x = atom_position(B, prec, D.iatom[k]);
+    const int cx = wrap_cell(x.x, S.invL, S.nc), cy = wrap_cell(x.y, S.invL, S.nc), cz = wrap_cell(x.z, S.invL, S.nc);
+    const int c = S.c0 + (cz * S.nc + cy) * S.nc + cx;
+    D.cell_of[k] = c;
+    atomicAdd(D.cell_count + c, 1);
+}
+
+// Exclusive scan of one system's cell counts, in chunks of blockDim.x; the counts are reset.
+__global__ void ff_scan(FFDev D) {
+    __shared__ int s[256];
+    const FFSys S = D.sys[blockIdx.x];
+    const int ncell = S.nc * S.nc * S.nc;
+    if (S.nc == 1) {
+        if (threadIdx.x == 0) {
+            D.cell_start[S.c0] = S.i0;
+            D.cell_start[S.c0 + 1] = S.i1;
+        }
+        return;
+    }
+    int base = S.i0;
+    for (int c0 = 0; c0 < ncell; c0 += blockDim.x) {
+        const int c = c0 + threadIdx.x;
+        const int v = c < ncell ? D.cell_count[S.c0 + c] : 0;
+        s[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < (int)blockDim.x; o <<= 1) {  // Hillis-Steele inclusive scan
+            const int t = threadIdx.x >= (unsigned)o ? s[threadIdx.x - o] : 0;
+            __syncthreads();
+            s[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (c < ncell) {
+            const int start = base + s[threadIdx.x] - v;
+            D.cell_start[S.c0 + c] = start;
+            D.cell_cursor[S.c0 + c] = start;
+            D.cell_count[S.c0 + c] = 0;
+        }
+        base += s[blockDim.x - 1];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) D.cell_start[S.c0 + ncell] = base;  // equals S.i1
+}
+
+__global__ void ff_scatter(FFDev D) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= D.n_int) return;
+    const FFSys S = D.sys[D.isys[k]];
+    if (S.nc == 1) {
+        D.cell_list[k] = k;  // one cell: interacting-atom order
+        return;
+    }
+    const int p = atomicAdd(D.cell_cursor + D.cell_of[k], 1);
+    D.cell_list[p] = k;
+}
+
+// Sort each cell by interacting-atom index and write its cell-ordered position/parameter copies.
+__global__ void ff_order(FFDev D, DevBuf B, int prec) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= D.n_cells) return;
+    const int b = D.cell_start[c], e = D.cell_start[c + 1];
+    // insertion sort: a cell of a multi-cell box holds tens of atoms; the one cell of a small box
+    // is already in order (linear pass)
+    for (int i = b + 1; i < e; i++) {
+        const int v = D.cell_list[i];
+        int j = i - 1;
+        while (j >= b && D.cell_list[j] > v) {
+            D.cell_list[j + 1] = D.cell_list[j];
+            j--;
+        }
+        D.cell_list[j + 1] = v;
+    }
+    for (int i = b; i < e; i++) {
+        const int k = D.cell_list[i];
+        const int slot = D.iatom[k];
+        const float3 x = atom_position(B, prec, slot);
+        const float4 p = D.param[k];  // scaled charge, sigma/2, sqrt(eps), body id bits
+        D.cpos[i] = make_float4(x.x, x.y, x.z, p.x);
+        D.cpar[i] = make_float4(p.y, p.z, p.w, __int_as_float(slot));
+    }
+}
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(128) ff_force(FFDev D, long long* __restrict__ force, int stride) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.n_int) return;
+    const FFSys S = D.sys[D.isys[p]];  // systems keep one contiguous range in both orders
+    const float4 xi = D.cpos[p];
+    const float4 pi = D.cpar[p];
+    const int body = __float_as_int(pi.z);
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    double e = 0.0;
+    auto pair = [&](int q) {
+        if (q == p) return;
+        const float4 xq = D.cpos[q];
+        const float4 pq = D.cpar[q];
+        if (body > 0 && __float_as_int(pq.z) == body) return;
+        float dx = xi.x - xq.x, dy = xi.y - xq.y, dz = xi.z - xq.z;
+        dx -= S.L * rintf(dx * S.invL);
+        dy -= S.L * rintf(dy * S.invL);
+        dz -= S.L * rintf(dz * S.invL);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        if (r2 >= S.rc2) return;
+        const float inv_r2 = 1.0f / r2, inv_r = rsqrtf(r2);
+        const float qq = xi.w * xq.w;
+        const float sig = pi.x + pq.x, eps = pi.y * pq.y;
+        const float s2 = sig * sig * inv_r2, s6 = s2 * s2 * s2;
+        const float g = qq * (inv_r * inv_r2 - 2.0f * S.krf) + 4.0f * eps * (12.0f * s6 * s6 - 6.0f * s6) * inv_r2;
+        fx = fmaf(g, dx, fx);
+        fy = fmaf(g, dy, fy);
+        fz = fmaf(g, dz, fz);
+        if (ENERGY) {  // the pair energy in FP64 from the FP32 displacement
+            const double r2d = (double)r2, inv_rd = 1.0 / sqrt(r2d), s2d = (double)sig * (double)sig / r2d;
+            const double s6d = s2d * s2d * s2d;
+            e += (double)qq * (inv_rd + (double)S.krf * r2d - (double)S.crf) + 4.0 * (double)eps * (s6d * s6d - s6d);
+        }
+    };
+    if (S.nc == 1) {
+        for (int q = S.i0; q < S.i1; q++) pair(q);
+    } else {
+        const int cell = D.cell_of[D.cell_list[p]] - S.c0;
+        const int cx = cell % S.nc, cy = (cell / S.nc) % S.nc, cz = cell / (S.nc * S.nc);
+        for (int oz = -1; oz <= 1; oz++) {
+            const int z = (cz + oz + S.nc) % S.nc;
+            for (int oy = -1; oy <= 1; oy++) {
+                const int y = (cy + oy + S.nc) % S.nc;
+                for (int ox = -1; ox <= 1; ox++) {
+                    const int x = (cx + ox + S.nc) % S.nc;
+                    const int c = S.c0 + (z * S.nc + y) * S.nc + x;
+                    const int qe = D.cell_start[c + 1];
+                    for (int q = D.cell_start[c]; q < qe; q++) pair(q);
+                }
+            }
+        }
+    }
+    if (D.fcap > 0.0f) {  // relaxation: cap the magnitude
+        const float f2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
+        if (f2 > D.fcap * D.fcap) {
+            const float s = D.fcap * rsqrtf(f2);
+            fx *= s;
+            fy *= s;
+            fz *= s;
+        }
+    }
+    // keep each component inside the 2^32 fixed-point range (|F| < 2^31 kJ/mol/nm)
+    const float kMaxF = 2.0e9f;
+    fx = fminf(fmaxf(fx, -kMaxF), kMaxF);
+    fy = fminf(fmaxf(fy, -kMaxF), kMaxF);
+    fz = fminf(fmaxf(fz, -kMaxF), kMaxF);
+    const int slot = __float_as_int(pi.w);
+    force[slot] = __float2ll_rn(fx * 0x1p32f);
+    force[slot + stride] = __float2ll_rn(fy * 0x1p32f);
+    force[slot + 2 * stride] = __float2ll_rn(fz * 0x1p32f);
+    if (ENERGY) D.e_atom[p] = 0.5 * e;
+}
+
+__global__ void ff_energy(FFDev D) {
+    __shared__ double s[256];
+    const FFSys S = D.sys[blockIdx.x];
+    double e = 0.0;
+    for (int p = S.i0 + threadIdx.x; p < S.i1; p += blockDim.x) e += D.e_atom[p];
+    s[threadIdx.x] = e;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) D.energy[blockIdx.x] = s[0];
+}
+
+__global__ void forces_to_user(const long long* __restrict__ f, int stride, int n, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int c = 0; c < 3; c++) out[3 * i + c] = (double)f[i + c * stride] * 0x1p-32;
+}
+
+}  // namespace
+
+int launch_forces_to_user(const long long* force, int stride, int natoms, double* out, void* stream) {
+    if (natoms == 0) return 0;
+    forces_to_user<<<(natoms + 255) / 256, 256, 0, (cudaStream_t)stream>>>(force, stride, natoms, out);
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (D.n_int == 0) return 0;
+    const int t = 256, g = (D.n_int + t - 1) / t;
+    ff_bin<<<g, t, 0, st>>>(D, B, prec);
+    ff_scan<<<D.S, 256, 0, st>>>(D);
+    ff_scatter<<<g, t, 0, st>>>(D);
+    ff_order<<<(D.n_cells + 127) / 128, 128, 0, st>>>(D, B, prec);
+    const int gf = (D.n_int + 127) / 128;
+    if (energy) {
+        ff_force<true><<<gf, 128, 0, st>>>(D, const_cast<long long*>(B.force), B.stride);
+        ff_energy<<<D.S, 256, 0, st>>>(D);
+    } else {
+        ff_force<false><<<gf, 128, 0, st>>>(D, const_cast<long long*>(B.force), B.stride);
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? (energy ? 6 : 5) : -1;
+}
+
+}  // namespace rbx

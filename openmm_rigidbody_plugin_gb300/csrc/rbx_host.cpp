@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -16,6 +17,7 @@
 #include <vector>
 
 #include "../../include/rbx.h"
+#include "rbx_devarray.h"
 #include "rbx_internal.h"
 #include "rbx_math.cuh"
 
@@ -40,26 +42,6 @@ int fail(int code, const char* fmt, ...) {
         cudaError_t e_ = (call);                                                                  \
         if (e_ != cudaSuccess) return fail(RBX_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
-
-template <class T> struct DevArray {
-    T* p = nullptr;
-    size_t n = 0;
-    ~DevArray() { release(); }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    // The allocation is rounded up to a multiple of 256 bytes, so that bulk L2 prefetches of any
-    // element range, widened to 16-byte boundaries, stay inside it.
-    cudaError_t alloc(size_t count) {
-        release();
-        n = count;
-        if (count == 0) return cudaSuccess;
-        const size_t bytes = ((count * sizeof(T) + 255) / 256) * 256;
-        return cudaMalloc((void**)&p, bytes);
-    }
-};
 
 }  // namespace
 
@@ -128,6 +110,34 @@ struct rbx_integrator {
         if (h_ke) cudaFreeHost(h_ke);
     }
 };
+
+rbx::DevSys rbx::device_system(const rbx_integrator* h) { return h->sys(); }
+
+void rbx::system_ranges(const rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
+                        std::vector<int>& free0, std::vector<int>& dof) {
+    const int S = (int)slot_offsets.size() - 1;
+    body0.assign(S + 1, h->nb);
+    free0.assign(S + 1, h->nf);
+    dof.assign(S, 0);
+    // library order: bodies by their lowest slot, free atoms by slot (both ascending)
+    int s = 0;
+    for (int L = 0; L < h->nb; L++) {
+        int lo = INT32_MAX;
+        for (int k = h->body_first[L]; k < h->body_first[L + 1]; k++) lo = std::min(lo, h->location[h->body_atoms[k]]);
+        while (s < S && lo >= slot_offsets[s + 1]) body0[++s] = L;
+        if (s < S) dof[s] += h->dof[h->lib_body[L]];
+    }
+    for (int t = s + 1; t <= S; t++) body0[t] = h->nb;
+    body0[0] = 0;
+    s = 0;
+    for (int j = 0; j < h->nf; j++) {
+        const int slot = h->location[h->free_atoms[j]];
+        while (s < S && slot >= slot_offsets[s + 1]) free0[++s] = j;
+        if (s < S) dof[s] += 3;
+    }
+    for (int t = s + 1; t <= S; t++) free0[t] = h->nf;
+    free0[0] = 0;
+}
 
 namespace {
 
@@ -655,7 +665,7 @@ int rbx_upload_state(rbx_integrator* h, const double* positions, const double* v
     if (!positions || !velocities) return fail(RBX_ERR_INVALID_ARGUMENT, "null positions or velocities");
     const int nb = h->nb, nbp = h->nb_pad;
     std::vector<double> state((size_t)14 * nbp, 0.0);
-    int ndof = h->nf;
+    int ndof = 3 * h->nf;  // three per free atom (RigidBodySystem.cpp:130 counts one: defect D8)
     for (int b = 0; b < nb; b++) {
         const int f = h->ref_first[b], N = h->ref_first[b + 1] - f;
         BodySetup s;

@@ -16,7 +16,12 @@
 //   tile_body0   int [n_body_tiles+1]: bodies of tile t are [tile_body0[t], tile_body0[t+1])
 #pragma once
 
+#include <vector_types.h>
+
 #include <cstdint>
+#include <vector>
+
+struct rbx_integrator;  // include/rbx.h
 
 namespace rbx {
 
@@ -62,6 +67,36 @@ struct DevBuf {
     int stride;
 };
 
+// Cutoff LJ + reaction-field force field over many independent cubic boxes (rbx_forces.cu).
+// Interacting atoms (non-zero charge or LJ epsilon) are listed system by system; cells of all
+// systems are numbered consecutively.
+struct FFSys {
+    int a0, a1;   // device slots of the system's atoms
+    int i0, i1;   // its interacting atoms, as a range of the interacting-atom list
+    int c0, nc;   // first cell and cells per box edge (1: one cell, all pairs)
+    float L, invL, rc2, krf, crf;
+};
+struct FFDev {
+    int S, n_int, n_cells;
+    const FFSys* sys;     // [S]
+    const int* iatom;     // [n_int] device slot of each interacting atom
+    const int* isys;      // [n_int] its system
+    const float4* param;  // [n_int] sqrt(K) q, sigma/2, sqrt(epsilon), body id (int bits; 0 = free)
+    int* cell_of;         // [n_int]
+    int* cell_count;      // [n_cells], zero between evaluations
+    int* cell_start;      // [n_cells + 1] (entry c0 + nc^3 of each system ends it)
+    int* cell_cursor;     // [n_cells]
+    int* cell_list;       // [n_int] interacting-atom indices in cell order
+    float4* cpos;         // [n_int] cell order: x, y, z, sqrt(K) q
+    float4* cpar;         // [n_int] cell order: sigma/2, sqrt(epsilon), body id, device slot (int bits)
+    double* e_atom;       // [n_int] half pair-energy sums (energy evaluations)
+    double* energy;       // [S] potential energy per system (kJ/mol)
+    float fcap;           // > 0: each atom's force is scaled down to at most this magnitude
+};
+int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* stream);
+// Fixed-point forces of slots [0, natoms) -> user-order doubles out[3*natoms] (kJ/mol/nm).
+int launch_forces_to_user(const long long* force, int stride, int natoms, double* out, void* stream);
+
 struct KEScratch {
     double* partial;      // 2 * n_blocks
     unsigned int* count;  // 1
@@ -82,5 +117,18 @@ size_t step_smem_bytes(int prec);
 
 // Record an error message for rbx_last_error() and return `code` (defined in rbx_host.cpp).
 int set_error(int code, const char* fmt, ...);
+
+// Internal views of an integrator for the batched driver (defined in rbx_host.cpp).
+DevSys device_system(const rbx_integrator* h);
+// For systems whose atoms occupy consecutive device-slot ranges [slot_offsets[s],
+// slot_offsets[s+1]): the library-order ranges of their bodies (body0[S+1]) and free atoms
+// (free0[S+1]), and their degrees of freedom (dof[S]).
+void system_ranges(const rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
+                   std::vector<int>& free0, std::vector<int>& dof);
+// Zero the body COM velocities and quaternion momenta and the free atoms' velocities.
+int launch_zero_momenta(int prec, const DevSys& s, const DevBuf& b, void* stream);
+// [KE_t, KE_r] of each system (out[2*S]), FP64, fixed order, one block per system.
+int launch_kinetic_systems(int prec, const DevSys& s, const DevBuf& b, const int* body0, const int* free0,
+                           int num_systems, double* out, void* stream);
 
 }  // namespace rbx

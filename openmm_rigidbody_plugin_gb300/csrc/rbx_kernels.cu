@@ -629,6 +629,75 @@ __global__ void __launch_bounds__(kKEThreads) kinetic_kernel(DevSys S, DevBuf B,
     }
 }
 
+// [KE_t, KE_r] per system: one block per system over its library-order ranges of bodies and free
+// atoms, FP64, fixed-order tree.
+template <int P>
+__global__ void __launch_bounds__(kKEThreads) kinetic_systems_kernel(DevSys S, DevBuf B, const int* body0,
+                                                                     const int* free0, double* out) {
+    using V4 = typename Tr<P>::V4;
+    __shared__ double s_t[kKEThreads], s_r[kKEThreads];
+    const int sys = blockIdx.x;
+    double kt = 0.0, kr = 0.0;
+    for (int b = body0[sys] + threadIdx.x; b < body0[sys + 1]; b += blockDim.x) {
+        V3<double> v, invI;
+        Q4<double> q, pi;
+        double invm;
+        BodyRead<P>::get(S, b, v, q, pi, invm, invI);
+        V3<double> L = qBt(q, pi) * 0.5;
+        kt += dot(v, v) / invm;
+        kr += dot(L, mul(invI, L));
+    }
+    const V4* vel = (const V4*)B.velm;
+    for (int j = free0[sys] + threadIdx.x; j < free0[sys + 1]; j += blockDim.x) {
+        V4 vm = vel[S.free_loc[j]];
+        double vx = vm.x, vy = vm.y, vz = vm.z;
+        kt += (vx * vx + vy * vy + vz * vz) / (double)vm.w;
+    }
+    s_t[threadIdx.x] = kt;
+    s_r[threadIdx.x] = kr;
+    __syncthreads();
+    for (int w = kKEThreads / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            s_t[threadIdx.x] += s_t[threadIdx.x + w];
+            s_r[threadIdx.x] += s_r[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[2 * sys] = 0.5 * s_t[0];
+        out[2 * sys + 1] = 0.5 * s_r[0];
+    }
+}
+
+// Zero every momentum: body COM velocities and quaternion momenta (both state layouts) and the
+// free atoms' velocities (relaxation by quenched steps).
+template <int P>
+__global__ void zero_momenta_kernel(DevSys S, DevBuf B) {
+    using V4 = typename Tr<P>::V4;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < S.nb) {
+        const int rows[7] = {3, 4, 5, 10, 11, 12, 13};
+        if (P == PREC_DOUBLE) {
+            double* st = (double*)S.state;
+            for (int r : rows) st[i + (size_t)r * S.nb_pad] = 0.0;
+        } else {
+            float* st = (float*)S.state;
+            for (int r : rows) {
+                st[i + (size_t)r * S.nb_pad] = 0.0f;
+                st[i + (size_t)(14 + r) * S.nb_pad] = 0.0f;
+            }
+        }
+    }
+    if (i < S.nf) {
+        V4* vel = (V4*)B.velm;
+        V4 vm = vel[S.free_loc[i]];
+        vm.x = 0;
+        vm.y = 0;
+        vm.z = 0;
+        vel[S.free_loc[i]] = vm;
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // Layout conversion for the host-buffer API (user order doubles <-> OpenMM device layout).
 // ------------------------------------------------------------------------------------------
@@ -724,6 +793,31 @@ static int launch_step_p(int kind, const DevSys& s, const DevBuf& b, double dt, 
         case STEP_PART2: return launch_step_t<P, STEP_PART2, false>(s, b, dt, st);
         default: return exact ? launch_step_t<P, STEP_FUSED, true>(s, b, dt, st) : launch_step_t<P, STEP_FUSED, false>(s, b, dt, st);
     }
+}
+
+int launch_zero_momenta(int prec, const DevSys& s, const DevBuf& b, void* stream) {
+    const int n = s.nb > s.nf ? s.nb : s.nf;
+    if (n == 0) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int g = (n + 255) / 256;
+    switch (prec) {
+        case PREC_SINGLE: zero_momenta_kernel<PREC_SINGLE><<<g, 256, 0, st>>>(s, b); break;
+        case PREC_MIXED: zero_momenta_kernel<PREC_MIXED><<<g, 256, 0, st>>>(s, b); break;
+        default: zero_momenta_kernel<PREC_DOUBLE><<<g, 256, 0, st>>>(s, b); break;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_kinetic_systems(int prec, const DevSys& s, const DevBuf& b, const int* body0, const int* free0,
+                           int num_systems, double* out, void* stream) {
+    if (num_systems <= 0) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (prec) {
+        case PREC_SINGLE: kinetic_systems_kernel<PREC_SINGLE><<<num_systems, kKEThreads, 0, st>>>(s, b, body0, free0, out); break;
+        case PREC_MIXED: kinetic_systems_kernel<PREC_MIXED><<<num_systems, kKEThreads, 0, st>>>(s, b, body0, free0, out); break;
+        default: kinetic_systems_kernel<PREC_DOUBLE><<<num_systems, kKEThreads, 0, st>>>(s, b, body0, free0, out); break;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 int launch_step(int prec, int kind, const DevSys& s, const DevBuf& b, double dt, void* stream) {

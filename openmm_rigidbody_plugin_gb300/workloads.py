@@ -9,9 +9,18 @@ No public dataset is involved: every workload is generated here from a seed.
   6 H radially outside at 0.109 nm, masses 12.011/1.008), plus free LJ atoms (mass 39.95).
 * ``gaussian_forces`` -- seeded per-atom Gaussian forces (sd 500 kJ/mol/nm by default) for
   integrator-only timing.
+* ``batch_systems`` -- many independent mixed systems, each in its own box at 1 g/cm^3, with
+  body counts log-uniform in a range (the batched-replicas case).
 
 Every builder returns a ``System`` with masses, body indices (1-based per molecule, 0 = free
-atom, atoms of a molecule contiguous), positions, velocities and the cubic box edge.
+atom, atoms of a molecule contiguous), positions, velocities, the cubic box edge and the
+species of each atom, from which ``nonbonded`` gives charges and Lennard-Jones parameters.
+
+Nonbonded parameters (cutoff LJ + reaction field): water O -0.834 e, sigma 0.315061 nm,
+epsilon 0.636386 kJ/mol; water H +0.417 e, no LJ; argon 0 e, 0.34 nm, 0.996 kJ/mol. The
+tetrahedra and rings have no published parameters; this project fixes them as neutral, with LJ
+on carbon only (sigma 0.34 nm, epsilon 0.36 kJ/mol) and none on their hydrogens. The cutoff is
+0.9 nm, clamped to 0.49 box edges for boxes too small for it (below 1.84 nm).
 """
 from dataclasses import dataclass, field
 
@@ -35,6 +44,18 @@ RING_MASSES = (12.011,) * 6 + (1.008,) * 6
 ARGON_MASS = 39.95
 ARGON_SIGMA = 0.34
 ARGON_EPSILON = 0.996
+CARBON_SIGMA = 0.34
+CARBON_EPSILON = 0.36
+CUTOFF = 0.9
+
+# species codes and their (charge, sigma, epsilon)
+WATER_O, WATER_H, TETRA_C, TETRA_H, RING_C, RING_H, ARGON = range(7)
+NONBONDED = {WATER_O: (WATER_CHARGES[0], WATER_SIGMA, WATER_EPSILON), WATER_H: (WATER_CHARGES[1], 1.0, 0.0),
+             TETRA_C: (0.0, CARBON_SIGMA, CARBON_EPSILON), TETRA_H: (0.0, 1.0, 0.0),
+             RING_C: (0.0, CARBON_SIGMA, CARBON_EPSILON), RING_H: (0.0, 1.0, 0.0),
+             ARGON: (0.0, ARGON_SIGMA, ARGON_EPSILON)}
+SPECIES = {"water": (WATER_O, WATER_H, WATER_H), "tetra": (TETRA_C,) + (TETRA_H,) * 4,
+           "ring": (RING_C,) * 6 + (RING_H,) * 6}
 
 
 @dataclass
@@ -45,6 +66,7 @@ class System:
     velocities: np.ndarray
     box: float
     kinds: dict = field(default_factory=dict)
+    species: np.ndarray = None
 
     @property
     def num_atoms(self):
@@ -115,7 +137,7 @@ def _assemble(templates, masses_of, kinds, n_free, rng, temperature, box=None, f
     sites = _lattice(nmol + n_free, box)
     order = rng.permutation(nmol + n_free)
     rot = random_rotations(rng, nmol)
-    pos, mass, bidx = [], [], []
+    pos, mass, bidx, spec = [], [], [], []
     body = 0
     kind_count = {}
     for slot in order:
@@ -129,15 +151,17 @@ def _assemble(templates, masses_of, kinds, n_free, rng, temperature, box=None, f
             pos.append(centre + t @ rot[slot].T)
             mass.append(m)
             bidx.append(np.full(len(m), body, dtype=np.int32))
+            spec.append(np.array(SPECIES[k], dtype=np.int8))
             kind_count[k] = kind_count.get(k, 0) + 1
         else:
             pos.append(centre[None, :])
             mass.append(np.array([free_mass]))
             bidx.append(np.zeros(1, dtype=np.int32))
+            spec.append(np.array([ARGON], dtype=np.int8))
     masses = np.concatenate(mass)
     vel = _mb_velocities(rng, masses, temperature)
     kind_count["free"] = n_free
-    return System(masses, np.concatenate(bidx), np.vstack(pos), vel, box, kind_count)
+    return System(masses, np.concatenate(bidx), np.vstack(pos), vel, box, kind_count, np.concatenate(spec))
 
 
 TEMPLATES = {"water": water_template(), "tetra": tetra_template(), "ring": ring_template()}
@@ -192,6 +216,7 @@ def _assemble_fast(kinds, n_free, rng, temperature, free_mass=ARGON_MASS, groupe
     pos = np.empty((natoms, 3))
     mass = np.empty(natoms)
     bidx = np.zeros(natoms, dtype=np.int32)
+    spec = np.full(natoms, ARGON, dtype=np.int8)
     is_mol = seq_kind != 3
     body_id = np.zeros(len(order), dtype=np.int64)
     body_id[is_mol] = np.arange(1, int(is_mol.sum()) + 1)
@@ -212,12 +237,37 @@ def _assemble_fast(kinds, n_free, rng, temperature, free_mass=ARGON_MASS, groupe
         pos[idx] = placed
         mass[idx] = m[None, :]
         bidx[idx] = body_id[sel][:, None]
+        spec[idx] = np.array(SPECIES[n], dtype=np.int8)[None, :]
     vel = _mb_velocities(rng, mass, temperature)
     counts = {n: int(np.count_nonzero(kid == i)) for i, n in enumerate(names)}
     counts["free"] = n_free
-    return System(mass, bidx, pos, vel, box, counts)
+    return System(mass, bidx, pos, vel, box, counts, spec)
 
 
 def gaussian_forces(n_atoms, seed=5, sd=500.0):
     rng = np.random.default_rng(seed)
     return rng.standard_normal((n_atoms, 3)) * sd
+
+
+def nonbonded(system):
+    """Per-atom (charge, sigma, epsilon) arrays of a system from its species."""
+    table = np.array([NONBONDED[k] for k in range(len(NONBONDED))])
+    p = table[system.species.astype(np.int64)]
+    return p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy()
+
+
+def cutoff_for(box):
+    """The 0.9 nm cutoff, clamped to 0.49 box edges where the box is too small for it."""
+    return min(CUTOFF, 0.49 * box)
+
+
+def batch_systems(n_systems=4096, lo=64, hi=4096, fractions=(0.7, 0.2, 0.1), seed=6, temperature=300.0):
+    """Independent mixed systems without free atoms, body counts log-uniform in [lo, hi], each in
+    its own cubic box at 1 g/cm^3 and seeded from `seed` and its index."""
+    rng = np.random.default_rng(seed)
+    counts = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_systems)).astype(np.int64)
+    out = []
+    for k, nb in enumerate(counts):
+        out.append(mixed_system(n_bodies=int(nb), n_free=0, fractions=fractions, seed=seed * 100003 + k,
+                                temperature=temperature))
+    return out

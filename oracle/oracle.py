@@ -73,8 +73,43 @@ def lib():
         L.orc_carlson_rj.argtypes = [ctypes.c_double] * 4
         L.orc_eigen.argtypes = [_dp, _dp, _dp, ctypes.c_int]
         L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_lj_rf.argtypes = [ctypes.c_int, _ip, _dp, _dp, ctypes.c_double, _dp, _dp, _dp, _dp, _ip, _dp, _dp,
+                                ctypes.c_int]
+        L.orc_lj_rf_atoms.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                      _dp, _dp, _dp, _dp, _ip, ctypes.c_int, _ip, _dp]
         _lib = L
     return _lib
+
+
+EPS_SOLVENT = 78.3  # OpenMM's default reaction-field dielectric
+
+
+def lj_rf(atom_offsets, boxes, cutoffs, positions, charges, sigmas, epsilons, bodies, eps_solvent=EPS_SOLVENT,
+          nthreads=None):
+    """FP64 cutoff LJ + reaction-field forces and per-system energies (ff_oracle.c)."""
+    off = np.ascontiguousarray(atom_offsets, dtype=np.int32)
+    S = len(off) - 1
+    n = int(off[-1])
+    f = np.zeros((n, 3))
+    e = np.zeros(S)
+    cast = lambda a, t=np.float64: np.ascontiguousarray(a, dtype=t)
+    pos, q, sg, ep = cast(positions), cast(charges), cast(sigmas), cast(epsilons)
+    bd = cast(bodies, np.int32)
+    bx, rc = cast(np.broadcast_to(boxes, (S,))), cast(np.broadcast_to(cutoffs, (S,)))
+    lib().orc_lj_rf(S, _i(off), _d(bx), _d(rc), eps_solvent, _d(pos), _d(q), _d(sg), _d(ep), _i(bd), _d(f), _d(e),
+                    nthreads or (os.cpu_count() or 1))
+    return f, e
+
+
+def lj_rf_atoms(selected, box, cutoff, positions, charges, sigmas, epsilons, bodies, eps_solvent=EPS_SOLVENT):
+    """FP64 forces on the selected atoms of one box (all atoms of `positions` in that box)."""
+    sel = np.ascontiguousarray(selected, dtype=np.int32)
+    cast = lambda a, t=np.float64: np.ascontiguousarray(a, dtype=t)
+    pos, q, sg, ep, bd = cast(positions), cast(charges), cast(sigmas), cast(epsilons), cast(bodies, np.int32)
+    f = np.zeros((len(sel), 3))
+    lib().orc_lj_rf_atoms(0, len(pos), box, cutoff, eps_solvent, _d(pos), _d(q), _d(sg), _d(ep), _i(bd), len(sel),
+                          _i(sel), _d(f))
+    return f
 
 
 class _Base:

@@ -830,7 +830,9 @@ static void build_dynamics(orc_system* s, int b, const double* V) {
 }
 
 int orc_setup(orc_system* s, const double* R, const double* V, const double* F) {
-    s->ndof = s->nfree;
+    /* RigidBodySystem.cpp:130 counts one degree of freedom per free atom (defect D8); the robust
+     * oracle counts three */
+    s->ndof = s->robust ? 3 * s->nfree : s->nfree;
     for (int b = 0; b < s->nbodies; b++) {
         build_geometry(s, b, R, F);
         s->ndof += s->bdof[b];

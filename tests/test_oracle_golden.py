@@ -109,3 +109,17 @@ def test_single_bond_known_answer(oracle_mod, golden):
         F = force(o.R)
         o.part2(dt, F)
     assert abs(int(g["nsteps"]) * dt - 10.0) < 1e-12
+
+
+def test_free_atoms_count_three_degrees_of_freedom_in_the_robust_oracle(oracle_mod, golden):
+    """Defect D8: RigidBodySystem.cpp:130 counts one degree of freedom per free atom; the
+    reference-mode oracle keeps that count, the robust oracle (and the library) count three."""
+    g = golden("water64_mode0")
+    nfree = int(np.sum(g["body_indices"] == 0))
+    assert nfree > 0
+    ref = oracle_mod.Oracle(g["masses"], g["body_indices"], mode=0, robust=False)
+    rob = oracle_mod.Oracle(g["masses"], g["body_indices"], mode=0, robust=True)
+    ref.setup(g["R0"], g["V0"], g["F"])
+    rob.setup(g["R0"], g["V0"], g["F"])
+    assert ref.num_dof == int(g["dof"])
+    assert rob.num_dof == int(g["dof"]) + 2 * nfree
