@@ -66,6 +66,16 @@ def parse():
     p.add_argument("--reference-seconds", type=float, default=90.0,
                    help="bound on the timed CPU work of --impl reference")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--workload", default="single", choices=["single", "batched", "water"],
+                   help="single: the 1e6-body integrator step (default); batched: many independent systems, "
+                        "full steps with the cell-list force field, against one system per launch; water: "
+                        "512 rigid waters, full steps")
+    p.add_argument("--systems", type=int, default=4096, help="batched: number of systems")
+    p.add_argument("--relax-steps", type=int, default=400, help="batched/water: relaxation before dynamics")
+    p.add_argument("--graph-steps", type=int, default=50, help="batched/water: steps per captured CUDA graph")
+    p.add_argument("--plain-systems", type=int, default=32, help="batched: systems run one per launch")
+    p.add_argument("--plain-steps", type=int, default=0,
+                   help="batched: steps of the one-per-launch arm (0: the same as --steps)")
     return p.parse_args()
 
 
@@ -228,6 +238,8 @@ def run_reference(args, world, rank):
     step integrates a seeded sample of the same mix, sized to fit that time."""
     if rank != 0:
         return
+    if args.workload in ("batched", "water"):
+        return run_reference_full_steps(args)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
@@ -354,11 +366,207 @@ def run_gpu(args, world, rank, local):
     print(json.dumps(out), flush=True)
 
 
+def _drift(e_pre, e_post, steps, dt, dof):
+    """Energy drift per system: kJ/mol/ns/DOF and |dE|/|E0| of the total energy U + KE_t + KE_r."""
+    tot0, tot1 = e_pre.sum(axis=1), e_post.sum(axis=1)
+    per_ns = (tot1 - tot0) / (steps * dt * 1e-3) / np.asarray(dof, dtype=np.float64)
+    rel = np.abs(tot1 - tot0) / np.abs(tot0)
+    return {"kj_mol_ns_dof_median_abs": float(np.median(np.abs(per_ns))),
+            "kj_mol_ns_dof_max_abs": float(np.max(np.abs(per_ns))),
+            "rel_dE_median": float(np.median(rel)), "rel_dE_max": float(np.max(rel))}
+
+
+def cpu_full_steps(systems, x, v, offsets, seconds):
+    """The oracle's full step (CPU port of the reference integrator + FP64 O(N^2) LJ + reaction-field
+    forces on all host threads) over the given systems, for about `seconds`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    threads = os.cpu_count() or 1
+    runs = []
+    for k, s in enumerate(systems):
+        q, sg, ep = W.nonbonded(s)
+        rc = W.cutoff_for(s.box)
+        o = oracle.Oracle(s.masses, s.body_indices, mode=0, robust=True)
+        force = (lambda R, s=s, q=q, sg=sg, ep=ep, rc=rc:
+                 oracle.lj_rf([0, s.num_atoms], [s.box], [rc], R, q, sg, ep, s.body_indices, nthreads=threads)[0])
+        o.setup(x[offsets[k]:offsets[k + 1]], v[offsets[k]:offsets[k + 1]], force(x[offsets[k]:offsets[k + 1]]))
+        runs.append((o, force, s.num_bodies))
+    steps, body_steps, t0 = 0, 0, time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        for o, force, nb in runs:
+            o.part1(0.002, force(o.R))
+            o.part2(0.002, force(o.R))
+            body_steps += nb
+        steps += 1
+    t = time.perf_counter() - t0
+    return {"value": body_steps / t, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(runs)} systems ({sum(r[2] for r in runs)} bodies), {steps} full steps each "
+                      f"(integrator + FP64 all-pairs LJ/RF forces on {threads} threads), {t:.1f} s"}
+
+
+def run_reference_full_steps(args):
+    """CPU full steps (oracle integrator + FP64 LJ/RF forces, all host threads) on the batched or
+    water workload: the smallest systems of the batch (a bounded sample; the starting structures
+    are the generated ones, not relaxed, since the relaxation runs on the GPU)."""
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    if args.workload == "water":
+        systems = [W.water_box(512, seed=1)]
+    else:
+        allsys = W.batch_systems(args.systems, lo=64, hi=4096, seed=6)
+        systems = [allsys[k] for k in np.argsort([s.num_bodies for s in allsys])[:4]]
+    x = np.concatenate([s.positions for s in systems])
+    v = np.concatenate([s.velocities for s in systems])
+    offs = np.concatenate([[0], np.cumsum([s.num_atoms for s in systems])])
+    r = cpu_full_steps(systems, x, v, offs, args.reference_seconds / 3)
+    out = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": args.workload, "implementation": "CPU port of RigidBodySystem::integratePart1/2 "
+                      "(robust variant) + FP64 all-pairs cutoff LJ/RF forces"},
+           "cpu_baseline": r, "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                                      "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def run_batched(args, world, rank, local):
+    """Many independent systems stepped together (full steps: cell-list forces + integrator, runs of
+    graph_steps steps replayed from one captured CUDA graph), against the same systems stepped one
+    system per launch."""
+    import torch
+    from openmm_rigidbody_plugin_gb300 import batch, build
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    torch.cuda.set_device(local)
+    build.build_library()
+    dt = 0.002
+    if args.workload == "water":
+        systems = [W.water_box(512, seed=1 + 1000 * rank)]
+        name = ("512 rigid 3-site waters, cubic box at 1 g/cm3, cutoff 0.9 nm LJ + reaction field, "
+                "dt 2 fs, rotation mode 0, mixed precision, full steps")
+    else:
+        systems = W.batch_systems(args.systems, lo=64, hi=4096, seed=6 + 1000 * rank)
+        name = (f"batched replicas: {args.systems} independent systems, body counts log-uniform in [64, 4096] "
+                "(70% water, 20% tetrahedra, 10% rings), each in its own box at 1 g/cm3, cutoff 0.9 nm "
+                "(0.49 box below 1.84 nm) LJ + reaction field, dt 2 fs, rotation mode 0, mixed precision, "
+                f"full steps, {args.graph_steps} steps per captured CUDA graph")
+    nb = sum(s.num_bodies for s in systems)
+    na = sum(s.num_atoms for s in systems)
+    t0 = time.perf_counter()
+    b = batch.BatchedSystems.from_systems(systems, relax_steps=args.relax_steps, device=local)
+    b.set_graph_steps(args.graph_steps)
+    setup_s = time.perf_counter() - t0
+    dof = b.num_dof
+    b.step(max(args.warmup, 3), dt)
+    x0, v0 = b.get_state()
+    b.set_state(x0, v0)  # both arms start here
+    e_pre = b.energies()
+    stream = torch.cuda.current_stream()
+    torch.cuda.synchronize()
+    barrier(world)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        time.sleep(0.3)
+        torch.cuda.synchronize()
+        clocks.mark_start()
+        start.record(stream)
+        b.step(args.steps, dt)
+        end.record(stream)
+        torch.cuda.synchronize()
+        clocks.mark_end()
+    launches = b.last_launch_count
+    t_dev = max_over_ranks(start.elapsed_time(end) / 1e3, world)
+    e_post = b.energies()
+    value = world * nb * args.steps / t_dev
+    drift = _drift(e_pre, e_post, args.steps, dt, dof)
+
+    # kernel split (event-timed direct launches; same work)
+    b.set_timing(True)
+    b.step(20, dt)
+    ms_f, ms_i, _ = b.kernel_times()
+    b.set_timing(False)
+    bytes_step = BYTES_PER_BODY["mixed"] * nb + BYTES_PER_BODY_ATOM["mixed"] * na
+    t_int = ms_i / 21 / 1e3  # part1 + 19 fused + part2
+    peak, peak_kind = peaks()
+    achieved = bytes_step / t_int / 1e9
+
+    # e2e: the public call a user makes, chunks of 10 steps, energies read back per chunk
+    chunks = 3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(chunks):
+        b.step(10, dt)
+        b.energies()
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / (10 * chunks), world)
+    e2e = {"value": world * nb / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
+           "d2h_bytes_per_step": int(24 * len(systems) / 10),
+           "call": "BatchedSystems.step(10) + energies() per chunk (rbx_batch_step, rbx_batch_energies)"}
+
+    # the same systems, one system per launch (the plain drop-in way: one context per system)
+    plain = None
+    if args.workload == "batched" and args.plain_systems > 0:
+        idx = np.unique(np.linspace(0, len(systems) - 1, min(args.plain_systems, len(systems))).astype(int))
+        off = b.offsets
+        handles = []
+        for k in idx:
+            h = batch.BatchedSystems.from_systems([systems[k]], device=local)
+            h.set_state(x0[off[k]:off[k + 1]], v0[off[k]:off[k + 1]])
+            handles.append(h)
+        plain_steps = args.plain_steps or args.steps
+        e_pre_p = np.array([h.energies()[0] for h in handles])
+        torch.cuda.synchronize()
+        pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pa.record(stream)
+        for h in handles:
+            h.step(plain_steps, dt)
+        pb.record(stream)
+        torch.cuda.synchronize()
+        t_plain = pa.elapsed_time(pb) / 1e3
+        e_post_p = np.array([h.energies()[0] for h in handles])
+        nb_p = sum(systems[k].num_bodies for k in idx)
+        plain = {"value": nb_p * plain_steps / t_plain, "unit": UNIT, "systems": int(len(idx)),
+                 "bodies": int(nb_p), "steps": plain_steps,
+                 "energy_drift": _drift(e_pre_p, e_post_p, plain_steps, dt, dof[idx]),
+                 "how": "each system its own handle (rbx_batch of one system), steps launched system after system"}
+        if plain_steps == args.steps:  # the same systems inside the batch, over the same steps
+            plain["batched_energy_drift_same_systems"] = _drift(e_pre[idx], e_post[idx], args.steps, dt, dof[idx])
+            plain["same_final_energies_as_batched"] = bool(np.array_equal(e_post_p, e_post[idx]))
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu:
+        pick = [0] if args.workload == "water" else list(np.argsort([s.num_bodies for s in systems])[:4])
+        off = b.offsets
+        sub = [systems[k] for k in pick]
+        xs = np.concatenate([x0[off[k]:off[k + 1]] for k in pick])
+        vs = np.concatenate([v0[off[k]:off[k + 1]] for k in pick])
+        offs = np.concatenate([[0], np.cumsum([s.num_atoms for s in sub])])
+        cpu = cpu_full_steps(sub, xs, vs, offs, args.cpu_seconds)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32 atoms + f64 body state", "data": "synthetic",
+           "config": {"workload": name, "systems_per_gpu": len(systems), "bodies_per_gpu": nb, "atoms_per_gpu": na,
+                      "relax_steps": args.relax_steps, "setup_seconds": setup_s,
+                      "l2": "working set > 129 MB L2" if na * 120 > 129e6 else "working set fits in L2",
+                      "parallelism": f"{world} independent replicas"},
+           "energy_drift": drift, "plain": plain,
+           "speedup_vs_plain": (value / world / plain["value"]) if plain else None,
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "peak_source": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": bytes_step,
+                        "kernel": "rbx::step_kernel (integrator launches of the full step)",
+                        "integrator_ms_per_step": ms_i / 20, "force_ms_per_step": ms_f / 21,
+                        "force_share": ms_f / (ms_f + ms_i)},
+           "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(), "gpu_launches": launches}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, world, rank)
+    elif args.workload in ("batched", "water"):
+        run_batched(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

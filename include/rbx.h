@@ -210,15 +210,21 @@ int rbx_batch_destroy(rbx_batch* b);
 int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, const double* velocities);
 int rbx_batch_get_state(rbx_batch* b, void* stream, double* positions, double* velocities);
 int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt);
-/* Relaxation by quenched steps: nsteps times (forces capped at max_force kJ/mol/nm per atom, every
- * momentum zeroed, part1 of size dt), then every momentum zeroed. Removes the overlaps of
- * generated starting structures before dynamics; velocities are then reassigned by
- * rbx_batch_set_state. Not a step of the reference, which takes its starting state as given. */
-int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double max_force);
+/* Relaxation by damped dynamics: nsteps times (forces capped at max_force kJ/mol/nm per atom,
+ * every momentum scaled by `damping` in [0, 1), part1 of size dt), then every momentum zeroed.
+ * Removes the overlaps of generated starting structures before dynamics; velocities are then
+ * reassigned by rbx_batch_set_state. Not a step of the reference, which takes its starting state
+ * as given. */
+int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double max_force, double damping);
 int rbx_batch_energies(rbx_batch* b, void* stream, double* out /* [3*S] */);
 int rbx_batch_forces(rbx_batch* b, void* stream, double* forces /* [N*3], user order */, double* energies /* [S] */);
 int rbx_batch_get_num_dof(rbx_batch* b, int* dof /* [S] */);
 int rbx_batch_set_graph_steps(rbx_batch* b, int k);
+/* Event timing of the force and integrator launch groups of later calls (direct launches only:
+ * graphs are not used while timing is on); rbx_batch_kernel_times waits for and sums them
+ * (milliseconds) and starts a new tally. */
+int rbx_batch_set_timing(rbx_batch* b, int on);
+int rbx_batch_kernel_times(rbx_batch* b, double* ms_forces, double* ms_integrator, int* groups);
 int rbx_batch_last_launch_count(const rbx_batch* b);
 
 #ifdef __cplusplus

@@ -68,10 +68,11 @@ class BatchedSystems:
             b.thermalize(temperature, seed)
         return b
 
-    def relax(self, nsteps=300, dt=0.005, max_force=5000.0, stream=None):
-        """Quenched steps (forces capped at max_force, momenta zeroed each step) that remove the
-        overlaps of generated starting structures; leaves every momentum at zero."""
-        _lib.check(self._lib.rbx_batch_relax(self._h, _stream(stream), int(nsteps), float(dt), float(max_force)))
+    def relax(self, nsteps=400, dt=0.002, max_force=2000.0, damping=0.7, stream=None):
+        """Damped dynamics (forces capped at max_force, momenta scaled by `damping` each step) that
+        removes the overlaps of generated starting structures; leaves every momentum at zero."""
+        _lib.check(self._lib.rbx_batch_relax(self._h, _stream(stream), int(nsteps), float(dt), float(max_force),
+                                             float(damping)))
 
     def thermalize(self, temperature=300.0, seed=0, stream=None):
         """Seeded Maxwell-Boltzmann velocities at the current positions (projected onto rigid motion
@@ -124,6 +125,15 @@ class BatchedSystems:
 
     def set_graph_steps(self, k):
         _lib.check(self._lib.rbx_batch_set_graph_steps(self._h, int(k)))
+
+    def set_timing(self, on):
+        _lib.check(self._lib.rbx_batch_set_timing(self._h, int(bool(on))))
+
+    def kernel_times(self):
+        """(ms in force kernels, ms in integrator kernels, launch groups) since the last call."""
+        f, i, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_int()
+        _lib.check(self._lib.rbx_batch_kernel_times(self._h, ctypes.byref(f), ctypes.byref(i), ctypes.byref(n)))
+        return f.value, i.value, n.value
 
     @property
     def last_launch_count(self):

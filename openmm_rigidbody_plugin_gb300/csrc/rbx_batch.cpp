@@ -61,6 +61,12 @@ struct rbx_batch {
     bool forces_valid = false;
     int last_launches = 0;
     // captured runs of (forces, fused step)
+    // optional event timing of the force and integrator launch groups (direct launches only)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, int>> ev_marks;  // (start event, end event) per group
+    std::vector<int> ev_kind;                   // 0 = forces, 1 = integrator
+    int ev_used = 0;
     int graph_k = 0;
     int graph_launches = 0;  // kernels in one replay of the graph
     double graph_dt = 0.0;
@@ -71,7 +77,16 @@ struct rbx_batch {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
     }
+    cudaEvent_t event() {
+        if (ev_used == (int)ev_pool.size()) {
+            cudaEvent_t e = nullptr;
+            if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            ev_pool.push_back(e);
+        }
+        return ev_pool[ev_used++];
+    }
     ~rbx_batch() {
+        for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
         drop_graph();
         if (cap_stream) cudaStreamDestroy(cap_stream);
         if (h_out) cudaFreeHost(h_out);
@@ -95,23 +110,54 @@ DevBuf buffers(rbx_batch* b) {
     return d;
 }
 
+// Event pair around one launch group when timing is on (never inside a stream capture).
+struct Timed {
+    rbx_batch* b;
+    void* stream;
+    int kind, start = -1;
+    Timed(rbx_batch* b_, void* s, int k) : b(b_), stream(s), kind(k) {
+        if (b->timing) {
+            start = b->ev_used;
+            cudaEvent_t e = b->event();
+            if (e) cudaEventRecord(e, (cudaStream_t)stream); else start = -1;
+        }
+    }
+    ~Timed() {
+        if (start < 0) return;
+        const int end = b->ev_used;
+        cudaEvent_t e = b->event();
+        if (!e) return;
+        cudaEventRecord(e, (cudaStream_t)stream);
+        b->ev_marks.push_back({start, end});
+        b->ev_kind.push_back(kind);
+    }
+};
+
 int forces(rbx_batch* b, void* stream, bool energy) {
+    Timed t(b, stream, 0);
     const int n = launch_forces(b->ff, b->prec, buffers(b), energy, stream);
     if (n < 0) return set_error(RBX_ERR_CUDA, "force kernels failed: %s", cudaGetErrorString(cudaGetLastError()));
     b->last_launches += n;
     return RBX_OK;
 }
 
-int fused(rbx_batch* b, void* stream, double dt) {
+int integrate(rbx_batch* b, void* stream, int kind, double dt) {
+    Timed t(b, stream, 1);
     rbx_buffers rb;
     rbx_context_buffers(b->integ, &rb);
-    int rc = rbx_integrate_fused(b->integ, stream, &rb, dt);
+    int rc = kind == STEP_PART1 ? rbx_integrate_part1(b->integ, stream, &rb, dt)
+             : kind == STEP_PART2 ? rbx_integrate_part2(b->integ, stream, &rb, dt)
+                                  : rbx_integrate_fused(b->integ, stream, &rb, dt);
     if (!rc) b->last_launches += 1;
     return rc;
 }
 
+int fused(rbx_batch* b, void* stream, double dt) { return integrate(b, stream, STEP_FUSED, dt); }
+
 int capture(rbx_batch* b, double dt) {
     b->drop_graph();
+    const bool timing = b->timing;
+    b->timing = false;  // no event records inside the capture
     if (!b->cap_stream) BATCH_TRY(cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking));
     BATCH_TRY(cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeRelaxed));
     int rc = RBX_OK;
@@ -122,6 +168,7 @@ int capture(rbx_batch* b, double dt) {
     }
     b->graph_launches = b->last_launches - before;
     b->last_launches = before;
+    b->timing = timing;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(b->cap_stream, &g);
     if (rc) {
@@ -293,13 +340,10 @@ int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
     BATCH_TRY(cudaSetDevice(b->device));
     b->last_launches = 0;
-    rbx_buffers rb;
-    rbx_context_buffers(b->integ, &rb);
     if (!b->forces_valid && (rc = forces(b, stream, false))) return rc;
-    if ((rc = rbx_integrate_part1(b->integ, stream, &rb, dt))) return rc;
-    b->last_launches += 1;
+    if ((rc = integrate(b, stream, STEP_PART1, dt))) return rc;
     int remaining = nsteps - 1;
-    if (b->graph_k > 0 && remaining >= b->graph_k) {
+    if (b->graph_k > 0 && !b->timing && remaining >= b->graph_k) {
         if (!b->graph || b->graph_dt != dt) {
             if ((rc = capture(b, dt))) return rc;
         }
@@ -313,17 +357,17 @@ int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {
         if ((rc = forces(b, stream, false)) || (rc = fused(b, stream, dt))) return rc;
     }
     if ((rc = forces(b, stream, false))) return rc;
-    if ((rc = rbx_integrate_part2(b->integ, stream, &rb, dt))) return rc;
-    b->last_launches += 1;
+    if ((rc = integrate(b, stream, STEP_PART2, dt))) return rc;
     b->forces_valid = true;
     return RBX_OK;
 }
 
-int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double max_force) {
+int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double max_force, double damping) {
     int rc = check(b);
     if (rc) return rc;
-    if (nsteps < 1 || !(dt > 0.0) || !(max_force > 0.0))
-        return set_error(RBX_ERR_INVALID_ARGUMENT, "relaxation needs nsteps >= 1, dt > 0 and max_force > 0");
+    if (nsteps < 1 || !(dt > 0.0) || !(max_force > 0.0) || !(damping >= 0.0 && damping < 1.0))
+        return set_error(RBX_ERR_INVALID_ARGUMENT,
+                         "relaxation needs nsteps >= 1, dt > 0, max_force > 0 and 0 <= damping < 1");
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
     BATCH_TRY(cudaSetDevice(b->device));
     b->last_launches = 0;
@@ -333,14 +377,14 @@ int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double ma
     b->ff.fcap = (float)max_force;
     for (int n = 0; n < nsteps && !rc; n++) {
         rc = forces(b, stream, false);
-        if (!rc && launch_zero_momenta(b->prec, sys, buffers(b), stream) < 0)
-            rc = set_error(RBX_ERR_CUDA, "momentum reset failed");
+        if (!rc && launch_scale_momenta(b->prec, sys, buffers(b), damping, stream) < 0)
+            rc = set_error(RBX_ERR_CUDA, "momentum damping failed");
         if (!rc) rc = rbx_integrate_part1(b->integ, stream, &rb, dt);
         b->last_launches += 2;
     }
     b->ff.fcap = 0.0f;
     if (rc) return rc;
-    if (launch_zero_momenta(b->prec, sys, buffers(b), stream) < 0) return set_error(RBX_ERR_CUDA, "momentum reset failed");
+    if (launch_scale_momenta(b->prec, sys, buffers(b), 0.0, stream) < 0) return set_error(RBX_ERR_CUDA, "momentum reset failed");
     b->forces_valid = false;
     return RBX_OK;
 }
@@ -404,6 +448,35 @@ int rbx_batch_set_graph_steps(rbx_batch* b, int k) {
     if (k < 0) return set_error(RBX_ERR_INVALID_ARGUMENT, "graph run length must be >= 0");
     if (k != b->graph_k) b->drop_graph();
     b->graph_k = k;
+    return RBX_OK;
+}
+
+int rbx_batch_set_timing(rbx_batch* b, int on) {
+    int rc = check(b);
+    if (rc) return rc;
+    b->timing = on != 0;
+    b->ev_marks.clear();
+    b->ev_kind.clear();
+    b->ev_used = 0;
+    return RBX_OK;
+}
+
+int rbx_batch_kernel_times(rbx_batch* b, double* ms_forces, double* ms_integrator, int* groups) {
+    int rc = check(b);
+    if (rc) return rc;
+    double t[2] = {0.0, 0.0};
+    for (size_t i = 0; i < b->ev_marks.size(); i++) {
+        float ms = 0.0f;
+        BATCH_TRY(cudaEventSynchronize(b->ev_pool[b->ev_marks[i].second]));
+        BATCH_TRY(cudaEventElapsedTime(&ms, b->ev_pool[b->ev_marks[i].first], b->ev_pool[b->ev_marks[i].second]));
+        t[b->ev_kind[i]] += ms;
+    }
+    if (ms_forces) *ms_forces = t[0];
+    if (ms_integrator) *ms_integrator = t[1];
+    if (groups) *groups = (int)b->ev_marks.size();
+    b->ev_marks.clear();
+    b->ev_kind.clear();
+    b->ev_used = 0;
     return RBX_OK;
 }
 

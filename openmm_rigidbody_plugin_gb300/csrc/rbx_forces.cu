@@ -158,6 +158,7 @@ __global__ void __launch_bounds__(128) ff_force(FFDev D, long long* __restrict__
         dz -= S.L * rintf(dz * S.invL);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         if (r2 >= S.rc2) return;
+        if (D.fcap > 0.0f && r2 < 1e-8f) return;  // relaxation: coincident atoms have no direction
         const float inv_r2 = 1.0f / r2, inv_r = rsqrtf(r2);
         const float qq = xi.w * xq.w;
         const float sig = pi.x + pq.x, eps = pi.y * pq.y;

@@ -125,8 +125,8 @@ DevSys device_system(const rbx_integrator* h);
 // (free0[S+1]), and their degrees of freedom (dof[S]).
 void system_ranges(const rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
                    std::vector<int>& free0, std::vector<int>& dof);
-// Zero the body COM velocities and quaternion momenta and the free atoms' velocities.
-int launch_zero_momenta(int prec, const DevSys& s, const DevBuf& b, void* stream);
+// Scale the body COM velocities and quaternion momenta and the free atoms' velocities.
+int launch_scale_momenta(int prec, const DevSys& s, const DevBuf& b, double factor, void* stream);
 // [KE_t, KE_r] of each system (out[2*S]), FP64, fixed order, one block per system.
 int launch_kinetic_systems(int prec, const DevSys& s, const DevBuf& b, const int* body0, const int* free0,
                            int num_systems, double* out, void* stream);

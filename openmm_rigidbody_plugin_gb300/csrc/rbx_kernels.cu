@@ -669,31 +669,32 @@ __global__ void __launch_bounds__(kKEThreads) kinetic_systems_kernel(DevSys S, D
     }
 }
 
-// Zero every momentum: body COM velocities and quaternion momenta (both state layouts) and the
-// free atoms' velocities (relaxation by quenched steps).
+// Scale every momentum by `factor`: body COM velocities and quaternion momenta (both state
+// layouts) and the free atoms' velocities (damped relaxation; 0 zeroes them).
 template <int P>
-__global__ void zero_momenta_kernel(DevSys S, DevBuf B) {
+__global__ void scale_momenta_kernel(DevSys S, DevBuf B, double factor) {
     using V4 = typename Tr<P>::V4;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < S.nb) {
         const int rows[7] = {3, 4, 5, 10, 11, 12, 13};
         if (P == PREC_DOUBLE) {
             double* st = (double*)S.state;
-            for (int r : rows) st[i + (size_t)r * S.nb_pad] = 0.0;
+            for (int r : rows) st[i + (size_t)r * S.nb_pad] *= factor;
         } else {
             float* st = (float*)S.state;
+            const float f = (float)factor;
             for (int r : rows) {
-                st[i + (size_t)r * S.nb_pad] = 0.0f;
-                st[i + (size_t)(14 + r) * S.nb_pad] = 0.0f;
+                st[i + (size_t)r * S.nb_pad] *= f;
+                st[i + (size_t)(14 + r) * S.nb_pad] *= f;
             }
         }
     }
     if (i < S.nf) {
         V4* vel = (V4*)B.velm;
         V4 vm = vel[S.free_loc[i]];
-        vm.x = 0;
-        vm.y = 0;
-        vm.z = 0;
+        vm.x *= factor;
+        vm.y *= factor;
+        vm.z *= factor;
         vel[S.free_loc[i]] = vm;
     }
 }
@@ -795,15 +796,15 @@ static int launch_step_p(int kind, const DevSys& s, const DevBuf& b, double dt, 
     }
 }
 
-int launch_zero_momenta(int prec, const DevSys& s, const DevBuf& b, void* stream) {
+int launch_scale_momenta(int prec, const DevSys& s, const DevBuf& b, double factor, void* stream) {
     const int n = s.nb > s.nf ? s.nb : s.nf;
     if (n == 0) return 0;
     cudaStream_t st = (cudaStream_t)stream;
     const int g = (n + 255) / 256;
     switch (prec) {
-        case PREC_SINGLE: zero_momenta_kernel<PREC_SINGLE><<<g, 256, 0, st>>>(s, b); break;
-        case PREC_MIXED: zero_momenta_kernel<PREC_MIXED><<<g, 256, 0, st>>>(s, b); break;
-        default: zero_momenta_kernel<PREC_DOUBLE><<<g, 256, 0, st>>>(s, b); break;
+        case PREC_SINGLE: scale_momenta_kernel<PREC_SINGLE><<<g, 256, 0, st>>>(s, b, factor); break;
+        case PREC_MIXED: scale_momenta_kernel<PREC_MIXED><<<g, 256, 0, st>>>(s, b, factor); break;
+        default: scale_momenta_kernel<PREC_DOUBLE><<<g, 256, 0, st>>>(s, b, factor); break;
     }
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }

@@ -7,6 +7,10 @@ No public dataset is involved: every workload is generated here from a seed.
 * ``mixed_system`` -- the single-large-system case: 70 % waters, 20 % 5-atom tetrahedra
   (C + 4 H at 0.109 nm, masses 12/1), 10 % 12-atom planar rings (6 C on a 0.14 nm hexagon,
   6 H radially outside at 0.109 nm, masses 12.011/1.008), plus free LJ atoms (mass 39.95).
+  Molecules sit on a cubic lattice at 1 g/cm^3 with random orientations, except that the rings
+  take sites two lattice spacings apart and a staggered orientation (plane normal along a random
+  body diagonal, carbons between the neighbours), so that no carbons of neighbouring molecules
+  start inside each other's Lennard-Jones core.
 * ``gaussian_forces`` -- seeded per-atom Gaussian forces (sd 500 kJ/mol/nm by default) for
   integrator-only timing.
 * ``batch_systems`` -- many independent mixed systems, each in its own box at 1 g/cm^3, with
@@ -190,6 +194,57 @@ def mixed_system(n_bodies=1_000_000, n_free=100_000, fractions=(0.7, 0.2, 0.1), 
     return _assemble_fast(kinds, n_free, rng, temperature, grouped=grouped)
 
 
+def _mixed_sites(kid, ntot, box, rng):
+    """Lattice site of each slot (molecules, then free atoms). Rings take random points of the
+    sublattice of all-even grid indices (not touching across the periodic boundary), so that no
+    two rings are nearest neighbours (their carbon hexagons would interpenetrate); the grid is
+    refined until that sublattice holds every ring. The other slots take the remaining points
+    with the fewest ring neighbours first, so that small boxes leave their vacancies next to
+    rings."""
+    ring_slots = np.nonzero(kid == 2)[0]
+    sub_count = lambda k: ((k - 1) // 2 + (1 if k % 2 == 0 else 0)) ** 3 if k > 1 else 1
+    k = int(np.ceil(ntot ** (1.0 / 3.0) - 1e-9))
+    while sub_count(k) < len(ring_slots):
+        k += 1
+    g = (np.arange(k) + 0.5) * (box / k)
+    ii, jj, kk = (a.ravel() for a in np.meshgrid(np.arange(k), np.arange(k), np.arange(k), indexing="ij"))
+    grid = np.stack([g[ii], g[jj], g[kk]], axis=1)
+    top = k - 1 if k % 2 else k  # with an odd edge, indices 0 and k-1 are periodic neighbours
+    even = lambda a: (a % 2 == 0) & (a < top)
+    sub = np.nonzero(even(ii) & even(jj) & even(kk))[0]
+    site_of = np.empty(ntot, dtype=np.int64)
+    site_of[ring_slots] = rng.choice(sub, len(ring_slots), replace=False)
+    others = np.setdiff1d(np.arange(ntot), ring_slots)
+    taken = np.zeros(k ** 3, dtype=bool)
+    taken[site_of[ring_slots]] = True
+    # ring neighbours of each point (the 26 surrounding points, periodic)
+    near = np.zeros((k, k, k), dtype=np.int32)
+    rmask = taken.reshape(k, k, k).astype(np.int32)
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                if dx or dy or dz:
+                    near += np.roll(rmask, (dx, dy, dz), axis=(0, 1, 2))
+    free_points = np.nonzero(~taken)[0]
+    key = near.ravel()[free_points] + rng.random(len(free_points))  # random among equals
+    site_of[others] = free_points[np.argsort(key)[:len(others)]]
+    return grid[site_of]
+
+
+def _ring_rotations(rng, n):
+    """Ring orientations: the plane normal along a random body diagonal of the lattice and the
+    hexagon turned so that its carbons point between the in-plane projections of the six face
+    neighbours (30 degrees from them)."""
+    normal = rng.choice([-1.0, 1.0], size=(n, 3)) / np.sqrt(3.0)
+    x = np.array([1.0, 0.0, 0.0])
+    e1 = x - normal * (normal @ x)[:, None]
+    e1 /= np.linalg.norm(e1, axis=1)[:, None]
+    e2 = np.cross(normal, e1)
+    u = np.cos(np.pi / 6) * e1 + np.sin(np.pi / 6) * e2
+    v = np.cross(normal, u)
+    return np.stack([u, v, normal], axis=2)  # columns: images of the template's x, y, z axes
+
+
 def _assemble_fast(kinds, n_free, rng, temperature, free_mass=ARGON_MASS, grouped=False):
     """Vectorised version of _assemble for millions of molecules."""
     names = ["water", "tetra", "ring"]
@@ -199,9 +254,11 @@ def _assemble_fast(kinds, n_free, rng, temperature, free_mass=ARGON_MASS, groupe
     total_mass = sum(np.sum(MASSES[n]) * np.count_nonzero(kid == i) for i, n in enumerate(names))
     total_mass += n_free * free_mass
     box = _box_for_mass(total_mass)
-    sites = _lattice(nmol + n_free, box)
+    sites = _mixed_sites(kid, nmol + n_free, box, rng)
     order = rng.permutation(nmol + n_free)
     rot = random_rotations(rng, nmol)
+    rings = np.nonzero(kid == 2)[0]
+    rot[rings] = _ring_rotations(rng, len(rings))
     if grouped:  # list order: molecules by kind, then free atoms; lattice sites stay random
         site_of = order.copy()
         order = np.arange(nmol + n_free)
