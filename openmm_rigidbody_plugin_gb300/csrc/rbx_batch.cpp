@@ -50,6 +50,7 @@ struct rbx_batch {
     // force field
     DevArray<FFSys> d_sys;
     DevArray<int> d_iatom, d_isys, d_cell_of, d_cell_count, d_cell_start, d_cell_cursor, d_cell_list;
+    DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_i0;
     DevArray<float4> d_param, d_cpos, d_cpar;
     DevArray<double> d_e_atom, d_energy;
     FFDev ff{};
@@ -266,10 +267,30 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
         f.krf = (float)krf;
         f.crf = (float)(1.0 / rc_s + krf * rc_s * rc_s);
     }
+    // force work lists: cells of multi-cell boxes; 64-atom chunks of single-cell boxes
+    std::vector<int> mc_cell, mc_sys, sc_sys, sc_i0;
+    for (int s = 0; s < num_systems; s++) {
+        const FFSys& f = sys[s];
+        if (f.nc > 1) {
+            for (int c = 0; c < f.nc * f.nc * f.nc; c++) {
+                mc_cell.push_back(f.c0 + c);
+                mc_sys.push_back(s);
+            }
+        } else {
+            for (int i = f.i0; i < f.i1; i += 64) {
+                sc_sys.push_back(s);
+                sc_i0.push_back(i);
+            }
+        }
+    }
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) { delete b; return set_error(RBX_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); }
     const int nint = (int)iatom.size();
     rc = upload_vec(b->d_sys, sys);
+    if (!rc) rc = upload_vec(b->d_mc_cell, mc_cell);
+    if (!rc) rc = upload_vec(b->d_mc_sys, mc_sys);
+    if (!rc) rc = upload_vec(b->d_sc_sys, sc_sys);
+    if (!rc) rc = upload_vec(b->d_sc_i0, sc_i0);
     if (!rc) rc = upload_vec(b->d_iatom, iatom);
     if (!rc) rc = upload_vec(b->d_isys, isys);
     if (!rc) rc = upload_vec(b->d_param, param);
@@ -302,6 +323,13 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     D.cpar = b->d_cpar.p;
     D.e_atom = b->d_e_atom.p;
     D.energy = b->d_energy.p;
+    D.fcap = 0.0f;
+    D.n_mc = (int)mc_cell.size();
+    D.n_sc = (int)sc_sys.size();
+    D.mc_cell = b->d_mc_cell.p;
+    D.mc_sys = b->d_mc_sys.p;
+    D.sc_sys = b->d_sc_sys.p;
+    D.sc_i0 = b->d_sc_i0.p;
     // the owned OpenMM-layout buffers (forces of non-interacting atoms stay zero)
     rbx_buffers rb;
     if ((rc = rbx_context_buffers(b->integ, &rb))) { delete b; return rc; }

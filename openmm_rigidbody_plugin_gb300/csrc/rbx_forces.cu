@@ -11,13 +11,14 @@
 //   2. ff_scan     one block per system: exclusive scan of its cells' counts (and count reset)
 //   3. ff_scatter  one thread per interacting atom: slot in its cell (single-cell systems keep
 //                  their atom order and need no atomics)
-//   4. ff_order    one thread per cell: sorts the cell by atom index (the cell contents, and so
-//                  every force sum, are in a fixed order) and writes cell-ordered copies of the
-//                  positions and parameters, so that neighbour loads are contiguous
-//   5. ff_force    one thread per interacting atom, in cell order: all pairs within the cutoff
-//                  over the 27 neighbour cells (or the whole box of a single-cell system), no
-//                  atomics; forces written as OpenMM fixed point (2^32) to the atom's slot
-//   6. ff_energy   (energy evaluations only) one block per system: fixed-order FP64 sum.
+//   4. ff_sort     one thread per cell of a multi-cell box: sorts the cell by atom index (the
+//                  cell contents, and so every force sum, are in a fixed order)
+//   5. ff_gather   one thread per atom: cell-ordered copies of positions (wrapped into the box)
+//                  and parameters, so that neighbour loads are contiguous
+//   6. ff_force_cells / ff_force_box  one block per cell (multi-cell boxes) or per 64 atoms of a
+//                  single-cell box: neighbour atoms staged in shared memory, all pairs within the
+//                  cutoff, no atomics; forces written as OpenMM fixed point (2^32) to the slot
+//   7. ff_energy   (energy evaluations only) one block per system: fixed-order FP64 sum.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -111,13 +112,14 @@ __global__ void ff_scatter(FFDev D) {
     D.cell_list[p] = k;
 }
 
-// Sort each cell by interacting-atom index and write its cell-ordered position/parameter copies.
-__global__ void ff_order(FFDev D, DevBuf B, int prec) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= D.n_cells) return;
+// Sort each cell of a multi-cell box by interacting-atom index (insertion sort: such a cell holds
+// tens of atoms), so that every cell, and so every force sum, is in a fixed order. The one cell
+// of a single-cell box is already in order.
+__global__ void ff_sort(FFDev D) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= D.n_mc) return;
+    const int c = D.mc_cell[w];
     const int b = D.cell_start[c], e = D.cell_start[c + 1];
-    // insertion sort: a cell of a multi-cell box holds tens of atoms; the one cell of a small box
-    // is already in order (linear pass)
     for (int i = b + 1; i < e; i++) {
         const int v = D.cell_list[i];
         int j = i - 1;
@@ -127,70 +129,57 @@ __global__ void ff_order(FFDev D, DevBuf B, int prec) {
         }
         D.cell_list[j + 1] = v;
     }
-    for (int i = b; i < e; i++) {
-        const int k = D.cell_list[i];
-        const int slot = D.iatom[k];
-        const float3 x = atom_position(B, prec, slot);
-        const float4 p = D.param[k];  // scaled charge, sigma/2, sqrt(eps), body id bits
-        D.cpos[i] = make_float4(x.x, x.y, x.z, p.x);
-        D.cpar[i] = make_float4(p.y, p.z, p.w, __int_as_float(slot));
+}
+
+// Cell-ordered copies: position wrapped into [0, L) and scaled charge; sigma/2, sqrt(epsilon), body
+// id and device slot.
+__global__ void ff_gather(FFDev D, DevBuf B, int prec) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.n_int) return;
+    const int k = D.cell_list[p];
+    const int slot = D.iatom[k];
+    const FFSys S = D.sys[D.isys[k]];
+    float3 x = atom_position(B, prec, slot);
+    x.x -= S.L * floorf(x.x * S.invL);
+    x.y -= S.L * floorf(x.y * S.invL);
+    x.z -= S.L * floorf(x.z * S.invL);
+    const float4 q = D.param[k];  // scaled charge, sigma/2, sqrt(eps), body id bits
+    D.cpos[p] = make_float4(x.x, x.y, x.z, q.x);
+    D.cpar[p] = make_float4(q.y, q.z, q.w, __int_as_float(slot));
+}
+
+constexpr int kFT = 64;  // threads of a force block; also the staged chunk of neighbour atoms
+
+// One pair term (r < rc): accumulates the force on i and (energy evaluations) the FP64 pair energy.
+template <bool ENERGY>
+__device__ __forceinline__ void pair_term(const FFSys& S, const FFDev& D, float4 xi, float4 pi, float4 xq, float4 pq,
+                                          float dx, float dy, float dz, float& fx, float& fy, float& fz, double& e) {
+    // the atom itself (same slot); ids are compared as integers: as floats they are denormals,
+    // which flush-to-zero arithmetic would make all equal
+    if (__float_as_int(pi.w) == __float_as_int(pq.w)) return;
+    const int body = __float_as_int(pi.z);
+    if (body > 0 && __float_as_int(pq.z) == body) return;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (r2 >= S.rc2) return;
+    if (D.fcap > 0.0f && r2 < 1e-8f) return;  // relaxation: coincident atoms have no direction
+    const float inv_r2 = 1.0f / r2, inv_r = rsqrtf(r2);
+    const float qq = xi.w * xq.w;
+    const float sig = pi.x + pq.x, eps = pi.y * pq.y;
+    const float s2 = sig * sig * inv_r2, s6 = s2 * s2 * s2;
+    const float g = qq * (inv_r * inv_r2 - 2.0f * S.krf) + 4.0f * eps * (12.0f * s6 * s6 - 6.0f * s6) * inv_r2;
+    fx = fmaf(g, dx, fx);
+    fy = fmaf(g, dy, fy);
+    fz = fmaf(g, dz, fz);
+    if (ENERGY) {  // the pair energy in FP64 from the FP32 displacement
+        const double r2d = (double)r2, inv_rd = 1.0 / sqrt(r2d), s2d = (double)sig * (double)sig / r2d;
+        const double s6d = s2d * s2d * s2d;
+        e += (double)qq * (inv_rd + (double)S.krf * r2d - (double)S.crf) + 4.0 * (double)eps * (s6d * s6d - s6d);
     }
 }
 
 template <bool ENERGY>
-__global__ void __launch_bounds__(128) ff_force(FFDev D, long long* __restrict__ force, int stride) {
-    const int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= D.n_int) return;
-    const FFSys S = D.sys[D.isys[p]];  // systems keep one contiguous range in both orders
-    const float4 xi = D.cpos[p];
-    const float4 pi = D.cpar[p];
-    const int body = __float_as_int(pi.z);
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    double e = 0.0;
-    auto pair = [&](int q) {
-        if (q == p) return;
-        const float4 xq = D.cpos[q];
-        const float4 pq = D.cpar[q];
-        if (body > 0 && __float_as_int(pq.z) == body) return;
-        float dx = xi.x - xq.x, dy = xi.y - xq.y, dz = xi.z - xq.z;
-        dx -= S.L * rintf(dx * S.invL);
-        dy -= S.L * rintf(dy * S.invL);
-        dz -= S.L * rintf(dz * S.invL);
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        if (r2 >= S.rc2) return;
-        if (D.fcap > 0.0f && r2 < 1e-8f) return;  // relaxation: coincident atoms have no direction
-        const float inv_r2 = 1.0f / r2, inv_r = rsqrtf(r2);
-        const float qq = xi.w * xq.w;
-        const float sig = pi.x + pq.x, eps = pi.y * pq.y;
-        const float s2 = sig * sig * inv_r2, s6 = s2 * s2 * s2;
-        const float g = qq * (inv_r * inv_r2 - 2.0f * S.krf) + 4.0f * eps * (12.0f * s6 * s6 - 6.0f * s6) * inv_r2;
-        fx = fmaf(g, dx, fx);
-        fy = fmaf(g, dy, fy);
-        fz = fmaf(g, dz, fz);
-        if (ENERGY) {  // the pair energy in FP64 from the FP32 displacement
-            const double r2d = (double)r2, inv_rd = 1.0 / sqrt(r2d), s2d = (double)sig * (double)sig / r2d;
-            const double s6d = s2d * s2d * s2d;
-            e += (double)qq * (inv_rd + (double)S.krf * r2d - (double)S.crf) + 4.0 * (double)eps * (s6d * s6d - s6d);
-        }
-    };
-    if (S.nc == 1) {
-        for (int q = S.i0; q < S.i1; q++) pair(q);
-    } else {
-        const int cell = D.cell_of[D.cell_list[p]] - S.c0;
-        const int cx = cell % S.nc, cy = (cell / S.nc) % S.nc, cz = cell / (S.nc * S.nc);
-        for (int oz = -1; oz <= 1; oz++) {
-            const int z = (cz + oz + S.nc) % S.nc;
-            for (int oy = -1; oy <= 1; oy++) {
-                const int y = (cy + oy + S.nc) % S.nc;
-                for (int ox = -1; ox <= 1; ox++) {
-                    const int x = (cx + ox + S.nc) % S.nc;
-                    const int c = S.c0 + (z * S.nc + y) * S.nc + x;
-                    const int qe = D.cell_start[c + 1];
-                    for (int q = D.cell_start[c]; q < qe; q++) pair(q);
-                }
-            }
-        }
-    }
+__device__ __forceinline__ void store_force(const FFDev& D, long long* __restrict__ force, int stride, int p, float4 pi,
+                                            float fx, float fy, float fz, double e) {
     if (D.fcap > 0.0f) {  // relaxation: cap the magnitude
         const float f2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
         if (f2 > D.fcap * D.fcap) {
@@ -210,6 +199,102 @@ __global__ void __launch_bounds__(128) ff_force(FFDev D, long long* __restrict__
     force[slot + stride] = __float2ll_rn(fy * 0x1p32f);
     force[slot + 2 * stride] = __float2ll_rn(fz * 0x1p32f);
     if (ENERGY) D.e_atom[p] = 0.5 * e;
+}
+
+// Multi-cell boxes: one block per cell. The block's threads take the cell's atoms (64 at a time);
+// each of the 27 neighbour cells is staged in shared memory, 64 atoms at a time, with its periodic
+// image shift applied once (exact for pairs within the cutoff: the cell edge is at least the
+// cutoff and there are at least three cells per edge).
+template <bool ENERGY>
+__global__ void __launch_bounds__(kFT) ff_force_cells(FFDev D, long long* __restrict__ force, int stride) {
+    __shared__ float4 sx[kFT], sp[kFT];
+    const int c = D.mc_cell[blockIdx.x];
+    const FFSys S = D.sys[D.mc_sys[blockIdx.x]];
+    const int b = D.cell_start[c], e = D.cell_start[c + 1];
+    const int local = c - S.c0, nc = S.nc;
+    const int cx = local % nc, cy = (local / nc) % nc, cz = local / (nc * nc);
+    const int t = threadIdx.x;
+    for (int i0 = b; i0 < e; i0 += kFT) {
+        const int p = i0 + t;
+        const bool mine = p < e;
+        const float4 xi = mine ? D.cpos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 pi = mine ? D.cpar[p] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        double en = 0.0;
+        for (int oz = -1; oz <= 1; oz++) {
+            int z = cz + oz;
+            const float shz = z < 0 ? -S.L : (z >= nc ? S.L : 0.f);
+            z = z < 0 ? z + nc : (z >= nc ? z - nc : z);
+            for (int oy = -1; oy <= 1; oy++) {
+                int y = cy + oy;
+                const float shy = y < 0 ? -S.L : (y >= nc ? S.L : 0.f);
+                y = y < 0 ? y + nc : (y >= nc ? y - nc : y);
+                for (int ox = -1; ox <= 1; ox++) {
+                    int x = cx + ox;
+                    const float shx = x < 0 ? -S.L : (x >= nc ? S.L : 0.f);
+                    x = x < 0 ? x + nc : (x >= nc ? x - nc : x);
+                    const int n = S.c0 + (z * nc + y) * nc + x;
+                    const int qb = D.cell_start[n], qe = D.cell_start[n + 1];
+                    for (int j0 = qb; j0 < qe; j0 += kFT) {
+                        __syncthreads();
+                        if (j0 + t < qe) {
+                            float4 a = D.cpos[j0 + t];
+                            a.x += shx;
+                            a.y += shy;
+                            a.z += shz;
+                            sx[t] = a;
+                            sp[t] = D.cpar[j0 + t];
+                        }
+                        __syncthreads();
+                        if (mine) {
+                            const int m = min(kFT, qe - j0);
+                            for (int j = 0; j < m; j++) {
+                                const float4 xq = sx[j];
+                                pair_term<ENERGY>(S, D, xi, pi, xq, sp[j], xi.x - xq.x, xi.y - xq.y, xi.z - xq.z,
+                                                  fx, fy, fz, en);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        if (mine) store_force<ENERGY>(D, force, stride, p, pi, fx, fy, fz, en);
+    }
+}
+
+// Single-cell boxes (fewer than three cutoffs across): one block per 64 atoms of the box, all
+// atoms of the box streamed through shared memory, minimum image per pair.
+template <bool ENERGY>
+__global__ void __launch_bounds__(kFT) ff_force_box(FFDev D, long long* __restrict__ force, int stride) {
+    __shared__ float4 sx[kFT], sp[kFT];
+    const FFSys S = D.sys[D.sc_sys[blockIdx.x]];
+    const int t = threadIdx.x;
+    const int p = D.sc_i0[blockIdx.x] + t;
+    const bool mine = p < S.i1;
+    const float4 xi = mine ? D.cpos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 pi = mine ? D.cpar[p] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    double en = 0.0;
+    for (int j0 = S.i0; j0 < S.i1; j0 += kFT) {
+        __syncthreads();
+        if (j0 + t < S.i1) {
+            sx[t] = D.cpos[j0 + t];
+            sp[t] = D.cpar[j0 + t];
+        }
+        __syncthreads();
+        if (mine) {
+            const int m = min(kFT, S.i1 - j0);
+            for (int j = 0; j < m; j++) {
+                const float4 xq = sx[j];
+                float dx = xi.x - xq.x, dy = xi.y - xq.y, dz = xi.z - xq.z;
+                dx -= S.L * rintf(dx * S.invL);
+                dy -= S.L * rintf(dy * S.invL);
+                dz -= S.L * rintf(dz * S.invL);
+                pair_term<ENERGY>(S, D, xi, pi, xq, sp[j], dx, dy, dz, fx, fy, fz, en);
+            }
+        }
+    }
+    if (mine) store_force<ENERGY>(D, force, stride, p, pi, fx, fy, fz, en);
 }
 
 __global__ void ff_energy(FFDev D) {
@@ -244,18 +329,33 @@ int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* 
     cudaStream_t st = (cudaStream_t)stream;
     if (D.n_int == 0) return 0;
     const int t = 256, g = (D.n_int + t - 1) / t;
+    int n = 0;
     ff_bin<<<g, t, 0, st>>>(D, B, prec);
     ff_scan<<<D.S, 256, 0, st>>>(D);
     ff_scatter<<<g, t, 0, st>>>(D);
-    ff_order<<<(D.n_cells + 127) / 128, 128, 0, st>>>(D, B, prec);
-    const int gf = (D.n_int + 127) / 128;
-    if (energy) {
-        ff_force<true><<<gf, 128, 0, st>>>(D, const_cast<long long*>(B.force), B.stride);
-        ff_energy<<<D.S, 256, 0, st>>>(D);
-    } else {
-        ff_force<false><<<gf, 128, 0, st>>>(D, const_cast<long long*>(B.force), B.stride);
+    n += 3;
+    if (D.n_mc) {
+        ff_sort<<<(D.n_mc + 127) / 128, 128, 0, st>>>(D);
+        n++;
     }
-    return cudaPeekAtLastError() == cudaSuccess ? (energy ? 6 : 5) : -1;
+    ff_gather<<<g, t, 0, st>>>(D, B, prec);
+    n++;
+    long long* f = const_cast<long long*>(B.force);
+    if (D.n_mc) {
+        if (energy) ff_force_cells<true><<<D.n_mc, kFT, 0, st>>>(D, f, B.stride);
+        else ff_force_cells<false><<<D.n_mc, kFT, 0, st>>>(D, f, B.stride);
+        n++;
+    }
+    if (D.n_sc) {
+        if (energy) ff_force_box<true><<<D.n_sc, kFT, 0, st>>>(D, f, B.stride);
+        else ff_force_box<false><<<D.n_sc, kFT, 0, st>>>(D, f, B.stride);
+        n++;
+    }
+    if (energy) {
+        ff_energy<<<D.S, 256, 0, st>>>(D);
+        n++;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? n : -1;
 }
 
 }  // namespace rbx

@@ -92,6 +92,13 @@ struct FFDev {
     double* e_atom;       // [n_int] half pair-energy sums (energy evaluations)
     double* energy;       // [S] potential energy per system (kJ/mol)
     float fcap;           // > 0: each atom's force is scaled down to at most this magnitude
+    // work lists of the force kernels (static): every cell of the multi-cell boxes with its
+    // system, and every 64-atom chunk (start in the interacting-atom list) of the single-cell boxes
+    int n_mc, n_sc;
+    const int* mc_cell;
+    const int* mc_sys;
+    const int* sc_sys;
+    const int* sc_i0;
 };
 int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* stream);
 // Fixed-point forces of slots [0, natoms) -> user-order doubles out[3*natoms] (kJ/mol/nm).
