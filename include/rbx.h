@@ -144,6 +144,14 @@ int rbx_context_set_state(rbx_integrator* h, void* stream, const double* positio
 int rbx_context_buffers(rbx_integrator* h, rbx_buffers* out);
 int rbx_context_set_forces(rbx_integrator* h, void* stream, const double* forces);
 int rbx_context_get_state(rbx_integrator* h, void* stream, double* positions, double* velocities);
+/* Exact restore of a saved state (no counterpart in the reference, which rebuilds its bodies from
+ * the Context's positions on every state change, RigidBodyIntegrator.cpp:63-74):
+ * rbx_context_load writes host positions and velocities into the owned buffers as they are, without
+ * rebuilding the body state; rbx_context_sync_bodies rewrites the body atoms' positions from the
+ * current body state with the step kernels' own arithmetic. With rbx_set_body_state in between,
+ * a state saved by rbx_get_body_state + rbx_context_get_state is restored bit for bit. */
+int rbx_context_load(rbx_integrator* h, void* stream, const double* positions, const double* velocities);
+int rbx_context_sync_bodies(rbx_integrator* h, void* stream);
 int rbx_step_host(rbx_integrator* h, void* stream, int nsteps, double dt, const double* forces, double* positions,
                   double* velocities);
 
@@ -202,6 +210,8 @@ int rbx_last_launch_count(const rbx_integrator* h);
  * (synchronous). rbx_batch_get_num_dof gives each system's degrees of freedom.
  */
 typedef struct rbx_batch rbx_batch;
+/* rbx_batch_set_state builds every body from the given positions and velocities (as
+ * rbx_upload_state does) and then places the body atoms where the body state puts them. */
 int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, const double* box_edges,
                      const double* cutoffs, const int* body_indices, const double* masses, const double* charges,
                      const double* sigmas, const double* epsilons, double eps_solvent, int rotation_mode,
@@ -209,6 +219,14 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
 int rbx_batch_destroy(rbx_batch* b);
 int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, const double* velocities);
 int rbx_batch_get_state(rbx_batch* b, void* stream, double* positions, double* velocities);
+/* Checkpoint and exact restore. rbx_batch_get_body_state gives every body's state (rows of 14, the
+ * layout of rbx_get_body_state; bodies system by system in ascending body index). After
+ * rbx_batch_set_state with the positions the saved batch was last set up from (they fix each
+ * body's principal frame and body-frame coordinates), rbx_batch_restore puts back a saved body
+ * state, positions and velocities bit for bit. */
+int rbx_batch_get_body_state(rbx_batch* b, double* body_state);
+int rbx_batch_restore(rbx_batch* b, void* stream, const double* body_state, const double* positions,
+                      const double* velocities);
 int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt);
 /* Relaxation by damped dynamics: nsteps times (forces capped at max_force kJ/mol/nm per atom,
  * every momentum scaled by `damping` in [0, 1), part1 of size dt), then every momentum zeroed.

@@ -51,6 +51,8 @@ SIGNATURES = [
     ("rbx_context_buffers", ctypes.c_int, [_vp, _bp]),
     ("rbx_context_set_forces", ctypes.c_int, [_vp, _vp, _dp]),
     ("rbx_context_get_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
+    ("rbx_context_load", ctypes.c_int, [_vp, _vp, _dp, _dp]),
+    ("rbx_context_sync_bodies", ctypes.c_int, [_vp, _vp]),
     ("rbx_step_host", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, _dp, _dp, _dp]),
     ("rbx_last_launch_count", ctypes.c_int, [_vp]),
     ("rbx_kinetic_energies_static", ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int, _dp, _dp, _vp, _ip, ctypes.c_int,
@@ -60,6 +62,8 @@ SIGNATURES = [
     ("rbx_batch_destroy", ctypes.c_int, [_vp]),
     ("rbx_batch_set_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_batch_get_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
+    ("rbx_batch_get_body_state", ctypes.c_int, [_vp, _dp]),
+    ("rbx_batch_restore", ctypes.c_int, [_vp, _vp, _dp, _dp, _dp]),
     ("rbx_batch_step", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double]),
     ("rbx_batch_relax", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("rbx_batch_energies", ctypes.c_int, [_vp, _vp, _dp]),

@@ -41,6 +41,11 @@ class BatchedSystems:
         cast = lambda a: np.ascontiguousarray(a, dtype=np.float64)
         self.boxes = cast(boxes)
         self.cutoffs = cast(cutoffs)
+        bidx = np.asarray(body_indices)
+        # bodies per system as the library counts them: ids shared by at least two atoms
+        self.bodies_per_system = np.array([
+            int(np.count_nonzero(np.bincount(np.maximum(bidx[a:b], 0))[1:] >= 2)) if b > a else 0
+            for a, b in zip(self.offsets[:-1], self.offsets[1:])])
         h = ctypes.c_void_p()
         _lib.check(self._lib.rbx_batch_create(
             ctypes.byref(h), self.num_systems, _i(self.offsets), _d(self.boxes), _d(self.cutoffs),
@@ -100,6 +105,23 @@ class BatchedSystems:
         v = np.zeros((self.num_atoms, 3))
         _lib.check(self._lib.rbx_batch_get_state(self._h, _stream(stream), _d(x), _d(v)))
         return x, v
+
+    def checkpoint(self, stream=None):
+        """Exact state of every system: a list of (body_state [nb_s, 14], positions, velocities)."""
+        bs = np.zeros((int(self.bodies_per_system.sum()), 14))
+        _lib.check(self._lib.rbx_batch_get_body_state(self._h, _d(bs)))
+        x, v = self.get_state(stream)
+        b_off = np.concatenate([[0], np.cumsum(self.bodies_per_system)])
+        return [(bs[b_off[k]:b_off[k + 1]].copy(), x[self.offsets[k]:self.offsets[k + 1]].copy(),
+                 v[self.offsets[k]:self.offsets[k + 1]].copy()) for k in range(self.num_systems)]
+
+    def restore(self, states, stream=None):
+        """Put back per-system states from ``checkpoint`` (bit for bit). The batch must hold the same
+        systems, set up from the positions the checkpointed batch was last set up from."""
+        bs = np.ascontiguousarray(np.concatenate([s[0] for s in states]) if states else np.zeros((0, 14)))
+        x = np.ascontiguousarray(np.concatenate([s[1] for s in states]))
+        v = np.ascontiguousarray(np.concatenate([s[2] for s in states]))
+        _lib.check(self._lib.rbx_batch_restore(self._h, _stream(stream), _d(bs), _d(x), _d(v)))
 
     def step(self, nsteps, dt, stream=None):
         _lib.check(self._lib.rbx_batch_step(self._h, _stream(stream), int(nsteps), float(dt)))

@@ -347,6 +347,9 @@ int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, con
     if (rc) return rc;
     b->drop_graph();  // the integrator re-plans its device arrays
     if ((rc = rbx_context_set_state(b->integ, stream, positions, velocities))) return rc;
+    // body atoms start where the body state puts them (the step kernels' arithmetic), so that a
+    // system's trajectory is a function of its body state alone, in or out of a batch
+    if ((rc = rbx_context_sync_bodies(b->integ, stream))) return rc;
     std::vector<int> body0, free0;
     system_ranges(b->integ, b->offsets, body0, free0, b->dof);
     if ((rc = upload_vec(b->d_body0, body0)) || (rc = upload_vec(b->d_free0, free0))) return rc;
@@ -358,6 +361,24 @@ int rbx_batch_get_state(rbx_batch* b, void* stream, double* positions, double* v
     int rc = check(b);
     if (rc) return rc;
     return rbx_context_get_state(b->integ, stream, positions, velocities);
+}
+
+int rbx_batch_get_body_state(rbx_batch* b, double* body_state) {
+    int rc = check(b);
+    if (rc) return rc;
+    return rbx_get_body_state(b->integ, body_state);
+}
+
+int rbx_batch_restore(rbx_batch* b, void* stream, const double* body_state, const double* positions,
+                      const double* velocities) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no geometry: call rbx_batch_set_state with the systems first");
+    if ((rc = rbx_context_load(b->integ, stream, positions, velocities))) return rc;
+    if ((rc = rbx_set_body_state(b->integ, body_state))) return rc;
+    if ((rc = rbx_context_sync_bodies(b->integ, stream))) return rc;
+    b->forces_valid = false;
+    return RBX_OK;
 }
 
 int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {

@@ -822,6 +822,35 @@ int rbx_context_set_state(rbx_integrator* h, void* stream, const double* positio
     return RBX_OK;
 }
 
+int rbx_context_load(rbx_integrator* h, void* stream, const double* positions, const double* velocities) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!positions || !velocities) return fail(RBX_ERR_INVALID_ARGUMENT, "null positions or velocities");
+    if ((rc = ensure_context(h))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(h->c_x.p, positions, sizeof(double) * 3 * h->natoms, cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(h->c_v.p, velocities, sizeof(double) * 3 * h->natoms, cudaMemcpyHostToDevice, st));
+    rbx_buffers b;
+    rbx_context_buffers(h, &b);
+    if (launch_load_positions(h->prec, h->c_x.p, h->c_v.p, h->c_m.p, h->c_loc.p, h->natoms, devbuf(&b), stream) < 0)
+        return fail(RBX_ERR_CUDA, "position upload kernel failed");
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RBX_OK;
+}
+
+int rbx_context_sync_bodies(rbx_integrator* h, void* stream) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body state");
+    if ((rc = ensure_context(h))) return rc;
+    rbx_buffers b;
+    rbx_context_buffers(h, &b);
+    if (launch_sync_positions(h->prec, h->sys(), devbuf(&b), stream) < 0)
+        return fail(RBX_ERR_CUDA, "position rebuild kernel failed");
+    h->last_launches = 1;
+    return RBX_OK;
+}
+
 int rbx_context_set_forces(rbx_integrator* h, void* stream, const double* forces) {
     int rc = check(h);
     if (rc) return rc;

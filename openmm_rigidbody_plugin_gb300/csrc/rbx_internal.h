@@ -132,6 +132,8 @@ DevSys device_system(const rbx_integrator* h);
 // (free0[S+1]), and their degrees of freedom (dof[S]).
 void system_ranges(const rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
                    std::vector<int>& free0, std::vector<int>& dof);
+// Body-atom positions rebuilt from the stored body state (the step kernels' arithmetic).
+int launch_sync_positions(int prec, const DevSys& s, const DevBuf& b, void* stream);
 // Scale the body COM velocities and quaternion momenta and the free atoms' velocities.
 int launch_scale_momenta(int prec, const DevSys& s, const DevBuf& b, double factor, void* stream);
 // [KE_t, KE_r] of each system (out[2*S]), FP64, fixed order, one block per system.

@@ -490,18 +490,21 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
             }
             const float eps = ((n2.hi - 1.0f) + n2.lo) + tail;
 #pragma unroll
-            for (int c = 6; c < 10; c++) x[c] = ff_acc(x[c], -0.5f * eps * x[c].hi);
+            for (int c = 6; c < 10; c++) x[c] = ff_norm(ff_acc(x[c], -0.5f * eps * x[c].hi));
 #pragma unroll
             for (int c = 0; c < 3; c++) {
                 x[c] = ff_norm(x[c]);
                 sR[6 * tid + 2 * c] = x[c].hi;
                 sR[6 * tid + 2 * c + 1] = x[c].lo;
             }
+            // positions are rebuilt from exactly the r and q stored below, so that they are a
+            // function of the stored state alone (sync_positions_kernel rebuilds them identically)
             rotation_matrix(q4<float>(x[6].hi, x[7].hi, x[8].hi, x[9].hi), sM + 9 * tid);
         }
 #pragma unroll
         for (int c = 0; c < 14; c++) {
-            const ff y = ff_norm(x[c]);
+            const bool normed = KIND != STEP_PART2 && (c < 3 || (c >= 6 && c < 10));
+            const ff y = normed ? x[c] : ff_norm(x[c]);
             ghi[b + c * nbp] = y.hi;
             glo[b + c * nbp] = y.lo;
         }
@@ -699,6 +702,49 @@ __global__ void scale_momenta_kernel(DevSys S, DevBuf B, double factor) {
     }
 }
 
+// Body-atom positions from the stored body state (r + At(q) d), with exactly the arithmetic of the
+// step kernels' position rebuild: after a restore of the body state they equal the positions the
+// last step wrote. One thread per body.
+template <int P>
+__global__ void sync_positions_kernel(DevSys S, DevBuf B) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= S.nb) return;
+    const int nbp = S.nb_pad;
+    const int a0 = S.atom0[b], a1 = S.atom0[b + 1];
+    if (P == PREC_DOUBLE) {
+        const double* st = (const double*)S.state;
+        const double* d = (const double*)S.d;
+        const V3<double> r = v3<double>(st[b], st[b + nbp], st[b + 2 * nbp]);
+        const Q4<double> q = q4<double>(st[b + 6 * nbp], st[b + 7 * nbp], st[b + 8 * nbp], st[b + 9 * nbp]);
+        for (int k = a0; k < a1; k++) {
+            const V3<double> delta = rotate_to_space(q, v3<double>(d[k], d[k + S.nba_pad], d[k + 2 * S.nba_pad]));
+            PosIO<P>::store(B, S.atom_loc[k], r, delta);
+        }
+    } else {
+        const float* hi = (const float*)S.state;
+        const float* lo = hi + 14 * nbp;
+        const float* d = (const float*)S.d;
+        float m[9];
+        rotation_matrix(q4<float>(hi[b + 6 * nbp], hi[b + 7 * nbp], hi[b + 8 * nbp], hi[b + 9 * nbp]), m);
+        const float rf[6] = {hi[b], lo[b], hi[b + nbp], lo[b + nbp], hi[b + 2 * nbp], lo[b + 2 * nbp]};
+        for (int k = a0; k < a1; k++) {
+            const V3<float> delta = mat_vec(m, v3<float>(d[k], d[k + S.nba_pad], d[k + 2 * S.nba_pad]));
+            float* pq = (float*)B.posq + 4 * (size_t)S.atom_loc[k];
+            if (P == PREC_MIXED) {
+                const ff px = ff_add(ff{rf[0], rf[1]}, delta.x);
+                const ff py = ff_add(ff{rf[2], rf[3]}, delta.y);
+                const ff pz = ff_add(ff{rf[4], rf[5]}, delta.z);
+                *(float2*)pq = make_float2(px.hi, py.hi);
+                pq[2] = pz.hi;
+                ((float4*)B.corr)[S.atom_loc[k]] = make_float4(px.lo, py.lo, pz.lo, 0.0f);
+            } else {
+                *(float2*)pq = make_float2(rf[0] + (rf[1] + delta.x), rf[2] + (rf[3] + delta.y));
+                pq[2] = rf[4] + (rf[5] + delta.z);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------------------------------
 // Layout conversion for the host-buffer API (user order doubles <-> OpenMM device layout).
 // ------------------------------------------------------------------------------------------
@@ -794,6 +840,18 @@ static int launch_step_p(int kind, const DevSys& s, const DevBuf& b, double dt, 
         case STEP_PART2: return launch_step_t<P, STEP_PART2, false>(s, b, dt, st);
         default: return exact ? launch_step_t<P, STEP_FUSED, true>(s, b, dt, st) : launch_step_t<P, STEP_FUSED, false>(s, b, dt, st);
     }
+}
+
+int launch_sync_positions(int prec, const DevSys& s, const DevBuf& b, void* stream) {
+    if (s.nb == 0) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int g = (s.nb + 127) / 128;
+    switch (prec) {
+        case PREC_SINGLE: sync_positions_kernel<PREC_SINGLE><<<g, 128, 0, st>>>(s, b); break;
+        case PREC_MIXED: sync_positions_kernel<PREC_MIXED><<<g, 128, 0, st>>>(s, b); break;
+        default: sync_positions_kernel<PREC_DOUBLE><<<g, 128, 0, st>>>(s, b); break;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }
 
 int launch_scale_momenta(int prec, const DevSys& s, const DevBuf& b, double factor, void* stream) {
