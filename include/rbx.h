@@ -151,6 +151,9 @@ int rbx_context_get_state(rbx_integrator* h, void* stream, double* positions, do
  * current body state with the step kernels' own arithmetic. With rbx_set_body_state in between,
  * a state saved by rbx_get_body_state + rbx_context_get_state is restored bit for bit. */
 int rbx_context_load(rbx_integrator* h, void* stream, const double* positions, const double* velocities);
+/* rbx_context_get_state for the user atoms [first_atom, first_atom + count) only. */
+int rbx_context_get_range(rbx_integrator* h, void* stream, int first_atom, int count, double* positions,
+                          double* velocities);
 int rbx_context_sync_bodies(rbx_integrator* h, void* stream);
 int rbx_step_host(rbx_integrator* h, void* stream, int nsteps, double dt, const double* forces, double* positions,
                   double* velocities);
@@ -219,6 +222,8 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
 int rbx_batch_destroy(rbx_batch* b);
 int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, const double* velocities);
 int rbx_batch_get_state(rbx_batch* b, void* stream, double* positions, double* velocities);
+/* Positions and velocities of system s only ([n_s*3] each). */
+int rbx_batch_get_system_state(rbx_batch* b, void* stream, int s, double* positions, double* velocities);
 /* Checkpoint and exact restore. rbx_batch_get_body_state gives every body's state (rows of 14, the
  * layout of rbx_get_body_state; bodies system by system in ascending body index). After
  * rbx_batch_set_state with the positions the saved batch was last set up from (they fix each

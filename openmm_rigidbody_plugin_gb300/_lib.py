@@ -52,6 +52,7 @@ SIGNATURES = [
     ("rbx_context_set_forces", ctypes.c_int, [_vp, _vp, _dp]),
     ("rbx_context_get_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_context_load", ctypes.c_int, [_vp, _vp, _dp, _dp]),
+    ("rbx_context_get_range", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     ("rbx_context_sync_bodies", ctypes.c_int, [_vp, _vp]),
     ("rbx_step_host", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, _dp, _dp, _dp]),
     ("rbx_last_launch_count", ctypes.c_int, [_vp]),
@@ -63,6 +64,7 @@ SIGNATURES = [
     ("rbx_batch_set_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_batch_get_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_batch_get_body_state", ctypes.c_int, [_vp, _dp]),
+    ("rbx_batch_get_system_state", ctypes.c_int, [_vp, _vp, ctypes.c_int, _dp, _dp]),
     ("rbx_batch_restore", ctypes.c_int, [_vp, _vp, _dp, _dp, _dp]),
     ("rbx_batch_step", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double]),
     ("rbx_batch_relax", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]),

@@ -106,6 +106,14 @@ class BatchedSystems:
         _lib.check(self._lib.rbx_batch_get_state(self._h, _stream(stream), _d(x), _d(v)))
         return x, v
 
+    def get_system_state(self, s, stream=None):
+        """Positions and velocities of system s only."""
+        n = int(self.offsets[s + 1] - self.offsets[s])
+        x = np.zeros((n, 3))
+        v = np.zeros((n, 3))
+        _lib.check(self._lib.rbx_batch_get_system_state(self._h, _stream(stream), int(s), _d(x), _d(v)))
+        return x, v
+
     def checkpoint(self, stream=None):
         """Exact state of every system: a list of (body_state [nb_s, 14], positions, velocities)."""
         bs = np.zeros((int(self.bodies_per_system.sum()), 14))

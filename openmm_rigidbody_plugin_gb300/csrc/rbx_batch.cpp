@@ -363,6 +363,14 @@ int rbx_batch_get_state(rbx_batch* b, void* stream, double* positions, double* v
     return rbx_context_get_state(b->integ, stream, positions, velocities);
 }
 
+int rbx_batch_get_system_state(rbx_batch* b, void* stream, int s, double* positions, double* velocities) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (s < 0 || s >= b->S) return set_error(RBX_ERR_INVALID_ARGUMENT, "system %d outside [0, %d)", s, b->S);
+    return rbx_context_get_range(b->integ, stream, b->offsets[s], b->offsets[s + 1] - b->offsets[s], positions,
+                                 velocities);
+}
+
 int rbx_batch_get_body_state(rbx_batch* b, double* body_state) {
     int rc = check(b);
     if (rc) return rc;

@@ -150,10 +150,22 @@ __global__ void ff_gather(FFDev D, DevBuf B, int prec) {
 
 constexpr int kFT = 64;  // threads of a force block; also the staged chunk of neighbour atoms
 
-// One pair term (r < rc): accumulates the force on i and (energy evaluations) the FP64 pair energy.
+// Compensated FP32 accumulator (Knuth's two-sum): the running sum keeps its rounding error in `lo`.
+struct ESum {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = hi + x, bp = s - hi;
+        lo += (hi - (s - bp)) + (x - bp);
+        hi = s;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// One pair term (r < rc): accumulates the force on i and (energy evaluations) the pair energy,
+// formed in FP32 and summed with compensation.
 template <bool ENERGY>
 __device__ __forceinline__ void pair_term(const FFSys& S, const FFDev& D, float4 xi, float4 pi, float4 xq, float4 pq,
-                                          float dx, float dy, float dz, float& fx, float& fy, float& fz, double& e) {
+                                          float dx, float dy, float dz, float& fx, float& fy, float& fz, ESum& e) {
     // the atom itself (same slot); ids are compared as integers: as floats they are denormals,
     // which flush-to-zero arithmetic would make all equal
     if (__float_as_int(pi.w) == __float_as_int(pq.w)) return;
@@ -170,16 +182,12 @@ __device__ __forceinline__ void pair_term(const FFSys& S, const FFDev& D, float4
     fx = fmaf(g, dx, fx);
     fy = fmaf(g, dy, fy);
     fz = fmaf(g, dz, fz);
-    if (ENERGY) {  // the pair energy in FP64 from the FP32 displacement
-        const double r2d = (double)r2, inv_rd = 1.0 / sqrt(r2d), s2d = (double)sig * (double)sig / r2d;
-        const double s6d = s2d * s2d * s2d;
-        e += (double)qq * (inv_rd + (double)S.krf * r2d - (double)S.crf) + 4.0 * (double)eps * (s6d * s6d - s6d);
-    }
+    if (ENERGY) e.add(qq * (inv_r + S.krf * r2 - S.crf) + 4.0f * eps * (s6 * s6 - s6));
 }
 
 template <bool ENERGY>
 __device__ __forceinline__ void store_force(const FFDev& D, long long* __restrict__ force, int stride, int p, float4 pi,
-                                            float fx, float fy, float fz, double e) {
+                                            float fx, float fy, float fz, const ESum& e) {
     if (D.fcap > 0.0f) {  // relaxation: cap the magnitude
         const float f2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
         if (f2 > D.fcap * D.fcap) {
@@ -198,7 +206,7 @@ __device__ __forceinline__ void store_force(const FFDev& D, long long* __restric
     force[slot] = __float2ll_rn(fx * 0x1p32f);
     force[slot + stride] = __float2ll_rn(fy * 0x1p32f);
     force[slot + 2 * stride] = __float2ll_rn(fz * 0x1p32f);
-    if (ENERGY) D.e_atom[p] = 0.5 * e;
+    if (ENERGY) D.e_atom[p] = 0.5 * e.value();
 }
 
 // Multi-cell boxes: one block per cell. The block's threads take the cell's atoms (64 at a time);
@@ -220,7 +228,7 @@ __global__ void __launch_bounds__(kFT) ff_force_cells(FFDev D, long long* __rest
         const float4 xi = mine ? D.cpos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 pi = mine ? D.cpar[p] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
         float fx = 0.f, fy = 0.f, fz = 0.f;
-        double en = 0.0;
+        ESum en;
         for (int oz = -1; oz <= 1; oz++) {
             int z = cz + oz;
             const float shz = z < 0 ? -S.L : (z >= nc ? S.L : 0.f);
@@ -274,7 +282,7 @@ __global__ void __launch_bounds__(kFT) ff_force_box(FFDev D, long long* __restri
     const float4 xi = mine ? D.cpos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 pi = mine ? D.cpar[p] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
     float fx = 0.f, fy = 0.f, fz = 0.f;
-    double en = 0.0;
+    ESum en;
     for (int j0 = S.i0; j0 < S.i1; j0 += kFT) {
         __syncthreads();
         if (j0 + t < S.i1) {

@@ -822,6 +822,28 @@ int rbx_context_set_state(rbx_integrator* h, void* stream, const double* positio
     return RBX_OK;
 }
 
+int rbx_context_get_range(rbx_integrator* h, void* stream, int first_atom, int count, double* positions,
+                          double* velocities) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (first_atom < 0 || count < 0 || first_atom + count > h->natoms)
+        return fail(RBX_ERR_INVALID_ARGUMENT, "atom range [%d, %d) outside [0, %d)", first_atom, first_atom + count, h->natoms);
+    if ((rc = ensure_context(h))) return rc;
+    if (count == 0) return RBX_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    rbx_buffers b;
+    rbx_context_buffers(h, &b);
+    double* x = h->c_x.p + 3 * (size_t)first_atom;
+    double* v = h->c_v.p + 3 * (size_t)first_atom;
+    if (launch_store_positions(h->prec, devbuf(&b), h->c_loc.p + first_atom, count, x, velocities ? v : nullptr,
+                               stream) < 0)
+        return fail(RBX_ERR_CUDA, "position download kernel failed");
+    if (positions) CUDA_TRY(cudaMemcpyAsync(positions, x, sizeof(double) * 3 * count, cudaMemcpyDeviceToHost, st));
+    if (velocities) CUDA_TRY(cudaMemcpyAsync(velocities, v, sizeof(double) * 3 * count, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RBX_OK;
+}
+
 int rbx_context_load(rbx_integrator* h, void* stream, const double* positions, const double* velocities) {
     int rc = check(h);
     if (rc) return rc;

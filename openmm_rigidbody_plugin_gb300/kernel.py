@@ -232,6 +232,17 @@ class IntegratorKernel:
         _lib.check(self._lib.rbx_step_host(self._h, _stream_handle(stream), int(nsteps), float(dt), _dptr(forces),
                                            _dptr(positions_out), _dptr(velocities_out)))
 
+    def context_set_forces(self, forces, stream=None):
+        f = np.ascontiguousarray(forces, dtype=np.float64)
+        _lib.check(self._lib.rbx_context_set_forces(self._h, _stream_handle(stream), _dptr(f)))
+
+    def context_step(self, kind, dt, stream=None):
+        """part1, part2 or fused on the owned buffers."""
+        fn = {"part1": self._lib.rbx_integrate_part1, "part2": self._lib.rbx_integrate_part2,
+              "fused": self._lib.rbx_integrate_fused}[kind]
+        b = self.context_buffers()
+        _lib.check(fn(self._h, _stream_handle(stream), ctypes.byref(b), float(dt)))
+
     def context_kinetic_energies(self, stream=None):
         out = np.zeros(2)
         b = self.context_buffers()

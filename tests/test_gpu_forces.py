@@ -6,7 +6,7 @@ Tolerances: forces are accumulated in FP32 from FP32 positions, so 99.9 % of the
 a force error of 2e-5 of the largest force. The rest may hold a pair whose distance lies within
 FP32 rounding of the cutoff, where FP32 and FP64 disagree on whether it counts: the reaction-field
 force does not vanish at the cutoff (K q_i q_j (1/rc^2 - 2 k_rf rc), 0.76 kJ/mol/nm for an O-H
-pair at 0.9 nm), so such an atom's force jumps by up to 2e-3 of the largest force. Energies are summed in FP64 from FP32 pair distances: the FP32 rounding of
+pair at 0.9 nm), so such an atom's force jumps by up to 2e-3 of the largest force. Pair energies are formed in FP32 and summed with compensation; the FP32 rounding of
 the positions (about 2e-7 nm) moves a box's energy by about sqrt(N) |F| 2e-7, a random walk over
 its atoms, so the bound is absolute, 1e-5 kJ/mol per atom plus 1e-6 relative (a missing pair or
 a wrong exclusion moves it by more than 1 kJ/mol; measured: 2.3e-3 kJ/mol on 512 waters, 2.3e-2
