@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--reference-seconds", type=float, default=90.0,
                    help="bound on the timed CPU work of --impl reference")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", default="single", choices=["single", "batched", "water"],
+    p.add_argument("--workload", default="single", choices=["single", "batched", "water", "served", "precision"],
                    help="single: the 1e6-body integrator step (default); batched: many independent systems, "
                         "full steps with the cell-list force field, against one system per launch; water: "
                         "512 rigid waters, full steps")
@@ -74,6 +74,13 @@ def parse():
     p.add_argument("--relax-steps", type=int, default=400, help="batched/water: relaxation before dynamics")
     p.add_argument("--graph-steps", type=int, default=50, help="batched/water: steps per captured CUDA graph")
     p.add_argument("--plain-systems", type=int, default=32, help="batched: systems run one per launch")
+    p.add_argument("--pbodies", type=int, default=8192, help="precision: near-degenerate bodies")
+    p.add_argument("--pwaters", type=int, default=20000, help="precision: waters")
+    p.add_argument("--psteps", type=int, default=1000, help="precision: steps per run")
+    p.add_argument("--rate", type=float, default=200.0, help="served: request arrivals per second")
+    p.add_argument("--duration", type=float, default=2.0, help="served: seconds of arrivals")
+    p.add_argument("--max-atoms", type=int, default=20000, help="served: largest request (atoms)")
+    p.add_argument("--max-steps", type=int, default=5000, help="served: longest request (steps)")
     p.add_argument("--plain-steps", type=int, default=0,
                    help="batched: steps of the one-per-launch arm (0: the same as --steps)")
     return p.parse_args()
@@ -560,6 +567,159 @@ def run_batched(args, world, rank, local):
     print(json.dumps(out), flush=True)
 
 
+def run_served(args, world, rank, local):
+    """Continuous batching of a seeded Poisson stream of simulation requests (serving.Server), with
+    p50/p99 completion latency and aggregate body-steps/s, against a one-request-at-a-time server on
+    a subset of the same stream."""
+    import torch
+    from openmm_rigidbody_plugin_gb300 import batch, build, serving
+    torch.cuda.set_device(local)
+    build.build_library()
+    stream = serving.poisson_stream(args.rate, args.duration, (100, args.max_atoms), (100, args.max_steps),
+                                    seed=8 + 1000 * rank)
+    nreq = len(stream)
+    # warm the library (module load, kernel attributes) outside the served clock
+    warm = batch.BatchedSystems.from_systems([stream[0].system])
+    warm.set_graph_steps(25)
+    warm.step(60, 0.002)
+    del warm
+    torch.cuda.synchronize()
+    server = serving.Server(budget_bytes=150e9, chunk_steps=100, graph_steps=25, device=local)
+    barrier(world)
+    with ClockSampler(local) as clocks:
+        clocks.mark_start()
+        t0 = time.perf_counter()
+        done = server.run(stream, realtime=True)
+        wall = time.perf_counter() - t0
+        clocks.mark_end()
+    wall = max_over_ranks(wall, world)
+    lat = np.array([r.latency for r in done])
+    body_steps = sum(int(r.system.num_bodies) * r.steps for r in done)
+    value = world * body_steps / wall
+    # one request at a time (the plain way), on the first requests of the stream: each request's
+    # service time alone, then the FIFO queue replayed on the same arrival times
+    sub = sorted(done, key=lambda r: r.rid)[:min(24, nreq)]
+    service = []
+    for r in sub:
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        serving.serve_alone(r)
+        torch.cuda.synchronize()
+        service.append(time.perf_counter() - t1)
+    fin, lat_plain = 0.0, []
+    for r, t_s in zip(sub, service):
+        fin = max(fin, r.arrival) + t_s
+        lat_plain.append(fin - r.arrival)
+    lat_plain = np.array(lat_plain)
+    plain_value = sum(int(r.system.num_bodies) * r.steps for r in sub) / sum(service)
+    lat_sub = np.array([r.latency for r in sub])
+    if rank != 0:
+        return
+    bytes_in = sum(r.system.num_atoms * 48 for r in done)    # positions + velocities in
+    bytes_out = sum(r.system.num_atoms * 48 + 24 for r in done)  # positions, velocities, energies out
+    total_steps = sum(r.steps for r in done)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": total_steps,
+           "warmup": 60, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 atoms + f64 body state", "data": "synthetic",
+           "config": {"workload": f"served: Poisson arrivals at {args.rate:g} req/s for {args.duration:g} s "
+                                  f"({nreq} requests), rigid-water systems of 100 to {args.max_atoms} atoms "
+                                  f"(log-uniform), 100 to {args.max_steps} steps (log-uniform), dt 2 fs, cutoff "
+                                  "LJ + reaction field, mixed precision; 150 GB budget; chunks of 100 steps, "
+                                  "25-step CUDA graphs (the 10-minute, 200,000-atom, 50,000-step stream scaled "
+                                  "down to finish in seconds)",
+                      "requests": nreq, "rebuilds": server.rebuilds, "wall_seconds": wall,
+                      "server_seconds": server.seconds,
+                      "parallelism": f"{world} independent replicas"},
+           "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                         "max": float(lat.max())},
+           "plain": {"value": plain_value, "unit": UNIT, "requests": len(sub),
+                     "latency_s": {"p50": float(np.percentile(lat_plain, 50)), "p99": float(np.percentile(lat_plain, 99))},
+                     "served_latency_same_requests_s": {"p50": float(np.percentile(lat_sub, 50)),
+                                                        "p99": float(np.percentile(lat_sub, 99))},
+                     "how": "each request alone (its own handle, same chunks), queued first come first served"},
+           "speedup_vs_plain": value / world / plain_value,
+           "roofline": None, "cpu_baseline": None,
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(bytes_in / max(total_steps, 1)),
+                   "d2h_bytes_per_step": int(bytes_out / max(total_steps, 1)),
+                   "call": "serving.Server.run (host structures in, host results out; wall clock)"},
+           "clocks": clocks.summary(), "gpu_launches": server.launches}
+    print(json.dumps(out), flush=True)
+
+
+def run_precision(args, world, rank, local):
+    """Precision study: near-degenerate bodies (two principal moments 1+eps apart, eps log-uniform in
+    [1e-8, 1e-2]) among waters, full steps with the cell-list force field; every precision and
+    rotation mode from the same relaxed state; energy drift and trajectory error after --psteps
+    steps against the double-precision run of the same mode and step size."""
+    import torch
+    from openmm_rigidbody_plugin_gb300 import batch, build
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    torch.cuda.set_device(local)
+    build.build_library()
+    s = W.near_degenerate_system(args.pbodies, args.pwaters, seed=7 + 1000 * rank)
+    b0 = batch.BatchedSystems.from_systems([s], relax_steps=args.relax_steps, device=local)
+    x0, v0 = b0.get_state()
+    dof = int(b0.num_dof[0])
+    del b0
+    rows, stream = [], torch.cuda.current_stream()
+    mixed_rate = None
+    with ClockSampler(local) as clocks:
+        clocks.mark_start()
+        for dt in (0.001, 0.004):
+            for mode in (0, 1, 4, 16):
+                runs = {}
+                for prec in ("double", "mixed", "single"):
+                    b = batch.BatchedSystems.from_systems([s], rotation_mode=mode, precision=prec, device=local)
+                    b.set_graph_steps(50)
+                    b.set_state(x0, v0)
+                    e0 = b.energies()[0]
+                    early = []
+                    t, done = 0.0, 0
+                    for n in (10, 100, args.psteps):  # trajectory samples after 10, 100 and all steps
+                        a, c = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        torch.cuda.synchronize()
+                        a.record(stream)
+                        b.step(n - done, dt)
+                        c.record(stream)
+                        torch.cuda.synchronize()
+                        t += a.elapsed_time(c) / 1e3
+                        done = n
+                        early.append(b.get_state())
+                    e1 = b.energies()[0]
+                    x, v = early[-1]
+                    runs[prec] = (x, v, e0, e1, t, early)
+                    if prec == "mixed" and mode == 0 and dt == 0.001:
+                        mixed_rate = s.num_bodies * args.psteps / t
+                xd, vd = runs["double"][0], runs["double"][1]
+                rel = lambda a, r: float(np.max(np.abs(a - r)) / np.max(np.abs(r)))
+                for prec, (x, v, e0, e1, t, early) in runs.items():
+                    de = float(e1.sum() - e0.sum())
+                    ed = runs["double"][5]
+                    rows.append({"dt_ps": dt, "mode": mode, "precision": prec, "ms_per_step": 1e3 * t / args.psteps,
+                                 "drift_kj_mol_ns_dof": de / (args.psteps * dt * 1e-3) / dof,
+                                 "rel_dE": abs(de) / abs(float(e0.sum())),
+                                 "traj_err_x_vs_double": rel(x, xd), "traj_err_v_vs_double": rel(v, vd),
+                                 "traj_err_x_10_100_steps": [rel(early[0][0], ed[0][0]), rel(early[1][0], ed[1][0])],
+                                 "traj_err_v_10_100_steps": [rel(early[0][1], ed[0][1]), rel(early[1][1], ed[1][1])]})
+        clocks.mark_end()
+    if rank != 0:
+        return
+    out = {"metric": METRIC, "value": mixed_rate, "unit": UNIT, "n_gpus": world, "steps": args.psteps, "warmup": 0,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 atoms + f64 body state",
+           "data": "synthetic",
+           "config": {"workload": f"precision study: {args.pbodies} near-degenerate rigid bodies (planar 4-atom "
+                                  "crosses, two principal moments 1+eps apart, eps log-uniform in [1e-8, 1e-2]) + "
+                                  f"{args.pwaters} waters at 1 g/cm3, cutoff LJ + reaction field; {args.psteps} "
+                                  "steps at dt 1 and 4 fs in single, mixed and double, rotation modes 0, 1, 4, 16; "
+                                  "value = mixed, mode 0, 1 fs (the stated 100,000-step runs shortened to "
+                                  f"{args.psteps})",
+                      "bodies": int(s.num_bodies), "atoms": int(s.num_atoms), "dof": dof,
+                      "forces": "FP32 cell-list kernel in every precision (the study varies the integrator)"},
+           "precision_study": rows, "roofline": None, "cpu_baseline": None,
+           "e2e": None, "clocks": clocks.summary(), "gpu_launches": None}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_init(args)
@@ -567,6 +727,10 @@ def main():
         run_reference(args, world, rank)
     elif args.workload in ("batched", "water"):
         run_batched(args, world, rank, local)
+    elif args.workload == "served":
+        run_served(args, world, rank, local)
+    elif args.workload == "precision":
+        run_precision(args, world, rank, local)
     else:
         run_gpu(args, world, rank, local)
     if world > 1:

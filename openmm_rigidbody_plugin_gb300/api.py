@@ -214,6 +214,7 @@ class RigidBodyIntegrator:
 
     def getRigidBodySystem(self):
         self._require()
+        self._context._ensure_state()
         return RigidBodySystem(self._kernel, self._bodyIndices)
 
     def _require(self):

@@ -112,22 +112,39 @@ __global__ void ff_scatter(FFDev D) {
     D.cell_list[p] = k;
 }
 
-// Sort each cell of a multi-cell box by interacting-atom index (insertion sort: such a cell holds
-// tens of atoms), so that every cell, and so every force sum, is in a fixed order. The one cell
-// of a single-cell box is already in order.
-__global__ void ff_sort(FFDev D) {
-    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+// Sort each cell of a multi-cell box by interacting-atom index, so that every cell, and so every
+// force sum, is in a fixed order. One warp per cell: the cell is staged in shared memory and each
+// lane ranks its entries against all of them (the entries are distinct, so the ranks are a
+// permutation); a cell larger than the stage falls back to an insertion sort by one lane. The one
+// cell of a single-cell box is already in order.
+constexpr int kSortWarps = 4, kSortStage = 512;
+__global__ void __launch_bounds__(32 * kSortWarps) ff_sort(FFDev D) {
+    __shared__ int stage[kSortWarps][kSortStage];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = blockIdx.x * kSortWarps + warp;
     if (w >= D.n_mc) return;
     const int c = D.mc_cell[w];
-    const int b = D.cell_start[c], e = D.cell_start[c + 1];
-    for (int i = b + 1; i < e; i++) {
-        const int v = D.cell_list[i];
-        int j = i - 1;
-        while (j >= b && D.cell_list[j] > v) {
-            D.cell_list[j + 1] = D.cell_list[j];
-            j--;
+    const int b = D.cell_start[c], e = D.cell_start[c + 1], n = e - b;
+    int* s = stage[warp];
+    if (n <= kSortStage) {
+        for (int i = lane; i < n; i += 32) s[i] = D.cell_list[b + i];
+        __syncwarp();
+        for (int i = lane; i < n; i += 32) {
+            const int v = s[i];
+            int rank = 0;
+            for (int j = 0; j < n; j++) rank += s[j] < v;
+            D.cell_list[b + rank] = v;
         }
-        D.cell_list[j + 1] = v;
+    } else if (lane == 0) {
+        for (int i = b + 1; i < e; i++) {
+            const int v = D.cell_list[i];
+            int j = i - 1;
+            while (j >= b && D.cell_list[j] > v) {
+                D.cell_list[j + 1] = D.cell_list[j];
+                j--;
+            }
+            D.cell_list[j + 1] = v;
+        }
     }
 }
 
@@ -343,7 +360,7 @@ int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* 
     ff_scatter<<<g, t, 0, st>>>(D);
     n += 3;
     if (D.n_mc) {
-        ff_sort<<<(D.n_mc + 127) / 128, 128, 0, st>>>(D);
+        ff_sort<<<(D.n_mc + kSortWarps - 1) / kSortWarps, 32 * kSortWarps, 0, st>>>(D);
         n++;
     }
     ff_gather<<<g, t, 0, st>>>(D, B, prec);

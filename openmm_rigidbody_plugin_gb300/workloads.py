@@ -306,6 +306,42 @@ def gaussian_forces(n_atoms, seed=5, sd=500.0):
     return rng.standard_normal((n_atoms, 3)) * sd
 
 
+def near_degenerate_system(n_bodies=8192, n_waters=20000, eps_range=(1e-8, 1e-2), seed=7, temperature=300.0,
+                           arm=0.1):
+    """Rigid bodies with nearly degenerate inertia among waters (the precision-study case): each
+    body is a planar cross of four carbon-like atoms (mass 12, LJ on all four) with arms a and
+    a*sqrt(1+eps), so that two of its principal moments differ by the factor 1+eps, eps
+    log-uniform in eps_range; random orientations; all molecules on one lattice at 1 g/cm^3."""
+    rng = np.random.default_rng(seed)
+    eps = np.exp(rng.uniform(np.log(eps_range[0]), np.log(eps_range[1]), size=n_bodies))
+    nmol = n_bodies + n_waters
+    m_body = np.full(4, 12.0)
+    total = n_bodies * m_body.sum() + n_waters * sum(WATER_MASSES)
+    box = _box_for_mass(total)
+    sites = _lattice(nmol, box)[rng.permutation(nmol)]
+    rot = random_rotations(rng, nmol)
+    wt = water_template()
+    wm = np.asarray(WATER_MASSES)
+    wt = wt - (wm[:, None] * wt).sum(0) / wm.sum()
+    pos, mass, bidx, spec = [], [], [], []
+    for k in range(nmol):
+        if k < n_bodies:
+            b = arm * np.sqrt(1.0 + eps[k])
+            t = np.array([[arm, 0, 0], [-arm, 0, 0], [0, b, 0], [0, -b, 0]])
+            m, sp = m_body, (TETRA_C,) * 4
+        else:
+            t, m, sp = wt, wm, SPECIES["water"]
+        pos.append(sites[k] + t @ rot[k].T)
+        mass.append(m)
+        bidx.append(np.full(len(m), k + 1, dtype=np.int32))
+        spec.append(np.array(sp, dtype=np.int8))
+    masses = np.concatenate(mass)
+    s = System(masses, np.concatenate(bidx), np.vstack(pos), _mb_velocities(rng, masses, temperature), box,
+               {"cross": n_bodies, "water": n_waters}, np.concatenate(spec))
+    s.eps = eps
+    return s
+
+
 def nonbonded(system):
     """Per-atom (charge, sigma, epsilon) arrays of a system from its species."""
     table = np.array([NONBONDED[k] for k in range(len(NONBONDED))])
