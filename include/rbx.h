@@ -186,6 +186,18 @@ int rbx_kinetic_energies_static(const double* body_state, int num_bodies, int bo
                                 const double* inv_inertia, const void* velm, const int* free_slots, int num_free,
                                 int precision, void* stream, double* out_device);
 
+/*
+ * Pipelined rbx_step_host: the same work (forces in, nsteps steps, positions and velocities out),
+ * asynchronous. Consecutive calls overlap one call's force upload and another's result download
+ * with a third's kernels (double-buffered device staging, internal copy streams ordered by
+ * events); the kernels run on `stream`. The host arrays must stay untouched until the results
+ * are waited for, and should be pinned (pageable memory makes the copies synchronous).
+ * rbx_step_host_wait blocks until every result of earlier calls is in its host arrays.
+ */
+int rbx_step_host_async(rbx_integrator* h, void* stream, int nsteps, double dt, const double* forces,
+                        double* positions, double* velocities);
+int rbx_step_host_wait(rbx_integrator* h);
+
 /* Number of kernel launches the last integrate/kinetic/step call enqueued (for accounting). */
 int rbx_last_launch_count(const rbx_integrator* h);
 

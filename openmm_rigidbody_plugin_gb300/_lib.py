@@ -55,6 +55,8 @@ SIGNATURES = [
     ("rbx_context_get_range", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_int, _dp, _dp]),
     ("rbx_context_sync_bodies", ctypes.c_int, [_vp, _vp]),
     ("rbx_step_host", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, _dp, _dp, _dp]),
+    ("rbx_step_host_async", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, _dp, _dp, _dp]),
+    ("rbx_step_host_wait", ctypes.c_int, [_vp]),
     ("rbx_last_launch_count", ctypes.c_int, [_vp]),
     ("rbx_kinetic_energies_static", ctypes.c_int, [_dp, ctypes.c_int, ctypes.c_int, _dp, _dp, _vp, _ip, ctypes.c_int,
                                                    ctypes.c_int, _vp, _dp]),

@@ -95,6 +95,12 @@ struct rbx_integrator {
     DevArray<unsigned char> c_posq, c_corr, c_velm;
     DevArray<long long> c_force;
     DevArray<double> c_x, c_v, c_f, c_m;
+    // pipelined host-buffer steps: double-buffered staging, copy streams and their events
+    DevArray<double> p_f[2], p_x[2], p_v[2];
+    cudaStream_t p_in = nullptr, p_out = nullptr;
+    cudaEvent_t p_in_done[2] = {nullptr, nullptr}, p_compute_done[2] = {nullptr, nullptr};
+    cudaEvent_t p_out_done[2] = {nullptr, nullptr};
+    long p_calls = 0;
     DevArray<int> c_loc;
 
     DevSys sys() const {
@@ -108,6 +114,13 @@ struct rbx_integrator {
     }
     ~rbx_integrator() {
         if (h_ke) cudaFreeHost(h_ke);
+        for (int s = 0; s < 2; s++) {
+            if (p_in_done[s]) cudaEventDestroy(p_in_done[s]);
+            if (p_compute_done[s]) cudaEventDestroy(p_compute_done[s]);
+            if (p_out_done[s]) cudaEventDestroy(p_out_done[s]);
+        }
+        if (p_in) cudaStreamDestroy(p_in);
+        if (p_out) cudaStreamDestroy(p_out);
     }
 };
 
@@ -919,6 +932,77 @@ int rbx_step_host(rbx_integrator* h, void* stream, int nsteps, double dt, const 
     launches += 2;  // part2 + force conversion
     if ((rc = rbx_context_get_state(h, stream, positions, velocities))) return rc;
     h->last_launches = launches + 1;
+    return RBX_OK;
+}
+
+// Pipelined host-buffer steps. Call i uses staging slot i % 2: its forces go up on the input
+// stream once call i-2 has finished reading that slot, its kernels run on `stream` once the
+// upload has landed (and once call i-2's results have left the output slot), and its positions
+// and velocities go down on the output stream once the kernels are done. Consecutive calls so
+// overlap one call's upload and another's download with a third's kernels.
+int rbx_step_host_async(rbx_integrator* h, void* stream, int nsteps, double dt, const double* forces,
+                        double* positions, double* velocities) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (nsteps < 1) return fail(RBX_ERR_INVALID_ARGUMENT, "nsteps must be >= 1");
+    if (!forces || !positions || !velocities) return fail(RBX_ERR_INVALID_ARGUMENT, "null host array");
+    if ((rc = ensure_context(h))) return rc;
+    CUDA_TRY(cudaSetDevice(h->device));
+    const size_t n3 = (size_t)3 * h->natoms;
+    if (!h->p_in) {
+        for (int s = 0; s < 2; s++) {
+            if (h->p_f[s].alloc(n3) != cudaSuccess || h->p_x[s].alloc(n3) != cudaSuccess || h->p_v[s].alloc(n3) != cudaSuccess)
+                return fail(RBX_ERR_CUDA, "cudaMalloc of pipeline staging failed");
+            CUDA_TRY(cudaEventCreateWithFlags(&h->p_in_done[s], cudaEventDisableTiming));
+            CUDA_TRY(cudaEventCreateWithFlags(&h->p_compute_done[s], cudaEventDisableTiming));
+            CUDA_TRY(cudaEventCreateWithFlags(&h->p_out_done[s], cudaEventDisableTiming));
+            CUDA_TRY(cudaEventRecord(h->p_compute_done[s], (cudaStream_t)stream));
+            CUDA_TRY(cudaEventRecord(h->p_out_done[s], (cudaStream_t)stream));
+        }
+        CUDA_TRY(cudaStreamCreateWithFlags(&h->p_in, cudaStreamNonBlocking));
+        CUDA_TRY(cudaStreamCreateWithFlags(&h->p_out, cudaStreamNonBlocking));
+    }
+    const int s = (int)(h->p_calls & 1);
+    cudaStream_t st = (cudaStream_t)stream;
+    // upload
+    CUDA_TRY(cudaStreamWaitEvent(h->p_in, h->p_compute_done[s], 0));
+    CUDA_TRY(cudaMemcpyAsync(h->p_f[s].p, forces, sizeof(double) * n3, cudaMemcpyHostToDevice, h->p_in));
+    CUDA_TRY(cudaEventRecord(h->p_in_done[s], h->p_in));
+    // kernels
+    CUDA_TRY(cudaStreamWaitEvent(st, h->p_in_done[s], 0));
+    if (launch_forces_from_host(h->prec, h->p_f[s].p, h->c_loc.p, h->natoms, h->c_force.p, h->stride, stream) < 0)
+        return fail(RBX_ERR_CUDA, "force conversion kernel failed");
+    rbx_buffers b;
+    rbx_context_buffers(h, &b);
+    int launches = 1;
+    if ((rc = rbx_integrate_part1(h, stream, &b, dt))) return rc;
+    for (int n = 1; n < nsteps; n++) {
+        if ((rc = rbx_integrate_fused(h, stream, &b, dt))) return rc;
+        launches++;
+    }
+    if ((rc = rbx_integrate_part2(h, stream, &b, dt))) return rc;
+    launches += 2;
+    CUDA_TRY(cudaStreamWaitEvent(st, h->p_out_done[s], 0));
+    if (launch_store_positions(h->prec, devbuf(&b), h->c_loc.p, h->natoms, h->p_x[s].p, h->p_v[s].p, stream) < 0)
+        return fail(RBX_ERR_CUDA, "position download kernel failed");
+    CUDA_TRY(cudaEventRecord(h->p_compute_done[s], st));
+    // download
+    CUDA_TRY(cudaStreamWaitEvent(h->p_out, h->p_compute_done[s], 0));
+    CUDA_TRY(cudaMemcpyAsync(positions, h->p_x[s].p, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->p_out));
+    CUDA_TRY(cudaMemcpyAsync(velocities, h->p_v[s].p, sizeof(double) * n3, cudaMemcpyDeviceToHost, h->p_out));
+    CUDA_TRY(cudaEventRecord(h->p_out_done[s], h->p_out));
+    h->p_calls++;
+    h->last_launches = launches + 1;
+    return RBX_OK;
+}
+
+int rbx_step_host_wait(rbx_integrator* h) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->p_out) return RBX_OK;
+    CUDA_TRY(cudaSetDevice(h->device));
+    CUDA_TRY(cudaStreamSynchronize(h->p_out));
+    for (int s = 0; s < 2; s++) CUDA_TRY(cudaEventSynchronize(h->p_out_done[s]));
     return RBX_OK;
 }
 

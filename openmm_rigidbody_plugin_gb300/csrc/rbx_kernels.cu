@@ -336,8 +336,7 @@ struct FSmem {
     static constexpr int TA = kTileAtomsF, TB = kTileBodiesF;
     static constexpr int SF = 0;              // 3 x TA: F
     static constexpr int ST = SF + 3 * TA;    // 3 x TA: torque
-    static constexpr int SX = ST + 3 * TA;    // 3 x TA: d (part1, fused) or delta (part2)
-    static constexpr int SM = SX + 3 * TA;    // 9 x TB: rotation matrix At(q), row-major per body
+    static constexpr int SM = ST + 3 * TA;    // 9 x TB: rotation matrix At(q), row-major per body
     static constexpr int SR = SM + 9 * TB;    // 6 x TB: COM (hi, lo) or COM velocity (double)
     static constexpr int SW = SR + 6 * TB;    // 3 x TB: space-frame omega (part2)
     static constexpr int SB = SW + 3 * TB;    // TA ushort: atom -> tile body
@@ -368,7 +367,6 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
     extern __shared__ __align__(16) float fsm[];
     float* sF = fsm + FSmem::SF;
     float* sT = fsm + FSmem::ST;
-    float* sX = fsm + FSmem::SX;
     float* sM = fsm + FSmem::SM;
     float* sR = fsm + FSmem::SR;
     float* sW = fsm + FSmem::SW;
@@ -418,8 +416,6 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
                 const V3<float> tau = cross(delta, F[i]);
                 sF[3 * a] = F[i].x; sF[3 * a + 1] = F[i].y; sF[3 * a + 2] = F[i].z;
                 sT[3 * a] = tau.x; sT[3 * a + 1] = tau.y; sT[3 * a + 2] = tau.z;
-                const V3<float> x = KIND == STEP_PART2 ? delta : d[i];
-                sX[3 * a] = x.x; sX[3 * a + 1] = x.y; sX[3 * a + 2] = x.z;
             }
         }
     }
@@ -511,14 +507,17 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
     }
     __syncthreads();
 
-    // Phase 3: positions (part1, fused) or velocities (part2)
+    // Phase 3: positions (part1, fused) or velocities (part2); d is read again (an L2 hit after
+    // phase 1) and, for part2, delta rebuilt from the unchanged orientation
+    const float* __restrict__ dg3 = (const float*)S.d;
     for (int a = tid; a < nat; a += kThreadsF) {
         const int t = sBody[a];
         const int loc = __ldg(S.atom_loc + a0 + a);
-        const V3<float> x = v3<float>(sX[3 * a], sX[3 * a + 1], sX[3 * a + 2]);
+        const int k = a0 + a;
+        const V3<float> x = v3<float>(__ldg(dg3 + k), __ldg(dg3 + k + S.nba_pad), __ldg(dg3 + k + 2 * S.nba_pad));
         if (KIND == STEP_PART2) {
             using V4 = typename Tr<P>::V4;
-            const V3<float> rel = cross(v3<float>(sW[3 * t], sW[3 * t + 1], sW[3 * t + 2]), x);
+            const V3<float> rel = cross(v3<float>(sW[3 * t], sW[3 * t + 1], sW[3 * t + 2]), mat_vec(sM + 9 * t, x));
             const double* v = (const double*)(sR + 6 * t);
             V4* vel = (V4*)B.velm;
             V4 vm = vel[loc];

@@ -243,6 +243,15 @@ class IntegratorKernel:
         b = self.context_buffers()
         _lib.check(fn(self._h, _stream_handle(stream), ctypes.byref(b), float(dt)))
 
+    def step_host_async(self, nsteps, dt, forces, positions_out, velocities_out, stream=None):
+        """Pipelined step_host: returns at once; the host arrays (C-contiguous float64, pinned for
+        overlap) must stay alive and untouched until step_host_wait()."""
+        _lib.check(self._lib.rbx_step_host_async(self._h, _stream_handle(stream), int(nsteps), float(dt),
+                                                 _dptr(forces), _dptr(positions_out), _dptr(velocities_out)))
+
+    def step_host_wait(self):
+        _lib.check(self._lib.rbx_step_host_wait(self._h))
+
     def context_kinetic_energies(self, stream=None):
         out = np.zeros(2)
         b = self.context_buffers()

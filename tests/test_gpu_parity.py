@@ -250,3 +250,28 @@ def test_determinism(rbx, golden):
         outs.append((buf.get_positions(), buf.get_velocities(), k.kinetic_energies(buf)))
     for a, b in zip(outs[0], outs[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "double"])
+def test_pipelined_host_steps_equal_synchronous_ones(rbx, golden, prec):
+    """rbx_step_host_async (copies overlapped across calls) gives the synchronous results."""
+    import torch
+    g = golden("water64_sd50_mode0")
+    rng = np.random.default_rng(3)
+    forces = [np.ascontiguousarray(g["F"] * (1.0 + 0.1 * k)) for k in range(5)]
+    out = {}
+    for mode in ("sync", "async"):
+        k = rbx.IntegratorKernel(g["masses"], g["body_indices"], rotation_mode=0, precision=prec)
+        k.context_set_state(g["R0"], g["V0"])
+        pinned = [(torch.zeros((len(g["masses"]), 3), dtype=torch.float64).pin_memory().numpy(),
+                   torch.zeros((len(g["masses"]), 3), dtype=torch.float64).pin_memory().numpy()) for _ in forces]
+        for f, (x, v) in zip(forces, pinned):
+            if mode == "sync":
+                k.step_host(2, 0.002, f, x, v)
+            else:
+                k.step_host_async(2, 0.002, f, x, v)
+        if mode == "async":
+            k.step_host_wait()
+        out[mode] = [(x.copy(), v.copy()) for x, v in pinned]
+    for (xs, vs), (xa, va) in zip(out["sync"], out["async"]):
+        assert np.array_equal(xs, xa) and np.array_equal(vs, va)
