@@ -88,6 +88,15 @@ int rbx_set_atom_locations(rbx_integrator* h, const int* location);
  */
 int rbx_upload_state(rbx_integrator* h, const double* positions, const double* velocities);
 
+/*
+ * Body setup on the device, from the positions, velocities (and the masses given to rbx_create) of
+ * the atoms already in `buf` at their device slots: the same robust setup as rbx_upload_state, the
+ * same arithmetic (bit-identical results), without copying positions and velocities to the host.
+ * Replaces RigidBodySystem::update + uploadBodySystem on a state change
+ * (RigidBodyIntegrator.cpp:63-74, CudaRigidBodyKernels.cpp:293-372). Synchronises `stream`.
+ */
+int rbx_upload_state_device(rbx_integrator* h, void* stream, const rbx_buffers* buf);
+
 /* Counts: RigidBodySystem::getNumDOF/getNumBodies/getNumFree (RigidBodySystem.h:38-42). */
 int rbx_get_num_dof(const rbx_integrator* h, int* out);
 int rbx_get_num_bodies(const rbx_integrator* h, int* out);

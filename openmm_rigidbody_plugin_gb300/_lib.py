@@ -35,6 +35,7 @@ SIGNATURES = [
     ("rbx_destroy", ctypes.c_int, [_vp]),
     ("rbx_set_atom_locations", ctypes.c_int, [_vp, _ip]),
     ("rbx_upload_state", ctypes.c_int, [_vp, _dp, _dp]),
+    ("rbx_upload_state_device", ctypes.c_int, [_vp, _vp, _bp]),
     ("rbx_get_num_dof", ctypes.c_int, [_vp, _ip]),
     ("rbx_get_num_bodies", ctypes.c_int, [_vp, _ip]),
     ("rbx_get_num_free", ctypes.c_int, [_vp, _ip]),

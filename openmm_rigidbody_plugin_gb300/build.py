@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librbx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["rbx_kernels.cu", "rbx_forces.cu", "rbx_host.cpp", "rbx_batch.cpp"]
+SOURCES = ["rbx_kernels.cu", "rbx_forces.cu", "rbx_setup.cu", "rbx_host.cpp", "rbx_batch.cpp"]
 
 
 def nvcc():
@@ -34,6 +34,9 @@ def _compile(src, verbose):
         # (rotation increments and series; the float-float sums use explicit round-to-nearest
         # adds); FP64 code is unaffected by these flags.
         cmd += ARCH + ["-lineinfo", "--expt-relaxed-constexpr", "-prec-div=false", "-prec-sqrt=false", "-ftz=true"]
+        if src == "rbx_setup.cu":
+            # the device body setup repeats the host's FP64 arithmetic exactly: no contraction
+            cmd += ["-fmad=false"]
         if verbose:
             cmd += ["-Xptxas", "-v"]
     else:

@@ -20,6 +20,7 @@
 #include "rbx_devarray.h"
 #include "rbx_internal.h"
 #include "rbx_math.cuh"
+#include "rbx_setup.cuh"
 
 using namespace rbx;
 
@@ -84,6 +85,9 @@ struct rbx_integrator {
     DevArray<double> d_state, d_invm, d_invI;  // d_state holds FP64 rows or float-float rows
     DevArray<float> d_bconst;                   // single/mixed: 11 rows (see kBconstRows)
     DevArray<int> d_atom0, d_atom_loc, d_free_loc, d_tiles;
+    DevArray<double> d_bmass, d_I;  // body-atom masses (library order); moments of the device setup
+    DevArray<int> d_dof, d_setup_counts;
+    bool host_geom_valid = true;    // host copies of the geometry match the device (false after a device setup)
     DevArray<uint8_t> d_cls;
     DevArray<unsigned char> d_fixed;  // float or double SoA
     DevArray<double> d_ke_partial, d_ke_out;
@@ -126,6 +130,48 @@ struct rbx_integrator {
 
 rbx::DevSys rbx::device_system(const rbx_integrator* h) { return h->sys(); }
 
+int rbx::ensure_host_geometry(rbx_integrator* h) {
+    if (h->host_geom_valid || !h->have_state) return RBX_OK;
+    const int nb = h->nb, nbp = h->nb_pad, nbap = h->nba_pad;
+    std::vector<double> I((size_t)3 * nbp);
+    std::vector<int> dof(std::max(nb, 1));
+    std::vector<uint8_t> cls(std::max(nb, 1));
+    CUDA_TRY(cudaMemcpy(I.data(), h->d_I.p, I.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(dof.data(), h->d_dof.p, dof.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(cls.data(), h->d_cls.p, cls.size(), cudaMemcpyDeviceToHost));
+    std::vector<double> invm(std::max(nb, 1)), invI((size_t)3 * nbp), d((size_t)3 * nbap);
+    if (h->prec == PREC_DOUBLE) {
+        CUDA_TRY(cudaMemcpy(invm.data(), h->d_invm.p, invm.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(invI.data(), h->d_invI.p, invI.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(d.data(), h->d_fixed.p, d.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+        std::vector<float> bc((size_t)kBconstRows * nbp), df((size_t)3 * nbap);
+        CUDA_TRY(cudaMemcpy(bc.data(), h->d_bconst.p, bc.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        CUDA_TRY(cudaMemcpy(df.data(), h->d_fixed.p, df.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        for (int L = 0; L < nb; L++) {
+            invm[L] = (double)bc[L] + (double)bc[L + (size_t)7 * nbp];
+            for (int k = 0; k < 3; k++)
+                invI[L + (size_t)k * nbp] = (double)bc[L + (size_t)(1 + k) * nbp] + (double)bc[L + (size_t)(8 + k) * nbp];
+        }
+        for (size_t i = 0; i < df.size(); i++) d[i] = df[i];
+    }
+    for (int L = 0; L < nb; L++) {
+        const int b = h->lib_body[L];
+        for (int k = 0; k < 3; k++) {
+            h->I[3 * b + k] = I[L + (size_t)k * nbp];
+            h->invI[3 * b + k] = invI[L + (size_t)k * nbp];
+        }
+        h->invm[b] = invm[L];
+        h->cls[b] = cls[L];
+        h->dof[b] = dof[L];
+        for (int j = 0; j < h->ref_first[b + 1] - h->ref_first[b]; j++)
+            for (int c = 0; c < 3; c++)
+                h->dfix[3 * (size_t)(h->ref_first[b] + j) + c] = d[h->body_first[L] + j + (size_t)c * nbap];
+    }
+    h->host_geom_valid = true;
+    return RBX_OK;
+}
+
 void rbx::system_ranges(const rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
                         std::vector<int>& free0, std::vector<int>& dof) {
     const int S = (int)slot_offsets.size() - 1;
@@ -154,214 +200,29 @@ void rbx::system_ranges(const rbx_integrator* h, const std::vector<int>& slot_of
 
 namespace {
 
-// ---------------------------------------------------------------------------------------------
-// Body geometry (robust): principal frame by cyclic Jacobi rotations, sorted descending, as the
-// rows of a proper rotation A (space -> body).
-// ---------------------------------------------------------------------------------------------
-void principal_axes(const double M[9], double w[3], double A[9]) {
-    double a[3][3], v[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++) a[i][j] = 0.5 * (M[3 * i + j] + M[3 * j + i]);
-    for (int sweep = 0; sweep < 60; sweep++) {
-        double off = a[0][1] * a[0][1] + a[0][2] * a[0][2] + a[1][2] * a[1][2];
-        double diag = a[0][0] * a[0][0] + a[1][1] * a[1][1] + a[2][2] * a[2][2];
-        if (off == 0.0 || off <= 1e-36 * diag) break;
-        for (int p = 0; p < 2; p++)
-            for (int r = p + 1; r < 3; r++) {
-                if (a[p][r] == 0.0) continue;
-                double theta = (a[r][r] - a[p][p]) / (2.0 * a[p][r]);
-                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-                double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-                for (int k = 0; k < 3; k++) {
-                    double akp = a[k][p], akr = a[k][r];
-                    a[k][p] = c * akp - s * akr;
-                    a[k][r] = s * akp + c * akr;
-                }
-                for (int k = 0; k < 3; k++) {
-                    double apk = a[p][k], ark = a[r][k];
-                    a[p][k] = c * apk - s * ark;
-                    a[r][k] = s * apk + c * ark;
-                }
-                for (int k = 0; k < 3; k++) {
-                    double vkp = v[k][p], vkr = v[k][r];
-                    v[k][p] = c * vkp - s * vkr;
-                    v[k][r] = s * vkp + c * vkr;
-                }
-            }
+// The atoms of one body in the user's host arrays (the accessor of build_body, rbx_setup.cuh).
+struct HostAtoms {
+    int n;
+    const int* atoms;
+    const double* masses;
+    const double* R;
+    const double* V;
+    double* dfix;
+    double mass(int j) const { return masses[atoms[j]]; }
+    V3<double> pos(int j) const {
+        const int i = atoms[j];
+        return v3<double>(R[3 * i], R[3 * i + 1], R[3 * i + 2]);
     }
-    int idx[3] = {0, 1, 2};
-    for (int i = 0; i < 3; i++)
-        for (int j = i + 1; j < 3; j++)
-            if (a[idx[j]][idx[j]] > a[idx[i]][idx[i]]) std::swap(idx[i], idx[j]);
-    for (int i = 0; i < 3; i++) {
-        w[i] = a[idx[i]][idx[i]];
-        for (int k = 0; k < 3; k++) A[3 * i + k] = v[k][idx[i]];
+    V3<double> vel(int j) const {
+        const int i = atoms[j];
+        return v3<double>(V[3 * i], V[3 * i + 1], V[3 * i + 2]);
     }
-    A[6] = A[1] * A[5] - A[2] * A[4];
-    A[7] = A[2] * A[3] - A[0] * A[5];
-    A[8] = A[0] * A[4] - A[1] * A[3];
-}
-
-// Unit quaternion of a proper rotation matrix (Shepperd's method, as in MatVec.cpp:344-373).
-Q4<double> quaternion_of(const double* M) {
-    double t[4] = {1.0 + M[0] + M[4] + M[8], 1.0 + M[0] - M[4] - M[8], 1.0 - M[0] + M[4] - M[8], 1.0 - M[0] - M[4] + M[8]};
-    int k = 0;
-    for (int i = 1; i < 4; i++)
-        if (t[i] > t[k]) k = i;
-    double f = 0.5 / std::sqrt(t[k]);
-    double q[4];
-    switch (k) {
-        case 0: q[1] = (M[5] - M[7]) * f; q[2] = (M[6] - M[2]) * f; q[3] = (M[1] - M[3]) * f; break;
-        case 1: q[0] = (M[5] - M[7]) * f; q[2] = (M[1] + M[3]) * f; q[3] = (M[2] + M[6]) * f; break;
-        case 2: q[0] = (M[6] - M[2]) * f; q[1] = (M[1] + M[3]) * f; q[3] = (M[5] + M[7]) * f; break;
-        default: q[0] = (M[1] - M[3]) * f; q[1] = (M[2] + M[6]) * f; q[2] = (M[5] + M[7]) * f; break;
+    void set_d(int j, V3<double> d) {
+        dfix[3 * j] = d.x;
+        dfix[3 * j + 1] = d.y;
+        dfix[3 * j + 2] = d.z;
     }
-    q[k] = t[k] * f;
-    return q4<double>(q[0], q[1], q[2], q[3]);
-}
-
-uint8_t rotation_class(const double I[3]) {
-    if (I[2] == 0.0) return ROT_SYMMETRIC_AXIS2;  // linear body
-    const double tol = 1e-12 * I[0];
-    bool g01 = I[0] - I[1] <= tol, g12 = I[1] - I[2] <= tol;
-    if (g01 && g12) return ROT_SPHERICAL;
-    if (g01) return ROT_SYMMETRIC_AXIS2;
-    if (g12) return ROT_SYMMETRIC_AXIS0;
-    return ROT_ASYMMETRIC;
-}
-
-// Canonical body frame: each eigenvector row gets its largest-magnitude component positive; a top
-// with two equal moments has its degenerate axes fixed by the first atom off the unique axis; a
-// spherical top uses the space frame. Equivalent frames therefore never depend on rounding.
-void canon_sign(V3<double>& v) {
-    double a[3] = {std::fabs(v.x), std::fabs(v.y), std::fabs(v.z)};
-    double c[3] = {v.x, v.y, v.z};
-    int k = 0;
-    for (int i = 1; i < 3; i++)
-        if (a[i] > a[k]) k = i;
-    if (c[k] < 0) v = v * -1.0;
-}
-
-void canonical_frame(double* A, const double* I, const std::vector<V3<double>>& delta, const std::vector<double>& d2) {
-    const uint8_t cls = rotation_class(I);
-    auto row = [&](int r) { return v3(A[3 * r], A[3 * r + 1], A[3 * r + 2]); };
-    auto set = [&](int r, V3<double> v) { A[3 * r] = v.x; A[3 * r + 1] = v.y; A[3 * r + 2] = v.z; };
-    if (cls == ROT_SPHERICAL) {
-        for (int i = 0; i < 9; i++) A[i] = (i % 4 == 0) ? 1.0 : 0.0;
-        return;
-    }
-    if (cls == ROT_ASYMMETRIC) {
-        V3<double> a = row(0), b = row(1);
-        canon_sign(a);
-        canon_sign(b);
-        set(0, a); set(1, b); set(2, cross(a, b));
-        return;
-    }
-    const int k = cls == ROT_SYMMETRIC_AXIS0 ? 0 : 2;
-    V3<double> u = row(k), e1 = row(k == 0 ? 1 : 0);
-    canon_sign(u);
-    double d2max = 0.0;
-    for (double x : d2) d2max = std::max(d2max, x);
-    for (size_t j = 0; j < delta.size(); j++) {
-        V3<double> p = delta[j] - u * dot(u, delta[j]);
-        double pp = dot(p, p);
-        if (pp > 1e-6 * d2max) { e1 = p * (1.0 / std::sqrt(pp)); break; }
-    }
-    V3<double> e2 = cross(u, e1);
-    if (k == 0) { set(0, u); set(1, e1); set(2, e2); }
-    else { set(0, e1); set(1, e2); set(2, u); }
-}
-
-struct BodySetup {
-    double mass, invm, I[3], invI[3];
-    int dof;
-    uint8_t cls;
-    V3<double> r, v;
-    Q4<double> q, pi;
 };
-
-// Geometry and momenta of one body from its atoms (RigidBody.cpp:65-142, robust variants:
-// longest displacement as the axis of a linear body, |component| orthonormal vector, Jacobi
-// principal axes, momenta recomputed from scratch on every call).
-void build_body(const int* atoms, int N, const double* masses, const double* R, const double* V, double* dfix,
-                BodySetup& out) {
-    double mass = 0.0;
-    V3<double> rcm = v3(0.0, 0.0, 0.0);
-    for (int j = 0; j < N; j++) {
-        int i = atoms[j];
-        mass += masses[i];
-        rcm = rcm + v3(R[3 * i], R[3 * i + 1], R[3 * i + 2]) * masses[i];
-    }
-    rcm = rcm * (1.0 / mass);
-    std::vector<V3<double>> delta(N);
-    std::vector<double> d2(N);
-    int jmax = 0;
-    for (int j = 0; j < N; j++) {
-        int i = atoms[j];
-        delta[j] = v3(R[3 * i], R[3 * i + 1], R[3 * i + 2]) - rcm;
-        d2[j] = dot(delta[j], delta[j]);
-        if (d2[j] > d2[jmax]) jmax = j;
-    }
-    const double TOL = 1.0e-5;
-    V3<double> u = delta[jmax] * (1.0 / std::sqrt(d2[jmax]));
-    canon_sign(u);
-    bool linear = d2[jmax] > 0.0;
-    for (int j = 0; linear && j < N; j++) {
-        double udj = dot(u, delta[j]);
-        linear = d2[j] < TOL * d2[jmax] || std::fabs(udj * udj / d2[j] - 1.0) < TOL;
-    }
-    double A[9];
-    if (linear) {
-        double moi = 0.0;
-        for (int j = 0; j < N; j++) moi += masses[atoms[j]] * d2[j];
-        out.I[0] = out.I[1] = moi;
-        out.I[2] = 0.0;
-        double c[3] = {std::fabs(u.x), std::fabs(u.y), std::fabs(u.z)};
-        int imin = c[0] < c[1] ? 0 : 1;
-        if (c[2] < c[imin]) imin = 2;
-        V3<double> e = v3(imin == 0 ? 1.0 : 0.0, imin == 1 ? 1.0 : 0.0, imin == 2 ? 1.0 : 0.0);
-        V3<double> vv = e - u * dot(u, e);
-        vv = vv * (1.0 / std::sqrt(dot(vv, vv)));
-        V3<double> ww = cross(u, vv);
-        double rows[9] = {vv.x, vv.y, vv.z, ww.x, ww.y, ww.z, u.x, u.y, u.z};
-        std::memcpy(A, rows, sizeof rows);
-        out.dof = 5;
-    } else {
-        double M[9] = {0};
-        for (int j = 0; j < N; j++) {
-            double m = masses[atoms[j]];
-            double x[3] = {delta[j].x, delta[j].y, delta[j].z};
-            for (int r = 0; r < 3; r++)
-                for (int c = 0; c < 3; c++) M[3 * r + c] += ((r == c ? d2[j] : 0.0) - x[r] * x[c]) * m;
-        }
-        principal_axes(M, out.I, A);
-        canonical_frame(A, out.I, delta, d2);
-        out.dof = 6;
-    }
-    out.q = quaternion_of(A);
-    for (int j = 0; j < N; j++)
-        for (int r = 0; r < 3; r++) dfix[3 * j + r] = A[3 * r] * delta[j].x + A[3 * r + 1] * delta[j].y + A[3 * r + 2] * delta[j].z;
-    out.mass = mass;
-    out.invm = 1.0 / mass;
-    for (int k = 0; k < 3; k++) out.invI[k] = out.I[k] == 0.0 ? 0.0 : 1.0 / out.I[k];
-    out.cls = rotation_class(out.I);
-    out.r = rcm;
-    V3<double> p = v3(0.0, 0.0, 0.0);
-    for (int j = 0; j < N; j++) {
-        int i = atoms[j];
-        p = p + v3(V[3 * i], V[3 * i + 1], V[3 * i + 2]) * masses[i];
-    }
-    V3<double> vcm = p * (1.0 / mass);
-    V3<double> L = v3(0.0, 0.0, 0.0);
-    for (int j = 0; j < N; j++) {
-        int i = atoms[j];
-        V3<double> dv = v3(V[3 * i], V[3 * i + 1], V[3 * i + 2]) - vcm;
-        V3<double> body = rotate_to_body(out.q, dv) * masses[i];
-        L = L + cross(v3(dfix[3 * j], dfix[3 * j + 1], dfix[3 * j + 2]), body);
-    }
-    out.v = vcm;
-    out.pi = qB(out.q, L * 2.0);
-}
 
 template <class T> int upload(DevArray<T>& a, const std::vector<T>& h) {
     if (a.alloc(h.size()) != cudaSuccess) return fail(RBX_ERR_CUDA, "cudaMalloc of %zu bytes failed", h.size() * sizeof(T));
@@ -416,7 +277,10 @@ int upload_layout(rbx_integrator* h) {
     std::vector<int> atom_loc(h->nba), free_loc(h->nf);
     for (int k = 0; k < h->nba; k++) atom_loc[k] = h->location[h->body_atoms[k]];
     for (int j = 0; j < h->nf; j++) free_loc[j] = h->location[h->free_atoms[j]];
+    std::vector<double> bmass(h->nba);
+    for (int k = 0; k < h->nba; k++) bmass[k] = h->masses[h->body_atoms[k]];
     int rc = upload(h->d_atom0, h->body_first);
+    if (!rc) rc = upload(h->d_bmass, bmass);
     if (!rc) rc = upload(h->d_tiles, h->tile_body0);
     if (!rc) rc = upload(h->d_atom_loc, atom_loc);
     if (!rc) rc = upload(h->d_free_loc, free_loc);
@@ -622,9 +486,10 @@ int rbx_set_atom_locations(rbx_integrator* h, const int* location) {
             seen[location[i]] = 1;
         }
     }
+    CUDA_TRY(cudaSetDevice(h->device));
+    if ((rc = ensure_host_geometry(h))) return rc;  // read in the current order, re-uploaded below
     h->location.assign(location, location + h->natoms);
     h->max_location = *std::max_element(h->location.begin(), h->location.end());
-    CUDA_TRY(cudaSetDevice(h->device));
     // Re-plan the library order for the new slots and carry the body state (and constants)
     // over to it; the raw rows are permuted, so the float-float state moves bit for bit.
     const std::vector<int> old_pos = h->lib_pos;
@@ -682,7 +547,8 @@ int rbx_upload_state(rbx_integrator* h, const double* positions, const double* v
     for (int b = 0; b < nb; b++) {
         const int f = h->ref_first[b], N = h->ref_first[b + 1] - f;
         BodySetup s;
-        build_body(&h->ref_atoms[f], N, h->masses.data(), positions, velocities, &h->dfix[3 * (size_t)f], s);
+        HostAtoms at{N, &h->ref_atoms[f], h->masses.data(), positions, velocities, &h->dfix[3 * (size_t)f]};
+        build_body(at, s);
         for (int k = 0; k < 3; k++) { h->I[3 * b + k] = s.I[k]; h->invI[3 * b + k] = s.invI[k]; }
         h->invm[b] = s.invm;
         h->cls[b] = s.cls;
@@ -699,6 +565,35 @@ int rbx_upload_state(rbx_integrator* h, const double* positions, const double* v
     if ((rc = put_state(h, state))) return rc;
     if ((rc = upload_bodies(h))) return rc;
     h->have_state = true;
+    h->host_geom_valid = true;
+    return RBX_OK;
+}
+
+int rbx_upload_state_device(rbx_integrator* h, void* stream, const rbx_buffers* buf) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!buf || !buf->posq || !buf->velm) return fail(RBX_ERR_INVALID_ARGUMENT, "null device buffer");
+    if (h->prec == PREC_MIXED && !buf->posq_correction)
+        return fail(RBX_ERR_INVALID_ARGUMENT, "mixed precision needs posq_correction");
+    if (buf->stride < h->natoms || h->max_location >= buf->stride)
+        return fail(RBX_ERR_INVALID_ARGUMENT, "device slots outside buffers of stride %d", buf->stride);
+    CUDA_TRY(cudaSetDevice(h->device));
+    if (!h->d_I.p && (h->d_I.alloc((size_t)3 * h->nb_pad) != cudaSuccess || h->d_dof.alloc(std::max(h->nb, 1)) != cudaSuccess ||
+                      h->d_setup_counts.alloc(2) != cudaSuccess))
+        return fail(RBX_ERR_CUDA, "cudaMalloc of setup arrays failed");
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemsetAsync(h->d_setup_counts.p, 0, 2 * sizeof(int), st));
+    SetupOut o{h->d_I.p, h->d_dof.p, h->d_setup_counts.p, (unsigned int*)(h->d_setup_counts.p + 1)};
+    if (launch_setup_bodies(h->prec, h->sys(), devbuf(buf), h->d_bmass.p, o, stream) < 0)
+        return fail(RBX_ERR_CUDA, "body setup kernel failed: %s", cudaGetErrorString(cudaGetLastError()));
+    int counts[2] = {0, 0};
+    CUDA_TRY(cudaMemcpyAsync(counts, h->d_setup_counts.p, sizeof counts, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (counts[1]) return fail(RBX_ERR_NUMERIC, "non-finite rigid-body state from the device setup");
+    h->ndof = 3 * h->nf + counts[0];
+    h->have_state = true;
+    h->host_geom_valid = false;
+    h->last_launches = 1;
     return RBX_OK;
 }
 
@@ -767,6 +662,7 @@ int rbx_get_body_geometry(rbx_integrator* h, double* moments, double* body_fixed
     int rc = check(h);
     if (rc) return rc;
     if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body geometry");
+    if ((rc = ensure_host_geometry(h))) return rc;
     if (moments) std::memcpy(moments, h->I.data(), h->I.size() * sizeof(double));
     if (body_fixed) std::memcpy(body_fixed, h->dfix.data(), h->dfix.size() * sizeof(double));
     return RBX_OK;

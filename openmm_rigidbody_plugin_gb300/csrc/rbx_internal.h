@@ -125,8 +125,21 @@ size_t step_smem_bytes(int prec);
 // Record an error message for rbx_last_error() and return `code` (defined in rbx_host.cpp).
 int set_error(int code, const char* fmt, ...);
 
+// Device-side body setup (rbx_setup.cu): principal moments I (3 rows of nb_pad), degrees of
+// freedom per body, their sum (atomically added) and a status word (bit 0: non-finite state).
+struct SetupOut {
+    double* I;
+    int* dof;
+    int* ndof;
+    unsigned int* status;
+};
+int launch_setup_bodies(int prec, const DevSys& s, const DevBuf& b, const double* bmass, const SetupOut& out,
+                        void* stream);
+
 // Internal views of an integrator for the batched driver (defined in rbx_host.cpp).
 DevSys device_system(const rbx_integrator* h);
+// Host copies of the body geometry, fetched from the device after a device-side setup.
+int ensure_host_geometry(rbx_integrator* h);
 // For systems whose atoms occupy consecutive device-slot ranges [slot_offsets[s],
 // slot_offsets[s+1]): the library-order ranges of their bodies (body0[S+1]) and free atoms
 // (free0[S+1]), and their degrees of freedom (dof[S]).

@@ -142,6 +142,11 @@ class IntegratorKernel:
         v = np.ascontiguousarray(velocities, dtype=np.float64)
         _lib.check(self._lib.rbx_upload_state(self._h, _dptr(x), _dptr(v)))
 
+    def upload_state_device(self, buffers, stream=None):
+        """Body setup on the device from the positions and velocities in `buffers`."""
+        b = buffers.struct()
+        _lib.check(self._lib.rbx_upload_state_device(self._h, _stream_handle(stream), ctypes.byref(b)))
+
     def _get_int(self, fn):
         out = ctypes.c_int()
         _lib.check(fn(self._h, ctypes.byref(out)))
