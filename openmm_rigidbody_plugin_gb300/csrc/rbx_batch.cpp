@@ -345,11 +345,16 @@ int rbx_batch_destroy(rbx_batch* b) {
 int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, const double* velocities) {
     int rc = check(b);
     if (rc) return rc;
-    b->drop_graph();  // the integrator re-plans its device arrays
-    if ((rc = rbx_context_set_state(b->integ, stream, positions, velocities))) return rc;
+    b->drop_graph();
+    // positions and velocities into the device buffers, bodies built there (no host round trip)
+    if ((rc = rbx_context_load(b->integ, stream, positions, velocities))) return rc;
+    rbx_buffers rb;
+    if ((rc = rbx_context_buffers(b->integ, &rb))) return rc;
+    if ((rc = rbx_upload_state_device(b->integ, stream, &rb))) return rc;
     // body atoms start where the body state puts them (the step kernels' arithmetic), so that a
     // system's trajectory is a function of its body state alone, in or out of a batch
     if ((rc = rbx_context_sync_bodies(b->integ, stream))) return rc;
+    if ((rc = sync_host_dof(b->integ))) return rc;
     std::vector<int> body0, free0;
     system_ranges(b->integ, b->offsets, body0, free0, b->dof);
     if ((rc = upload_vec(b->d_body0, body0)) || (rc = upload_vec(b->d_free0, free0))) return rc;

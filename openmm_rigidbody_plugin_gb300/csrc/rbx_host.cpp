@@ -130,6 +130,14 @@ struct rbx_integrator {
 
 rbx::DevSys rbx::device_system(const rbx_integrator* h) { return h->sys(); }
 
+int rbx::sync_host_dof(rbx_integrator* h) {
+    if (h->host_geom_valid || !h->have_state || h->nb == 0) return RBX_OK;
+    std::vector<int> dof(h->nb);
+    CUDA_TRY(cudaMemcpy(dof.data(), h->d_dof.p, dof.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int L = 0; L < h->nb; L++) h->dof[h->lib_body[L]] = dof[L];
+    return RBX_OK;
+}
+
 int rbx::ensure_host_geometry(rbx_integrator* h) {
     if (h->host_geom_valid || !h->have_state) return RBX_OK;
     const int nb = h->nb, nbp = h->nb_pad, nbap = h->nba_pad;

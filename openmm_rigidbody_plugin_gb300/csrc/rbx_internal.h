@@ -138,8 +138,10 @@ int launch_setup_bodies(int prec, const DevSys& s, const DevBuf& b, const double
 
 // Internal views of an integrator for the batched driver (defined in rbx_host.cpp).
 DevSys device_system(const rbx_integrator* h);
-// Host copies of the body geometry, fetched from the device after a device-side setup.
+// Host copies of the body geometry, fetched from the device after a device-side setup (all of
+// it, or only the degrees of freedom per body).
 int ensure_host_geometry(rbx_integrator* h);
+int sync_host_dof(rbx_integrator* h);
 // For systems whose atoms occupy consecutive device-slot ranges [slot_offsets[s],
 // slot_offsets[s+1]): the library-order ranges of their bodies (body0[S+1]) and free atoms
 // (free0[S+1]), and their degrees of freedom (dof[S]).
