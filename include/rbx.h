@@ -127,6 +127,36 @@ int rbx_integrate_fused(rbx_integrator* h, void* stream, const rbx_buffers* buf,
 int rbx_kinetic_energies(rbx_integrator* h, void* stream, const rbx_buffers* buf, double* out2);
 
 /*
+ * Refined ("shadow") energies. Replaces RigidBodyIntegrator::setComputeRefinedEnergies
+ * (openmmapi/src/RigidBodyIntegrator.cpp:34-38), which compiles the plugin's kernels with
+ * COMPMOD = 1 (CudaRigidBodyKernels.cpp:240); getRefinedKineticEnergies
+ * (CudaRigidBodyKernels.cpp:469-476, :118-163; refinedKineticEnergies kernel,
+ * rigidbodyintegrator.cu:433-443) and getPotentialEnergyRefinement (CudaRigidBodyKernels.cpp:
+ * 481-494, :168-194; potentialEnergyRefinement kernel, rigidbodyintegrator.cu:449-469).
+ *
+ * While on, every part1 / fused step starts and every part2 closes the stencils of the reference
+ * (rigidbodyintegrator.cu:238-243, :285-292, :318-321, :380-384): after part2 of step n,
+ *   refined KE_t = sum over bodies and free atoms of m v . s / (6h) (s/2 for free atoms),
+ *   refined KE_r = sum over bodies of qdot . pi / (6h),
+ *   U_refinement = -h^2/24 (sum |F|^2/m + tau . I^-1 . tau),
+ * with s and qdot the position and quaternion stencils over t-h .. t+2h. Free atoms use the
+ * stencil weights of the bodies (-1, 5, 2 on the three half-step displacements); the reference's
+ * free-atom path weights the first +1, which reports 4/3 of the kinetic energy for uniform motion.
+ * Sums are FP64 in a fixed order; the kernels write per-body corrections to the plain kinetic
+ * energy, so nothing is lost to cancellation in the FP32 paths.
+ * Off (the default): rbx_refined_kinetic_energies returns the plain kinetic energies and
+ * rbx_potential_energy_refinement 0, as the reference does. On, both need a completed step (part1
+ * or fused, then part2, same step size) since the last state change (RBX_ERR_STATE otherwise).
+ * Switching it on allocates 28-56 bytes per body and 12-24 per free atom; the step kernels then
+ * read and write them (the plain step is unchanged while it is off). Both queries synchronise
+ * `stream`.
+ */
+int rbx_set_compute_refined_energies(rbx_integrator* h, int compute);
+int rbx_get_compute_refined_energies(const rbx_integrator* h, int* out);
+int rbx_refined_kinetic_energies(rbx_integrator* h, void* stream, const rbx_buffers* buf, double* out2);
+int rbx_potential_energy_refinement(rbx_integrator* h, void* stream, const rbx_buffers* buf, double* out1);
+
+/*
  * Body state exchange for tests and checkpoints, host arrays with bodies in the reference's
  * order (ascending body index, as RigidBodySystem numbers them; RigidBodySystem.cpp:28-49):
  *   state [num_bodies*14]: r[3], v[3], q[4], pi[4] per body (v = centre-of-mass velocity)

@@ -44,6 +44,10 @@ SIGNATURES = [
     ("rbx_integrate_part2", ctypes.c_int, [_vp, _vp, _bp, ctypes.c_double]),
     ("rbx_integrate_fused", ctypes.c_int, [_vp, _vp, _bp, ctypes.c_double]),
     ("rbx_kinetic_energies", ctypes.c_int, [_vp, _vp, _bp, _dp]),
+    ("rbx_set_compute_refined_energies", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("rbx_get_compute_refined_energies", ctypes.c_int, [_vp, _ip]),
+    ("rbx_refined_kinetic_energies", ctypes.c_int, [_vp, _vp, _bp, _dp]),
+    ("rbx_potential_energy_refinement", ctypes.c_int, [_vp, _vp, _bp, _dp]),
     ("rbx_get_body_state", ctypes.c_int, [_vp, _dp]),
     ("rbx_set_body_state", ctypes.c_int, [_vp, _dp]),
     ("rbx_get_body_geometry", ctypes.c_int, [_vp, _dp, _dp]),

@@ -10,14 +10,16 @@
 * ``ForceField`` -- rigid-body templates over residue templates: registerBodyTemplate,
   resolveBodies with merge lists, removeConstraints, removeForces (python/forcefield.py:3-180).
 * ``StateDataReporter`` -- the extra columns of python/statedatareporter.py:5-90 (translational
-  and rotational energies; temperature from the rigid-body degrees of freedom, minus 3 with a
-  centre-of-mass motion remover).
+  and rotational energies, the refined ("shadow") energies and temperature; temperature from the
+  rigid-body degrees of freedom, minus 3 with a centre-of-mass motion remover).
 
 ``Context`` stands in for an OpenMM Context on one device: a ``System`` (masses, constraints,
 forces), the integrator, positions, velocities and a force provider, a callable positions ->
 (forces, potential energy) evaluated on the host between the two halves of each step, the way the
 Reference platform drives RigidBodySystem::integratePart1/2 (RigidBodySystem.cpp:170-204).
-Refined ("shadow") energies are not provided.
+Refined ("shadow") energies: setComputeRefinedEnergies before the integrator is bound, then
+getRefinedKineticEnergies / getPotentialEnergyRefinement after a step (RigidBodyIntegrator.cpp:
+34-38, 84-90), computed on the device by the step kernels.
 """
 import re
 import xml.etree.ElementTree as ET
@@ -211,6 +213,7 @@ class RigidBodyIntegrator:
         self._context = context
         self._kernel = _kernel.IntegratorKernel(context.system.masses, self._bodyIndices, rotation_mode=self._mode,
                                                 precision=context.precision, device=context.device)
+        self._kernel.set_compute_refined_energies(self._refined)
 
     def getRigidBodySystem(self):
         self._require()
@@ -243,10 +246,18 @@ class RigidBodyIntegrator:
         return sum(self.getKineticEnergies())
 
     def getRefinedKineticEnergies(self):
-        raise NotImplementedError("refined (shadow) kinetic energies are not provided by this build")
+        """[translational, rotational] refined kinetic energy (kJ/mol) after the last step; the plain
+        kinetic energies while refined energies are off (CudaRigidBodyKernels.cpp:469-476)."""
+        self._require()
+        self._context._ensure_state()
+        return [float(e) for e in self._kernel.context_refined_kinetic_energies()]
 
     def getPotentialEnergyRefinement(self):
-        raise NotImplementedError("the potential energy refinement is not provided by this build")
+        """-dt^2/24 (sum |F|^2/m + tau.I^-1.tau) after the last step; 0 while refined energies are off
+        (CudaRigidBodyKernels.cpp:481-494)."""
+        self._require()
+        self._context._ensure_state()
+        return self._kernel.context_potential_energy_refinement()
 
 
 class State:
@@ -444,26 +455,37 @@ class ForceField:
 class StateDataReporter:
     """Writes one comma-separated line per report: step, potential, kinetic and total energy,
     temperature (rigid-body degrees of freedom, minus 3 with a CMMotionRemover in the System),
-    and optionally the translational and rotational kinetic energies."""
+    and optionally the translational and rotational kinetic energies and the refined energies, in
+    the column order of python/statedatareporter.py:30-48."""
+
+    _NAMES = {"step": '#"Step"', "potentialEnergy": "Potential Energy (kJ/mole)",
+              "kineticEnergy": "Kinetic Energy (kJ/mole)", "totalEnergy": "Total Energy (kJ/mole)",
+              "temperature": "Temperature (K)", "translationalEnergy": "Translational Energy (kJ/mole)",
+              "rotationalEnergy": "Rotational Energy (kJ/mole)",
+              "refinedPotentialEnergy": "Refined Potential Energy (kJ/mole)",
+              "refinedKineticEnergy": "Refined Kinetic Energy (kJ/mole)",
+              "refinedTotalEnergy": "Refined Total Energy (kJ/mole)",
+              "refinedTemperature": "Refined Temperature (K)",
+              "refinedTranslationalEnergy": "Refined Translational Energy (kJ/mole)",
+              "refinedRotationalEnergy": "Refined Rotational Energy (kJ/mole)"}
 
     def __init__(self, file, reportInterval, step=True, potentialEnergy=True, kineticEnergy=True,
-                 totalEnergy=True, temperature=True, translationalEnergy=False, rotationalEnergy=False, **refined):
-        if any(refined.values()):
-            raise NotImplementedError("refined (shadow) energy columns are not provided by this build")
+                 totalEnergy=True, temperature=True, translationalEnergy=False, rotationalEnergy=False,
+                 refinedPotentialEnergy=False, refinedKineticEnergy=False, refinedTotalEnergy=False,
+                 refinedTemperature=False, refinedTranslationalEnergy=False, refinedRotationalEnergy=False):
         self._out = file
         self._interval = int(reportInterval)
         self._cols = dict(step=step, potentialEnergy=potentialEnergy, kineticEnergy=kineticEnergy,
                           totalEnergy=totalEnergy, temperature=temperature, translationalEnergy=translationalEnergy,
-                          rotationalEnergy=rotationalEnergy)
+                          rotationalEnergy=rotationalEnergy, refinedPotentialEnergy=refinedPotentialEnergy,
+                          refinedKineticEnergy=refinedKineticEnergy, refinedTotalEnergy=refinedTotalEnergy,
+                          refinedTemperature=refinedTemperature, refinedTranslationalEnergy=refinedTranslationalEnergy,
+                          refinedRotationalEnergy=refinedRotationalEnergy)
         self._header = False
         self._dof = None
 
     def headers(self):
-        names = {"step": '#"Step"', "potentialEnergy": "Potential Energy (kJ/mole)",
-                 "kineticEnergy": "Kinetic Energy (kJ/mole)", "totalEnergy": "Total Energy (kJ/mole)",
-                 "temperature": "Temperature (K)", "translationalEnergy": "Translational Energy (kJ/mole)",
-                 "rotationalEnergy": "Rotational Energy (kJ/mole)"}
-        return [names[k] for k, on in self._cols.items() if on]
+        return [self._NAMES[k] for k, on in self._cols.items() if on]
 
     def report(self, context, step):
         if self._dof is None:
@@ -474,8 +496,19 @@ class StateDataReporter:
             self._out.write(",".join(self.headers()) + "\n")
             self._header = True
         st = context.getState(getEnergy=True)
-        kt, kr = context.integrator.getKineticEnergies()
+        integ = context.integrator
+        kt, kr = integ.getKineticEnergies()
         u = st.getPotentialEnergy()
         vals = {"step": step, "potentialEnergy": u, "kineticEnergy": kt + kr, "totalEnergy": u + kt + kr,
                 "temperature": 2.0 * (kt + kr) / (self._dof * KB), "translationalEnergy": kt, "rotationalEnergy": kr}
-        self._out.write(",".join(str(vals[k]) for k, on in self._cols.items() if on) + "\n")
+        c = self._cols
+        if c["refinedPotentialEnergy"] or c["refinedTotalEnergy"]:
+            vals["refinedPotentialEnergy"] = u + integ.getPotentialEnergyRefinement()
+        if any(c[k] for k in ("refinedKineticEnergy", "refinedTotalEnergy", "refinedTemperature",
+                              "refinedTranslationalEnergy", "refinedRotationalEnergy")):
+            rt, rr = integ.getRefinedKineticEnergies()
+            vals.update(refinedKineticEnergy=rt + rr, refinedTranslationalEnergy=rt, refinedRotationalEnergy=rr,
+                        refinedTemperature=2.0 * (rt + rr) / (self._dof * KB))
+            if c["refinedTotalEnergy"]:
+                vals["refinedTotalEnergy"] = rt + rr + vals["refinedPotentialEnergy"]
+        self._out.write(",".join(str(vals[k]) for k, on in c.items() if on) + "\n")

@@ -59,7 +59,7 @@ int rbx::set_error(int code, const char* fmt, ...) {
 struct rbx_integrator {
     int natoms = 0, nb = 0, nf = 0, nba = 0, ndof = 0, mode = 0, prec = PREC_MIXED, device = 0;
     int max_location = 0;  // largest device slot in use; every buffer stride must exceed it
-    int nb_pad = 0, nba_pad = 0, n_body_tiles = 0, n_free_tiles = 0;
+    int nb_pad = 0, nba_pad = 0, nf_pad = 0, n_body_tiles = 0, n_free_tiles = 0;
     bool have_state = false;
     int last_launches = 0;
     std::vector<double> masses;
@@ -92,7 +92,16 @@ struct rbx_integrator {
     DevArray<unsigned char> d_fixed;  // float or double SoA
     DevArray<double> d_ke_partial, d_ke_out;
     DevArray<unsigned int> d_ke_count;
-    double* h_ke = nullptr;  // pinned [2]
+    double* h_ke = nullptr;  // pinned [8]: kinetic energies [0, 2), refined sums [2, 5)
+
+    // refined energies (rbx_set_compute_refined_energies): stencil sums and per-unit terms
+    bool refined = false;
+    int ref_phase = 0;  // 0: no stencil, 1: started by part1 or a fused step, 2: closed by part2
+    double ref_dt = 0.0;
+    DevArray<unsigned char> d_ref_start;
+    DevArray<float> d_ref_out;
+    DevArray<double> d_ref_partial, d_ref_res;
+    DevArray<unsigned int> d_ref_count;
 
     // owned OpenMM-layout context (host-buffer API)
     int stride = 0;
@@ -109,11 +118,13 @@ struct rbx_integrator {
 
     DevSys sys() const {
         DevSys s;
-        s.nb = nb; s.nf = nf; s.nba = nba; s.nb_pad = nb_pad; s.nba_pad = nba_pad;
+        s.nb = nb; s.nf = nf; s.nba = nba; s.nb_pad = nb_pad; s.nba_pad = nba_pad; s.nf_pad = nf_pad;
         s.n_body_tiles = n_body_tiles; s.n_free_tiles = n_free_tiles; s.rot_n = mode;
         s.state = d_state.p; s.invm = d_invm.p; s.invI = d_invI.p; s.bconst = d_bconst.p;
         s.atom0 = d_atom0.p; s.cls = d_cls.p;
         s.d = d_fixed.p; s.atom_loc = d_atom_loc.p; s.free_loc = d_free_loc.p; s.tile_body0 = d_tiles.p;
+        s.ref_start = refined ? (void*)d_ref_start.p : nullptr;
+        s.ref_out = refined ? d_ref_out.p : nullptr;
         return s;
     }
     ~rbx_integrator() {
@@ -372,7 +383,49 @@ int run_step(rbx_integrator* h, int kind, void* stream, const rbx_buffers* buf, 
     int n = launch_step(h->prec, kind, h->sys(), devbuf(buf), dt, stream);
     if (n < 0) return fail(RBX_ERR_CUDA, "step kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     h->last_launches = n;
+    if (h->refined) {
+        // part1 and fused steps start the refined-energy stencils; part2 closes them if the last
+        // start used the same step size
+        if (kind == STEP_PART2) h->ref_phase = h->ref_phase == 1 && h->ref_dt == dt ? 2 : 0;
+        else h->ref_phase = 1;
+        h->ref_dt = dt;
+    }
     return RBX_OK;
+}
+
+// Rows [r0, r0 + rows) of a device array of `es`-byte elements with row stride ld: entry i of
+// each row moves from position src[i].
+int permute_rows(void* p, size_t r0, size_t rows, size_t ld, size_t es, const std::vector<int>& src) {
+    if (src.empty()) return RBX_OK;
+    unsigned char* base = (unsigned char*)p + r0 * ld * es;
+    std::vector<unsigned char> in(rows * ld * es), out(rows * ld * es, 0);
+    CUDA_TRY(cudaMemcpy(in.data(), base, in.size(), cudaMemcpyDeviceToHost));
+    for (size_t r = 0; r < rows; r++)
+        for (size_t i = 0; i < src.size(); i++) std::memcpy(&out[(r * ld + i) * es], &in[(r * ld + src[i]) * es], es);
+    CUDA_TRY(cudaMemcpy(base, out.data(), out.size(), cudaMemcpyHostToDevice));
+    return RBX_OK;
+}
+
+// After a re-plan of the library order: move the refined-energy stencil sums and terms of every
+// body and free atom to its new position (bit for bit), so that a reordering of the device slots
+// between the two halves of a step, or between a step and the energy query, loses nothing.
+int move_refined(rbx_integrator* h, const std::vector<int>& old_pos, const std::vector<int>& old_free) {
+    const size_t es = h->prec == PREC_DOUBLE ? 8 : 4, nbp = h->nb_pad, nfp = h->nf_pad;
+    std::vector<int> bsrc(h->nb), fsrc(h->nf);
+    for (int L = 0; L < h->nb; L++) bsrc[L] = old_pos[h->lib_body[L]];
+    std::vector<int> old_index(h->natoms, -1);
+    for (int j = 0; j < h->nf; j++) old_index[old_free[j]] = j;
+    for (int j = 0; j < h->nf; j++) fsrc[j] = old_index[h->free_atoms[j]];
+    int rc = permute_rows(h->d_ref_start.p, 0, 7, nbp, es, bsrc);
+    if (!rc) rc = permute_rows(h->d_ref_out.p, 0, 3, nbp, 4, bsrc);
+    // free-atom rows follow the body rows: offsets in units of their own row length
+    if (!rc && h->nf) {
+        unsigned char* fs = h->d_ref_start.p + 7 * nbp * es;
+        unsigned char* fo = (unsigned char*)(h->d_ref_out.p + 3 * nbp);
+        rc = permute_rows(fs, 0, 3, nfp, es, fsrc);
+        if (!rc) rc = permute_rows(fo, 0, 2, nfp, 4, fsrc);
+    }
+    return rc;
 }
 
 }  // namespace
@@ -439,6 +492,7 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
     plan_order(h);
     h->nb_pad = ((std::max(nb, 1) + 31) / 32) * 32;
     h->nba_pad = ((std::max(h->nba, 1) + 31) / 32) * 32;
+    h->nf_pad = ((std::max(h->nf, 1) + 31) / 32) * 32;
     h->I.assign((size_t)nb * 3, 0.0);
     h->dfix.assign((size_t)h->nba * 3, 0.0);
     h->invm.assign(nb, 0.0);
@@ -466,7 +520,7 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
             h->d_ke_count.alloc(1) != cudaSuccess)
             rc = fail(RBX_ERR_CUDA, "cudaMalloc kinetic-energy scratch");
         else if (cudaMemset(h->d_ke_count.p, 0, sizeof(unsigned int)) != cudaSuccess ||
-                 cudaMallocHost((void**)&h->h_ke, 2 * sizeof(double)) != cudaSuccess)
+                 cudaMallocHost((void**)&h->h_ke, 8 * sizeof(double)) != cudaSuccess)
             rc = fail(RBX_ERR_CUDA, "kinetic-energy scratch initialisation failed");
     }
     if (!rc && h->d_state.p) rc = cudaMemset(h->d_state.p, 0, sizeof(double) * 14 * h->nb_pad) == cudaSuccess ? 0 : fail(RBX_ERR_CUDA, "cudaMemset");
@@ -500,9 +554,10 @@ int rbx_set_atom_locations(rbx_integrator* h, const int* location) {
     h->max_location = *std::max_element(h->location.begin(), h->location.end());
     // Re-plan the library order for the new slots and carry the body state (and constants)
     // over to it; the raw rows are permuted, so the float-float state moves bit for bit.
-    const std::vector<int> old_pos = h->lib_pos;
+    const std::vector<int> old_pos = h->lib_pos, old_free = h->free_atoms;
     plan_order(h);
     if ((rc = upload_layout(h))) return rc;
+    if (h->refined && h->ref_phase != 0 && (rc = move_refined(h, old_pos, old_free))) return rc;
     if (!h->have_state || h->nb == 0 || old_pos == h->lib_pos) return RBX_OK;
     const size_t rows = h->prec == PREC_DOUBLE ? 14 : 28, es = h->prec == PREC_DOUBLE ? 8 : 4, nbp = h->nb_pad;
     std::vector<unsigned char> in(rows * nbp * es), out(rows * nbp * es, 0);
@@ -574,6 +629,7 @@ int rbx_upload_state(rbx_integrator* h, const double* positions, const double* v
     if ((rc = upload_bodies(h))) return rc;
     h->have_state = true;
     h->host_geom_valid = true;
+    h->ref_phase = 0;
     return RBX_OK;
 }
 
@@ -601,6 +657,7 @@ int rbx_upload_state_device(rbx_integrator* h, void* stream, const rbx_buffers* 
     h->ndof = 3 * h->nf + counts[0];
     h->have_state = true;
     h->host_geom_valid = false;
+    h->ref_phase = 0;
     h->last_launches = 1;
     return RBX_OK;
 }
@@ -643,6 +700,84 @@ int rbx_kinetic_energies(rbx_integrator* h, void* stream, const rbx_buffers* buf
     return RBX_OK;
 }
 
+int rbx_set_compute_refined_energies(rbx_integrator* h, int compute) {
+    int rc = check(h);
+    if (rc) return rc;
+    h->refined = compute != 0;
+    h->ref_phase = 0;
+    if (!h->refined || h->d_ref_start.p) return RBX_OK;
+    CUDA_TRY(cudaSetDevice(h->device));
+    const size_t es = h->prec == PREC_DOUBLE ? sizeof(double) : sizeof(float);
+    const size_t start = (7 * (size_t)h->nb_pad + 3 * (size_t)h->nf_pad) * es;
+    const size_t terms = 3 * (size_t)h->nb_pad + 2 * (size_t)h->nf_pad;
+    const int blocks = refined_blocks(h->sys());
+    if (h->d_ref_start.alloc(start) != cudaSuccess || h->d_ref_out.alloc(terms) != cudaSuccess ||
+        h->d_ref_partial.alloc((size_t)3 * blocks) != cudaSuccess || h->d_ref_res.alloc(3) != cudaSuccess ||
+        h->d_ref_count.alloc(1) != cudaSuccess) {
+        h->refined = false;
+        return fail(RBX_ERR_CUDA, "cudaMalloc of the refined-energy arrays failed");
+    }
+    CUDA_TRY(cudaMemset(h->d_ref_start.p, 0, start));
+    CUDA_TRY(cudaMemset(h->d_ref_out.p, 0, terms * sizeof(float)));
+    CUDA_TRY(cudaMemset(h->d_ref_count.p, 0, sizeof(unsigned int)));
+    return RBX_OK;
+}
+
+int rbx_get_compute_refined_energies(const rbx_integrator* h, int* out) {
+    int rc = check(h);
+    if (!rc) *out = h->refined ? 1 : 0;
+    return rc;
+}
+
+// Plain kinetic energies and, with refined energies on, the sums of the refined terms written by
+// the last part2: h_ke[0, 2) and h_ke[2, 5).
+static int refined_sums(rbx_integrator* h, void* stream, const rbx_buffers* buf) {
+    int rc = check_ready(h, buf);
+    if (rc) return rc;
+    if (h->refined && h->ref_phase != 2)
+        return fail(RBX_ERR_STATE, "refined energies need a completed step (part1 or fused, then part2 with the same "
+                                   "step size) since the last state change");
+    CUDA_TRY(cudaSetDevice(h->device));
+    DevSys s = h->sys();
+    cudaStream_t st = (cudaStream_t)stream;
+    KEScratch k{h->d_ke_partial.p, h->d_ke_count.p, h->d_ke_out.p};
+    if (launch_kinetic(h->prec, s, devbuf(buf), k, kinetic_blocks(s), stream) < 0)
+        return fail(RBX_ERR_CUDA, "kinetic-energy launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    CUDA_TRY(cudaMemcpyAsync(h->h_ke, h->d_ke_out.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    h->last_launches = 1;
+    if (h->refined) {
+        RefScratch r{h->d_ref_partial.p, h->d_ref_count.p, h->d_ref_res.p};
+        if (launch_refined_sum(s, r, refined_blocks(s), stream) < 0)
+            return fail(RBX_ERR_CUDA, "refined-energy sum failed: %s", cudaGetErrorString(cudaGetLastError()));
+        CUDA_TRY(cudaMemcpyAsync(h->h_ke + 2, h->d_ref_res.p, 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+        h->last_launches = 2;
+    }
+    CUDA_TRY(cudaStreamSynchronize(st));
+    return RBX_OK;
+}
+
+int rbx_refined_kinetic_energies(rbx_integrator* h, void* stream, const rbx_buffers* buf, double* out2) {
+    if (!out2) return fail(RBX_ERR_INVALID_ARGUMENT, "null output");
+    int rc = refined_sums(h, stream, buf);
+    if (rc) return rc;
+    out2[0] = h->h_ke[0] + (h->refined ? h->h_ke[2] : 0.0);
+    out2[1] = h->h_ke[1] + (h->refined ? h->h_ke[3] : 0.0);
+    return RBX_OK;
+}
+
+int rbx_potential_energy_refinement(rbx_integrator* h, void* stream, const rbx_buffers* buf, double* out1) {
+    if (!out1) return fail(RBX_ERR_INVALID_ARGUMENT, "null output");
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->refined) {
+        *out1 = 0.0;
+        return RBX_OK;
+    }
+    if ((rc = refined_sums(h, stream, buf))) return rc;
+    *out1 = -h->h_ke[4] * h->ref_dt * h->ref_dt / 24.0;
+    return RBX_OK;
+}
+
 int rbx_get_body_state(rbx_integrator* h, double* state) {
     int rc = check(h);
     if (rc) return rc;
@@ -663,6 +798,7 @@ int rbx_set_body_state(rbx_integrator* h, const double* state) {
     for (int b = 0; b < h->nb; b++)
         for (int k = 0; k < 14; k++) s[h->lib_pos[b] + (size_t)k * h->nb_pad] = state[14 * (size_t)b + k];
     CUDA_TRY(cudaSetDevice(h->device));
+    h->ref_phase = 0;
     return put_state(h, s);
 }
 
@@ -774,6 +910,7 @@ int rbx_context_load(rbx_integrator* h, void* stream, const double* positions, c
     if (launch_load_positions(h->prec, h->c_x.p, h->c_v.p, h->c_m.p, h->c_loc.p, h->natoms, devbuf(&b), stream) < 0)
         return fail(RBX_ERR_CUDA, "position upload kernel failed");
     CUDA_TRY(cudaStreamSynchronize(st));
+    h->ref_phase = 0;
     return RBX_OK;
 }
 

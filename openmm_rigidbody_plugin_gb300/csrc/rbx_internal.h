@@ -14,6 +14,13 @@
 //   atom_loc     int [nba]: device slot of each body atom (library order)
 //   free_loc     int [nf]:  device slot of each free atom
 //   tile_body0   int [n_body_tiles+1]: bodies of tile t are [tile_body0[t], tile_body0[t+1])
+//   ref_start    refined energies only: the stencil sums that part1 and fused steps start and
+//                part2 completes. Bodies: 7 rows of nb_pad (F h/m, then the quaternion stencil
+//                0.5 [q(t-h) - q(t)] + 2.5 [q(t+h) - q(t)]); then free atoms: 3 rows of nf_pad
+//                (F h/m). float (single, mixed) or double (double precision).
+//   ref_out      refined energies only, float, written by part2. Bodies: 3 rows of nb_pad (KE_t
+//                correction, KE_r correction, |F|^2/m + tau.I^-1.tau); then free atoms: 2 rows of
+//                nf_pad (KE_t correction, |F|^2/m).
 #pragma once
 
 #include <vector_types.h>
@@ -44,7 +51,7 @@ inline int tile_bodies(int prec) { return prec == PREC_DOUBLE ? kTileBodies : kT
 inline int free_per_tile(int prec) { return prec == PREC_DOUBLE ? kThreads : kThreadsF; }
 
 struct DevSys {
-    int nb, nf, nba, nb_pad, nba_pad;
+    int nb, nf, nba, nb_pad, nba_pad, nf_pad;
     int n_body_tiles, n_free_tiles;
     int rot_n;  // NO-SQUISH substeps; 0 = exact rotation
     void* state;           // double* (double precision) or float* (float-float, single/mixed)
@@ -57,6 +64,8 @@ struct DevSys {
     const int* atom_loc;
     const int* free_loc;
     const int* tile_body0;
+    void* ref_start;  // null unless refined energies are on (then the step kernels fill it)
+    float* ref_out;
 };
 
 struct DevBuf {
@@ -111,7 +120,18 @@ struct KEScratch {
 };
 
 // Launchers (rbx_kernels.cu). Return the number of kernels enqueued, or -1 on a launch error.
+// launch_step runs the refined-energy variants of the step kernels when s.ref_start is set.
 int launch_step(int prec, int kind, const DevSys& s, const DevBuf& b, double dt, void* stream);
+// rbx_refined.cu: the refined-energy step kernels and the fixed-order FP64 sum of ref_out into
+// out[3] = [sum of KE_t corrections, sum of KE_r corrections, sum of |F|^2/m + tau.I^-1.tau].
+int launch_step_refined(int prec, int kind, const DevSys& s, const DevBuf& b, double dt, void* stream);
+struct RefScratch {
+    double* partial;      // 3 * n_blocks
+    unsigned int* count;  // 1
+    double* out;          // 3
+};
+int refined_blocks(const DevSys& s);
+int launch_refined_sum(const DevSys& s, const RefScratch& k, int n_blocks, void* stream);
 int launch_kinetic(int prec, const DevSys& s, const DevBuf& b, const KEScratch& k, int n_blocks, void* stream);
 int launch_forces_from_host(int prec, const double* f_dev_user, const int* location, int natoms, long long* force,
                             int stride, void* stream);

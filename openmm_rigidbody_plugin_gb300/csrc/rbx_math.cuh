@@ -33,6 +33,7 @@ template <class T> RBX_HD V3<T> operator-(V3<T> a, V3<T> b) { return v3<T>(a.x -
 template <class T> RBX_HD V3<T> operator*(V3<T> a, T s) { return v3<T>(a.x * s, a.y * s, a.z * s); }
 template <class T> RBX_HD V3<T> mul(V3<T> a, V3<T> b) { return v3<T>(a.x * b.x, a.y * b.y, a.z * b.z); }
 template <class T> RBX_HD Q4<T> operator+(Q4<T> a, Q4<T> b) { return q4<T>(a.w + b.w, a.x + b.x, a.y + b.y, a.z + b.z); }
+template <class T> RBX_HD Q4<T> operator-(Q4<T> a, Q4<T> b) { return q4<T>(a.w - b.w, a.x - b.x, a.y - b.y, a.z - b.z); }
 template <class T> RBX_HD Q4<T> operator*(Q4<T> a, T s) { return q4<T>(a.w * s, a.x * s, a.y * s, a.z * s); }
 
 template <class T> RBX_HD Q4<T> qB(Q4<T> q, V3<T> x) {

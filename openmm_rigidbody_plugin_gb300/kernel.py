@@ -187,6 +187,37 @@ class IntegratorKernel:
         _lib.check(self._lib.rbx_kinetic_energies(self._h, _stream_handle(stream), ctypes.byref(b), _dptr(out)))
         return out
 
+    # refined ("shadow") energies --------------------------------------------------------------
+    def set_compute_refined_energies(self, compute):
+        _lib.check(self._lib.rbx_set_compute_refined_energies(self._h, int(bool(compute))))
+
+    @property
+    def compute_refined_energies(self):
+        out = ctypes.c_int(0)
+        _lib.check(self._lib.rbx_get_compute_refined_energies(self._h, ctypes.byref(out)))
+        return bool(out.value)
+
+    def refined_kinetic_energies(self, buffers, stream=None):
+        """[KE_t, KE_r] refined (the plain kinetic energies while refined energies are off)."""
+        out = np.zeros(2)
+        b = buffers.struct() if hasattr(buffers, "struct") else buffers
+        _lib.check(self._lib.rbx_refined_kinetic_energies(self._h, _stream_handle(stream), ctypes.byref(b),
+                                                          _dptr(out)))
+        return out
+
+    def potential_energy_refinement(self, buffers, stream=None):
+        out = np.zeros(1)
+        b = buffers.struct() if hasattr(buffers, "struct") else buffers
+        _lib.check(self._lib.rbx_potential_energy_refinement(self._h, _stream_handle(stream), ctypes.byref(b),
+                                                             _dptr(out)))
+        return float(out[0])
+
+    def context_refined_kinetic_energies(self, stream=None):
+        return self.refined_kinetic_energies(self.context_buffers(), stream)
+
+    def context_potential_energy_refinement(self, stream=None):
+        return self.potential_energy_refinement(self.context_buffers(), stream)
+
     @property
     def last_launch_count(self):
         return self._lib.rbx_last_launch_count(self._h)

@@ -53,6 +53,8 @@ def lib():
         L.orc_part1.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp]
         L.orc_part2.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp]
         L.orc_kinetic.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.orc_set_refined.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_refined.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, _dp]
         for f in ("orc_num_dof", "orc_num_bodies", "orc_num_free", "orc_num_body_atoms"):
             getattr(L, f).argtypes = [ctypes.c_void_p]
         L.orc_atom_index.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -162,6 +164,16 @@ class Oracle(_Base):
     def kinetic(self):
         out = np.zeros(2)
         lib().orc_kinetic(self.h, _d(self.V), _d(out))
+        return out
+
+    def set_refined(self, mode=1):
+        """Refined energies on (1), off (0), or on with the reference's free-atom weights (2)."""
+        lib().orc_set_refined(self.h, int(mode))
+
+    def refined(self, dt, F):
+        """[KE_t, KE_r, U_refinement] after a part2 whose force array was F."""
+        out = np.zeros(3)
+        lib().orc_refined(self.h, _d(self.V), _d(self._f(F)), float(dt), _d(out))
         return out
 
     @property

@@ -618,6 +618,9 @@ struct orc_system {
     double *mass, *invm, *I, *invI, *rcm, *pcm, *q, *pi, *force, *torque, *twoKt, *twoKr;
     double* d;     /* [3*nbodyatoms] body-frame positions */
     double* delta; /* [3*nbodyatoms] space-frame displacements from the COM */
+    /* refined energies: 0 off, 1 on, 2 on with the reference's free-atom weights */
+    int refined;
+    double *rdot, *qdot, *posdot; /* [3*nbodies], [4*nbodies], [3*nfree] stencil sums */
 };
 
 static void* xcalloc(size_t n, size_t sz) {
@@ -633,6 +636,7 @@ void orc_destroy(orc_system* s) {
     free(s->mass); free(s->invm); free(s->I); free(s->invI); free(s->rcm); free(s->pcm);
     free(s->q); free(s->pi); free(s->force); free(s->torque); free(s->twoKt); free(s->twoKr);
     free(s->d); free(s->delta);
+    free(s->rdot); free(s->qdot); free(s->posdot);
     free(s);
 }
 
@@ -686,6 +690,9 @@ orc_system* orc_create(int natoms, const double* masses, const int* body_indices
 #undef ALLOC
     s->d = xcalloc(3 * (size_t)loc, sizeof(double));
     s->delta = xcalloc(3 * (size_t)loc, sizeof(double));
+    s->rdot = xcalloc(3 * (size_t)(nb ? nb : 1), sizeof(double));
+    s->qdot = xcalloc(4 * (size_t)(nb ? nb : 1), sizeof(double));
+    s->posdot = xcalloc(3 * (size_t)(nfree ? nfree : 1), sizeof(double));
     free(count); free(newid); free(bid);
     return s;
 fail:
@@ -871,11 +878,45 @@ static void update_velocities(orc_system* s, int b, double* V) {
     s->twoKr[b] = dot3(L, w);
 }
 
+/* Rotation of body b by `dt` from its current q with momentum pi + torque * kick, on copies: the
+ * virtualRotation of platforms/cuda/src/kernels/rigidbodyintegrator.cu:238-243. */
+static void virtual_rotation(const orc_system* s, int b, double kick, double dt, double* qv) {
+    double pv[4];
+    for (int x = 0; x < 4; x++) { qv[x] = s->q[4 * b + x]; pv[x] = s->pi[4 * b + x] + s->torque[4 * b + x] * kick; }
+    if (s->mode == 0) orc_exact_rotation(s->I + 3 * b, s->invI + 3 * b, qv, pv, dt, s->robust);
+    else orc_nosquish_rotation(s->invI + 3 * b, s->bdof[b], qv, pv, dt, s->mode);
+}
+
 static void part1_range(orc_system* s, double dt, const double* F, double* V, double* R, int f0, int f1, int b0,
                         int b1) {
     double halfDt = 0.5 * dt;
+    if (s->refined) {
+        /* Start of the refined-energy stencils at time t, before the kicks. Free atoms: freeAtomsDelta
+         * with -dt and freeAtomsDot with factor -1 (CudaRigidBodyKernels.cpp:406-415,
+         * rigidbodyintegrator.cu:285-292): the reference stores -(-dt)(v - F/m dt/2) = +dt v(t-dt/2);
+         * the stencil that matches the bodies' one (and gives KE for uniform motion) needs -dt v(t-dt/2)
+         * (refined == 1). Bodies: rigidbodyintegrator.cu:318-321. */
+        const double sgn = s->refined == 2 ? 1.0 : -1.0;
+        for (int a = f0; a < f1; a++) {
+            int i = s->atom_index[a];
+            for (int x = 0; x < 3; x++)
+                s->posdot[3 * a + x] = sgn * dt * (V[3 * i + x] - F[3 * i + x] * s->free_invm[a] * halfDt);
+        }
+        for (int b = b0; b < b1; b++) {
+            double qv[4];
+            for (int x = 0; x < 3; x++) {
+                double v = s->pcm[3 * b + x] * s->invm[b], dv = s->force[3 * b + x] * s->invm[b] * halfDt;
+                s->rdot[3 * b + x] = s->rcm[3 * b + x] * 2.5 + (v - dv) * halfDt;
+            }
+            virtual_rotation(s, b, -dt, -dt, qv);
+            for (int x = 0; x < 4; x++) s->qdot[4 * b + x] = qv[x] * 0.5 - s->q[4 * b + x] * 3.0;
+        }
+    }
     for (int a = f0; a < f1; a++) {
         int i = s->atom_index[a];
+        if (s->refined)
+            for (int x = 0; x < 3; x++)
+                s->posdot[3 * a + x] += 5.0 * dt * (V[3 * i + x] + F[3 * i + x] * s->free_invm[a] * halfDt);
         for (int x = 0; x < 3; x++) {
             V[3 * i + x] += F[3 * i + x] * s->free_invm[a] * halfDt;
             R[3 * i + x] += V[3 * i + x] * dt;
@@ -911,6 +952,26 @@ static void part2_range(orc_system* s, double dt, const double* R, const double*
         for (int x = 0; x < 4; x++) s->pi[4 * b + x] += s->torque[4 * b + x] * dt;
         update_velocities(s, b, V);
     }
+    if (!s->refined) return;
+    /* End of the stencils at time t+dt, after the kicks. Free atoms: freeAtomsDot with factor 5 on
+     * the part1 displacement (added in part1 above) and with factor 2 on dt v(t+3dt/2)
+     * (CudaRigidBodyKernels.cpp:428-438). Bodies: rigidbodyintegrator.cu:380-384. */
+    for (int a = f0; a < f1; a++) {
+        int i = s->atom_index[a];
+        for (int x = 0; x < 3; x++)
+            s->posdot[3 * a + x] += 2.0 * dt * (V[3 * i + x] + F[3 * i + x] * s->free_invm[a] * halfDt);
+    }
+    for (int b = b0; b < b1; b++) {
+        double qv[4], qq = 0.0;
+        for (int x = 0; x < 3; x++) {
+            double v = s->pcm[3 * b + x] * s->invm[b], dv = s->force[3 * b + x] * s->invm[b] * halfDt;
+            s->rdot[3 * b + x] = s->rcm[3 * b + x] * 2.5 + (v + dv) * dt - s->rdot[3 * b + x];
+        }
+        virtual_rotation(s, b, dt, dt, qv);
+        for (int x = 0; x < 4; x++) s->qdot[4 * b + x] += s->q[4 * b + x] * 1.5 + qv[x];
+        for (int x = 0; x < 4; x++) qq += s->qdot[4 * b + x] * s->q[4 * b + x];
+        for (int x = 0; x < 4; x++) s->qdot[4 * b + x] -= s->q[4 * b + x] * qq;
+    }
 }
 
 /* integratePart1 (RigidBodySystem.cpp:170-187) */
@@ -933,6 +994,34 @@ void orc_kinetic(orc_system* s, const double* V, double* out) {
     for (int b = 0; b < s->nbodies; b++) { kt += s->twoKt[b]; kr += s->twoKr[b]; }
     out[0] = 0.5 * kt;
     out[1] = 0.5 * kr;
+}
+
+void orc_set_refined(orc_system* s, int mode) { s->refined = mode; }
+
+/* Refined kinetic energies and potential-energy refinement after a part2 (the refinedKineticEnergies
+ * and potentialEnergyRefinement kernels, rigidbodyintegrator.cu:433-469, summed and scaled as in
+ * CudaRigidBodyKernels.cpp:118-194 and :481-494): out = [KE_t, KE_r, U_refinement]. F is the force
+ * array of the last part2. */
+void orc_refined(orc_system* s, const double* V, const double* F, double dt, double* out) {
+    double kt = 0.0, kr = 0.0, u = 0.0;
+    for (int a = 0; a < s->nfree; a++) {
+        int i = s->atom_index[a];
+        kt += dot3(s->posdot + 3 * a, V + 3 * i) * (0.5 / s->free_invm[a]);
+        u += dot3(F + 3 * i, F + 3 * i) * s->free_invm[a];
+    }
+    for (int b = 0; b < s->nbodies; b++) {
+        double v[3], tb[3];
+        for (int x = 0; x < 3; x++) v[x] = s->pcm[3 * b + x] * s->invm[b];
+        kt += dot3(s->rdot + 3 * b, v) / s->invm[b];
+        kr += dot4(s->qdot + 4 * b, s->pi + 4 * b);
+        qBt(s->q + 4 * b, s->torque + 4 * b, tb);
+        u += dot3(s->force + 3 * b, s->force + 3 * b) * s->invm[b];
+        for (int x = 0; x < 3; x++) u += tb[x] * s->invI[3 * b + x] * tb[x];
+    }
+    double factor = 1.0 / (6.0 * dt);
+    out[0] = kt * factor;
+    out[1] = kr * factor;
+    out[2] = -u * dt * dt / 24.0;
 }
 
 int orc_num_dof(const orc_system* s) { return s->ndof; }

@@ -12,7 +12,7 @@
  *   robust = 1  the project's robust FP64 oracle: cyclic-Jacobi eigensolver, |component|
  *               orthonormal(), pcm reset, singleton bodies become free atoms, and closed-form free
  *               rotation for spherical, symmetric and linear tops, where the reference divides
- *               by zero (reference defects D1-D5 described in the design doc).
+ *               by zero (reference defects D1-D5).
  */
 #ifndef RBX_ORACLE_H
 #define RBX_ORACLE_H
@@ -44,6 +44,15 @@ void orc_part2(orc_system* s, double dt, const double* R, const double* F, doubl
 
 /* RigidBodySystem::computeKineticEnergies (RigidBodySystem.cpp:210-220): out[0]=KE_t, out[1]=KE_r */
 void orc_kinetic(orc_system* s, const double* V, double* out);
+
+/* Refined ("shadow") energies, the reference's COMPMOD path (RigidBodyIntegrator::
+ * setComputeRefinedEnergies, openmmapi/src/RigidBodyIntegrator.cpp:34-38; kernels in
+ * platforms/cuda/src/kernels/rigidbodyintegrator.cu:238-243, :285-292, :318-321, :380-384,
+ * :433-469). mode 0 = off, 1 = on, 2 = on with the reference's free-atom weights (which give
+ * 4/3 of the kinetic energy for uniform motion). While on, part1/part2 accumulate the stencils;
+ * orc_refined gives [KE_t, KE_r, U_refinement] after a part2, F = that part2's force array. */
+void orc_set_refined(orc_system* s, int mode);
+void orc_refined(orc_system* s, const double* V, const double* F, double dt, double* out);
 
 int orc_num_dof(const orc_system* s);
 int orc_num_bodies(const orc_system* s);

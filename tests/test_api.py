@@ -36,8 +36,12 @@ def test_integrator_parameter_errors():
         intg.setRotationMode(-1)
     with pytest.raises(api.OpenMMException, match="not bound"):
         intg.step(1)
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(api.OpenMMException, match="not bound"):
         intg.getRefinedKineticEnergies()
+    with pytest.raises(api.OpenMMException, match="not bound"):
+        intg.getPotentialEnergyRefinement()
+    intg.setComputeRefinedEnergies(True)
+    assert intg.getComputeRefinedEnergies()
 
 
 def _waters_and_ligand():
@@ -101,6 +105,12 @@ class _FakeIntegrator:
     def getKineticEnergies(self):
         return [30.0, 12.0]
 
+    def getRefinedKineticEnergies(self):
+        return [31.0, 11.5]
+
+    def getPotentialEnergyRefinement(self):
+        return -0.25
+
 
 class _FakeContext:
     def __init__(self, dof, cmm):
@@ -125,5 +135,20 @@ def test_state_data_reporter_columns_and_temperature(cmm):
     v = [float(x) for x in line.split(",")]
     dof = 60 - (3 if cmm else 0)
     np.testing.assert_allclose(v, [10, -5.0, 42.0, 37.0, 2 * 42.0 / (dof * api.KB), 30.0, 12.0])
-    with pytest.raises(NotImplementedError):
-        api.StateDataReporter(out, 10, refinedTemperature=True)
+
+
+def test_state_data_reporter_refined_columns():
+    """Refined columns in the reference's order (python/statedatareporter.py:30-48): potential plus
+    refinement, refined kinetic, their total, refined temperature, refined translational/rotational."""
+    out = io.StringIO()
+    rep = api.StateDataReporter(out, 10, step=False, potentialEnergy=False, kineticEnergy=False, totalEnergy=False,
+                                temperature=False, refinedPotentialEnergy=True, refinedKineticEnergy=True,
+                                refinedTotalEnergy=True, refinedTemperature=True, refinedTranslationalEnergy=True,
+                                refinedRotationalEnergy=True)
+    rep.report(_FakeContext(60, True), 10)
+    header, line = out.getvalue().splitlines()
+    assert header.split(",") == ["Refined Potential Energy (kJ/mole)", "Refined Kinetic Energy (kJ/mole)",
+                                 "Refined Total Energy (kJ/mole)", "Refined Temperature (K)",
+                                 "Refined Translational Energy (kJ/mole)", "Refined Rotational Energy (kJ/mole)"]
+    v = [float(x) for x in line.split(",")]
+    np.testing.assert_allclose(v, [-5.25, 42.5, 37.25, 2 * 42.5 / (57 * api.KB), 31.0, 11.5])
