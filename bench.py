@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--bodies", type=int, default=1_000_000)
     p.add_argument("--free", type=int, default=100_000)
     p.add_argument("--e2e-steps", type=int, default=30)
+    p.add_argument("--refined", action="store_true",
+                   help="single: refined (shadow) energies on; each fused step also writes the stencil sums")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--reference-seconds", type=float, default=90.0,
                    help="bound on the timed CPU work of --impl reference")
@@ -298,6 +300,8 @@ def run_gpu(args, world, rank, local):
     buf.set_velocities(s.velocities, s.masses)
     buf.set_forces(F)
     k.upload_state(s.positions, s.velocities)
+    if args.refined:
+        k.set_compute_refined_energies(True)
     nb, nf = k.num_bodies, k.num_free
     nba = int(s.num_atoms) - nf
     stream = torch.cuda.current_stream()
@@ -326,12 +330,19 @@ def run_gpu(args, world, rank, local):
     ke = k.kinetic_energies(buf, stream)
     if not np.all(np.isfinite(ke)):
         raise RuntimeError(f"non-finite kinetic energy after the timed steps: {ke}")
+    refined = None
+    if args.refined:
+        refined = {"kinetic": [float(e) for e in k.refined_kinetic_energies(buf, stream)],
+                   "potential_refinement": k.potential_energy_refinement(buf, stream)}
     value = world * nb * args.steps / t_dev
     bytes_step = BYTES_PER_BODY[args.precision] * nb + BYTES_PER_BODY_ATOM[args.precision] * nba + BYTES_PER_FREE * nf
+    if args.refined:  # stencil sums written by every fused step: 7 values per body, 3 per free atom
+        es = 8 if args.precision == "double" else 4
+        bytes_step += 7 * es * nb + 3 * es * nf
     per_launch = t_dev / args.steps
     peak, peak_kind = peaks()
     achieved = bytes_step / per_launch / 1e9
-    traffic = ncu_traffic(args.mode, args.precision, nb)
+    traffic = None if args.refined else ncu_traffic(args.mode, args.precision, nb)  # captured for the plain kernel
 
     # e2e through the host-buffer C ABI (pinned host arrays, copies inside the timed region):
     # every step uploads its forces and downloads its positions and velocities; consecutive
@@ -367,7 +378,8 @@ def run_gpu(args, world, rank, local):
            "scaling": "weak", "vs_baseline": None,
            "dtype": {"mixed": "f32 atoms + f64 body state", "double": "f64", "single": "f32"}[args.precision],
            "data": "synthetic",
-           "config": {"workload": WORKLOAD + f"; rotation mode {args.mode}; {args.precision} precision",
+           "config": {"workload": WORKLOAD + f"; rotation mode {args.mode}; {args.precision} precision"
+                                  + ("; refined energies on" if args.refined else ""),
                       "bodies_per_gpu": nb, "body_atoms_per_gpu": nba, "free_atoms_per_gpu": nf,
                       "l2": "working set > 129 MB L2 (no flush needed)", "parallelism": f"{world} independent replicas"},
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -375,6 +387,8 @@ def run_gpu(args, world, rank, local):
                         "kernel": "rbx::step_kernel (fused)"},
            "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(), "gpu_launches": launches,
            "kinetic_energy_after": [float(ke[0]), float(ke[1])]}
+    if refined is not None:
+        out["refined_after"] = refined
     print(json.dumps(out), flush=True)
 
 

@@ -1,5 +1,6 @@
-// rbx_internal.h -- device-side system description shared by the host code (rbx_host.cpp) and
-// the CUDA kernels (rbx_kernels.cu).
+// rbx_internal.h -- device-side system description shared by the host code (rbx_host.cpp,
+// rbx_batch.cpp) and the CUDA kernels (rbx_step.cuh, rbx_kernels.cu, rbx_refined.cu, rbx_forces.cu,
+// rbx_setup.cu).
 //
 // HBM layout (one integrator):
 //   body state   14 components r.xyz, v.xyz, q.wxyz, pi.wxyz per body (112 B/body):
