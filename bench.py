@@ -286,6 +286,37 @@ def run_reference(args, world, rank):
     print(json.dumps(out), flush=True)
 
 
+def time_replan(k, buf, s, repeats=3):
+    """Wall time of rbx_set_atom_locations after OpenMM-style reorderings (whole molecules moved to
+    new slots, the buffers moved first as OpenMM moves them), best of `repeats`; the first call,
+    which allocates the re-plan scratch, is not counted."""
+    import torch
+    rng = np.random.default_rng(11)
+    bidx = np.asarray(s.body_indices)
+    times, moves = [], []
+    for r in range(repeats + 1):
+        key = rng.random(int(bidx.max()) + 1)[np.maximum(bidx, 0)]
+        free = bidx <= 0
+        key[free] = rng.random(int(free.sum()))
+        slot_to_atom = np.argsort(key, kind="stable")
+        loc = np.empty(len(slot_to_atom), dtype=np.int64)
+        loc[slot_to_atom] = np.arange(len(slot_to_atom))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        buf.relocate(loc)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        k.set_atom_locations(loc)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        if r:
+            moves.append(t1 - t0)
+            times.append(t2 - t1)
+    return {"set_atom_locations_ms": 1e3 * min(times), "buffer_moves_ms": 1e3 * min(moves),
+            "what": "molecules shuffled to new slots; buffer moves = the posq/correction/velm/force gathers "
+                    "OpenMM itself does (torch indexing here)"}
+
+
 def run_gpu(args, world, rank, local):
     import torch
     from openmm_rigidbody_plugin_gb300 import build, kernel
@@ -334,6 +365,7 @@ def run_gpu(args, world, rank, local):
     if args.refined:
         refined = {"kinetic": [float(e) for e in k.refined_kinetic_energies(buf, stream)],
                    "potential_refinement": k.potential_energy_refinement(buf, stream)}
+    replan = time_replan(k, buf, s) if not args.refined else None
     value = world * nb * args.steps / t_dev
     bytes_step = BYTES_PER_BODY[args.precision] * nb + BYTES_PER_BODY_ATOM[args.precision] * nba + BYTES_PER_FREE * nf
     if args.refined:  # stencil sums written by every fused step: 7 values per body, 3 per free atom
@@ -389,6 +421,8 @@ def run_gpu(args, world, rank, local):
            "kinetic_energy_after": [float(ke[0]), float(ke[1])]}
     if refined is not None:
         out["refined_after"] = refined
+    if replan is not None:
+        out["replan"] = replan
     print(json.dumps(out), flush=True)
 
 

@@ -15,7 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "librbx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["rbx_refined.cu", "rbx_kernels.cu", "rbx_forces.cu", "rbx_setup.cu", "rbx_host.cpp", "rbx_batch.cpp"]
+SOURCES = ["rbx_refined.cu", "rbx_kernels.cu", "rbx_forces.cu", "rbx_setup.cu", "rbx_plan.cu", "rbx_host.cpp",
+           "rbx_batch.cpp"]
 
 
 def nvcc():

@@ -356,7 +356,7 @@ int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, con
     if ((rc = rbx_context_sync_bodies(b->integ, stream))) return rc;
     if ((rc = sync_host_dof(b->integ))) return rc;
     std::vector<int> body0, free0;
-    system_ranges(b->integ, b->offsets, body0, free0, b->dof);
+    if ((rc = system_ranges(b->integ, b->offsets, body0, free0, b->dof))) return rc;
     if ((rc = upload_vec(b->d_body0, body0)) || (rc = upload_vec(b->d_free0, free0))) return rc;
     b->forces_valid = false;
     return RBX_OK;

@@ -19,6 +19,10 @@ template <class T> struct DevArray {
         p = nullptr;
         n = 0;
     }
+    void swap(DevArray& o) {
+        T* tp = p; p = o.p; o.p = tp;
+        size_t tn = n; n = o.n; o.n = tn;
+    }
     // The allocation is rounded up to a multiple of 256 bytes, so that any element range widened
     // to 16-byte boundaries stays inside it.
     cudaError_t alloc(size_t count) {

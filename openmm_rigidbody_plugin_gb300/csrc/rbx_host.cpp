@@ -14,6 +14,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/rbx.h"
@@ -81,6 +82,15 @@ struct rbx_integrator {
     std::vector<int> body_first;        // [nb+1] first body atom (library order)
     std::vector<int> body_atoms;        // [nba] user index of each body atom (library order)
     std::vector<int> tile_body0;        // [n_body_tiles+1]
+    // After a re-plan on the device only lib_body and tile_body0 are current on the host; location,
+    // free_atoms, lib_pos, body_first and body_atoms are rebuilt on demand (ensure_host_plan).
+    bool host_plan_valid = true;
+    // device copies of the plan: reference-order body atoms (fixed) and the current inverse maps
+    DevArray<int> d_ref_first, d_ref_atoms, d_lib_pos, d_free_atoms, d_free_index;
+    // scratch of the device re-plan (allocated at its first use)
+    DevArray<int> r_loc, r_marks, r_scan, r_aux, r_status, r_lib_body, r_free, r_idx;
+    DevArray<unsigned int> r_seen;
+    int r_nslots = 0;
 
     DevArray<double> d_state, d_invm, d_invI;  // d_state holds FP64 rows or float-float rows
     DevArray<float> d_bconst;                   // single/mixed: 11 rows (see kBconstRows)
@@ -141,6 +151,30 @@ struct rbx_integrator {
 
 rbx::DevSys rbx::device_system(const rbx_integrator* h) { return h->sys(); }
 
+namespace {
+// Host copies of the plan after a re-plan on the device: slots and free-atom order from the device,
+// the body order's inverse and atom lists rebuilt from lib_body.
+int ensure_host_plan(rbx_integrator* h) {
+    if (h->host_plan_valid) return RBX_OK;
+    CUDA_TRY(cudaSetDevice(h->device));
+    CUDA_TRY(cudaMemcpy(h->location.data(), h->c_loc.p, sizeof(int) * (size_t)h->natoms, cudaMemcpyDeviceToHost));
+    if (h->nf)
+        CUDA_TRY(cudaMemcpy(h->free_atoms.data(), h->d_free_atoms.p, sizeof(int) * (size_t)h->nf, cudaMemcpyDeviceToHost));
+    h->lib_pos.resize(h->nb);
+    h->body_first.assign(1, 0);
+    h->body_atoms.clear();
+    h->body_atoms.reserve(h->nba);
+    for (int L = 0; L < h->nb; L++) {
+        const int b = h->lib_body[L];
+        h->lib_pos[b] = L;
+        for (int a = h->ref_first[b]; a < h->ref_first[b + 1]; a++) h->body_atoms.push_back(h->ref_atoms[a]);
+        h->body_first.push_back((int)h->body_atoms.size());
+    }
+    h->host_plan_valid = true;
+    return RBX_OK;
+}
+}  // namespace
+
 int rbx::sync_host_dof(rbx_integrator* h) {
     if (h->host_geom_valid || !h->have_state || h->nb == 0) return RBX_OK;
     std::vector<int> dof(h->nb);
@@ -151,6 +185,7 @@ int rbx::sync_host_dof(rbx_integrator* h) {
 
 int rbx::ensure_host_geometry(rbx_integrator* h) {
     if (h->host_geom_valid || !h->have_state) return RBX_OK;
+    if (int rc = ensure_host_plan(h)) return rc;
     const int nb = h->nb, nbp = h->nb_pad, nbap = h->nba_pad;
     std::vector<double> I((size_t)3 * nbp);
     std::vector<int> dof(std::max(nb, 1));
@@ -191,8 +226,9 @@ int rbx::ensure_host_geometry(rbx_integrator* h) {
     return RBX_OK;
 }
 
-void rbx::system_ranges(const rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
+int rbx::system_ranges(rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
                         std::vector<int>& free0, std::vector<int>& dof) {
+    if (int rc = ensure_host_plan(h)) return rc;
     const int S = (int)slot_offsets.size() - 1;
     body0.assign(S + 1, h->nb);
     free0.assign(S + 1, h->nf);
@@ -215,6 +251,7 @@ void rbx::system_ranges(const rbx_integrator* h, const std::vector<int>& slot_of
     }
     for (int t = s + 1; t <= S; t++) free0[t] = h->nf;
     free0[0] = 0;
+    return RBX_OK;
 }
 
 namespace {
@@ -254,6 +291,26 @@ template <class T> int upload(DevArray<T>& a, const std::vector<T>& h) {
 // neighbouring slots of the force, position and velocity buffers. A tile is a run of
 // consecutive bodies under the per-CTA body and atom limits (rbx_create has rejected any body
 // larger than one tile).
+// Greedy packing of the library order into tiles of at most TB bodies and TA body atoms.
+void pack_tiles(rbx_integrator* h) {
+    const int TA = tile_atoms(h->prec), TB = tile_bodies(h->prec), nb = h->nb;
+    h->tile_body0.assign(1, 0);
+    for (int L = 0; L < nb;) {
+        int atoms = 0, cnt = 0;
+        while (L < nb && cnt < TB) {
+            const int b = h->lib_body[L];
+            const int n = h->ref_first[b + 1] - h->ref_first[b];
+            if (atoms + n > TA) break;
+            atoms += n;
+            cnt++;
+            L++;
+        }
+        h->tile_body0.push_back(L);
+    }
+    h->n_body_tiles = (int)h->tile_body0.size() - 1;
+    h->n_free_tiles = (h->nf + free_per_tile(h->prec) - 1) / free_per_tile(h->prec);
+}
+
 void plan_order(rbx_integrator* h) {
     const int nb = h->nb;
     std::vector<int> key(nb);
@@ -276,23 +333,13 @@ void plan_order(rbx_integrator* h) {
     }
     std::stable_sort(h->free_atoms.begin(), h->free_atoms.end(),
                      [&](int a, int b) { return h->location[a] < h->location[b]; });
-    const int TA = tile_atoms(h->prec), TB = tile_bodies(h->prec);
-    h->tile_body0.assign(1, 0);
-    for (int b = 0; b < nb;) {
-        int atoms = 0, cnt = 0;
-        while (b < nb && cnt < TB && atoms + (h->body_first[b + 1] - h->body_first[b]) <= TA) {
-            atoms += h->body_first[b + 1] - h->body_first[b];
-            cnt++;
-            b++;
-        }
-        h->tile_body0.push_back(b);
-    }
-    h->n_body_tiles = (int)h->tile_body0.size() - 1;
-    h->n_free_tiles = (h->nf + free_per_tile(h->prec) - 1) / free_per_tile(h->prec);
+    pack_tiles(h);
 }
 
-// Device copies of the library order: first atom of each body, tiles and device slots.
+// Device copies of the library order: first atom of each body, tiles and device slots, and the
+// maps a re-plan on the device starts from.
 int upload_layout(rbx_integrator* h) {
+    if (int rc = ensure_host_plan(h)) return rc;
     std::vector<int> atom_loc(h->nba), free_loc(h->nf);
     for (int k = 0; k < h->nba; k++) atom_loc[k] = h->location[h->body_atoms[k]];
     for (int j = 0; j < h->nf; j++) free_loc[j] = h->location[h->free_atoms[j]];
@@ -304,6 +351,13 @@ int upload_layout(rbx_integrator* h) {
     if (!rc) rc = upload(h->d_atom_loc, atom_loc);
     if (!rc) rc = upload(h->d_free_loc, free_loc);
     if (!rc) rc = upload(h->c_loc, h->location);
+    if (!rc) rc = upload(h->d_ref_first, h->ref_first);
+    if (!rc) rc = upload(h->d_ref_atoms, h->ref_atoms);
+    if (!rc) rc = upload(h->d_lib_pos, h->lib_pos);
+    if (!rc) rc = upload(h->d_free_atoms, h->free_atoms);
+    std::vector<int> free_index(h->natoms, -1);
+    for (int j = 0; j < h->nf; j++) free_index[h->free_atoms[j]] = j;
+    if (!rc) rc = upload(h->d_free_index, free_index);
     return rc;
 }
 
@@ -311,6 +365,7 @@ int upload_layout(rbx_integrator* h) {
 // float-float for single and mixed, with the moment gaps formed in FP64 so that they keep their
 // relative accuracy for nearly degenerate tops), rotation classes and body-frame positions.
 int upload_bodies(rbx_integrator* h) {
+    if (int rc = ensure_host_plan(h)) return rc;
     const int nb = h->nb, nbp = h->nb_pad, nbap = h->nba_pad;
     if (h->prec == PREC_DOUBLE) {
         std::vector<double> invm(std::max(nb, 1), 0.0), invI((size_t)3 * nbp, 0.0);
@@ -393,39 +448,133 @@ int run_step(rbx_integrator* h, int kind, void* stream, const rbx_buffers* buf, 
     return RBX_OK;
 }
 
-// Rows [r0, r0 + rows) of a device array of `es`-byte elements with row stride ld: entry i of
-// each row moves from position src[i].
-int permute_rows(void* p, size_t r0, size_t rows, size_t ld, size_t es, const std::vector<int>& src) {
-    if (src.empty()) return RBX_OK;
-    unsigned char* base = (unsigned char*)p + r0 * ld * es;
-    std::vector<unsigned char> in(rows * ld * es), out(rows * ld * es, 0);
-    CUDA_TRY(cudaMemcpy(in.data(), base, in.size(), cudaMemcpyDeviceToHost));
-    for (size_t r = 0; r < rows; r++)
-        for (size_t i = 0; i < src.size(); i++) std::memcpy(&out[(r * ld + i) * es], &in[(r * ld + src[i]) * es], es);
-    CUDA_TRY(cudaMemcpy(base, out.data(), out.size(), cudaMemcpyHostToDevice));
-    return RBX_OK;
-}
-
-// After a re-plan of the library order: move the refined-energy stencil sums and terms of every
-// body and free atom to its new position (bit for bit), so that a reordering of the device slots
-// between the two halves of a step, or between a step and the energy query, loses nothing.
-int move_refined(rbx_integrator* h, const std::vector<int>& old_pos, const std::vector<int>& old_free) {
-    const size_t es = h->prec == PREC_DOUBLE ? 8 : 4, nbp = h->nb_pad, nfp = h->nf_pad;
-    std::vector<int> bsrc(h->nb), fsrc(h->nf);
-    for (int L = 0; L < h->nb; L++) bsrc[L] = old_pos[h->lib_body[L]];
-    std::vector<int> old_index(h->natoms, -1);
-    for (int j = 0; j < h->nf; j++) old_index[old_free[j]] = j;
-    for (int j = 0; j < h->nf; j++) fsrc[j] = old_index[h->free_atoms[j]];
-    int rc = permute_rows(h->d_ref_start.p, 0, 7, nbp, es, bsrc);
-    if (!rc) rc = permute_rows(h->d_ref_out.p, 0, 3, nbp, 4, bsrc);
-    // free-atom rows follow the body rows: offsets in units of their own row length
-    if (!rc && h->nf) {
-        unsigned char* fs = h->d_ref_start.p + 7 * nbp * es;
-        unsigned char* fo = (unsigned char*)(h->d_ref_out.p + 3 * nbp);
-        rc = permute_rows(fs, 0, 3, nfp, es, fsrc);
-        if (!rc) rc = permute_rows(fo, 0, 2, nfp, 4, fsrc);
+// Re-plan the library order for new device slots, on the device (rbx_plan.cu): sort bodies by
+// the lowest slot of their atoms and free atoms by slot, pack tiles on the host, then move every
+// per-body, per-body-atom and per-free-atom array to the new order with raw gathers, so the state
+// moves bit for bit. Host copies of the plan are rebuilt only on demand.
+// Device allocations replaced during a re-plan, freed once the stream has finished with them.
+struct Retired {
+    cudaStream_t st = nullptr;
+    std::vector<void*> ptrs;
+    template <class A> void take(A& a) {
+        if (a.p) ptrs.push_back(a.p);
+        a.p = nullptr;
+        a.n = 0;
     }
-    return rc;
+    ~Retired() {
+        if (ptrs.empty()) return;
+        cudaStreamSynchronize(st);
+        for (void* p : ptrs) cudaFree(p);
+    }
+};
+
+int replan_device(rbx_integrator* h, const int* location, int nslots) {
+    const int n = h->natoms, nb = h->nb, nf = h->nf, nba = h->nba;
+    cudaStream_t st = nullptr;
+    Retired old;
+    old.st = st;
+    if (h->r_nslots < nslots) {
+        const size_t aux = scan_aux_len(std::max(nslots, nb + 1));
+        if (h->r_marks.alloc((size_t)2 * nslots) != cudaSuccess || h->r_scan.alloc(nslots) != cudaSuccess ||
+            h->r_seen.alloc((size_t)(nslots + 31) / 32) != cudaSuccess || h->r_aux.alloc(aux) != cudaSuccess)
+            return fail(RBX_ERR_CUDA, "cudaMalloc of the re-plan scratch failed");
+        h->r_nslots = nslots;
+    }
+    if (!h->r_loc.p && (h->r_loc.alloc(n) != cudaSuccess || h->r_status.alloc(1) != cudaSuccess ||
+                        h->r_lib_body.alloc(std::max(nb, 1)) != cudaSuccess ||
+                        h->r_free.alloc(std::max(nf, 1)) != cudaSuccess ||
+                        h->r_idx.alloc((size_t)nb + nba + nf + 1) != cudaSuccess))
+        return fail(RBX_ERR_CUDA, "cudaMalloc of the re-plan scratch failed");
+    CUDA_TRY(cudaMemcpyAsync(h->r_loc.p, location, sizeof(int) * (size_t)n, cudaMemcpyHostToDevice, st));
+    PlanOrder P;
+    P.nb = nb; P.nf = nf; P.natoms = n; P.nslots = nslots;
+    P.ref_first = h->d_ref_first.p; P.ref_atoms = h->d_ref_atoms.p; P.loc = h->r_loc.p; P.free_old = h->d_free_atoms.p;
+    P.seen = h->r_seen.p; P.status = h->r_status.p; P.mark_body = h->r_marks.p; P.mark_free = h->r_marks.p + nslots;
+    P.scan = h->r_scan.p; P.aux = h->r_aux.p; P.lib_body_new = h->r_lib_body.p; P.free_new = h->r_free.p;
+    if (launch_plan_order(P, st)) return fail(RBX_ERR_CUDA, "re-plan kernels failed: %s", cudaGetErrorString(cudaGetLastError()));
+    std::vector<int> lib_body(nb);
+    int status = 0;
+    if (nb) CUDA_TRY(cudaMemcpyAsync(lib_body.data(), h->r_lib_body.p, sizeof(int) * (size_t)nb, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(&status, h->r_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (status) return fail(RBX_ERR_INVALID_ARGUMENT, "a device slot is assigned to two atoms");
+
+    // new maps, then every array gathered into a fresh allocation and swapped in
+    DevArray<int> lib_pos, atom0, atom_loc, free_loc, free_index;
+    if (lib_pos.alloc(std::max(nb, 1)) != cudaSuccess || atom0.alloc(nb + 1) != cudaSuccess ||
+        atom_loc.alloc(std::max(nba, 1)) != cudaSuccess || free_loc.alloc(std::max(nf, 1)) != cudaSuccess ||
+        free_index.alloc(n) != cudaSuccess)
+        return fail(RBX_ERR_CUDA, "cudaMalloc of the new plan failed");
+    CUDA_TRY(cudaMemcpyAsync(free_index.p, h->d_free_index.p, sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, st));
+    int* idx_body = h->r_idx.p;
+    int* idx_atom = idx_body + nb;
+    int* idx_free = idx_atom + nba;
+    PlanMaps M;
+    M.nb = nb; M.nf = nf;
+    M.ref_first = h->d_ref_first.p; M.ref_atoms = h->d_ref_atoms.p; M.loc = h->r_loc.p;
+    M.lib_body_new = h->r_lib_body.p; M.lib_pos_old = h->d_lib_pos.p; M.atom0_old = h->d_atom0.p;
+    M.free_new = h->r_free.p; M.free_index_old = h->d_free_index.p;
+    M.lib_pos_new = lib_pos.p; M.atom0_new = atom0.p; M.idx_body = idx_body; M.idx_atom = idx_atom;
+    M.atom_loc_new = atom_loc.p; M.idx_free = idx_free; M.free_loc_new = free_loc.p; M.free_index_new = free_index.p;
+    M.aux = h->r_aux.p;
+    if (launch_plan_maps(M, st)) return fail(RBX_ERR_CUDA, "re-plan map kernels failed: %s", cudaGetErrorString(cudaGetLastError()));
+
+    const size_t nbp = h->nb_pad, nbap = h->nba_pad, nfp = h->nf_pad;
+    const int es = h->prec == PREC_DOUBLE ? 8 : 4;
+    // rows of `count` elements of `ebytes` bytes at stride ld, gathered by idx into a new array
+    auto regather = [&](auto& arr, int rows, size_t ld, int count, const int* idx, int ebytes) -> int {
+        if (!arr.p || count == 0) return RBX_OK;
+        std::remove_reference_t<decltype(arr)> tmp;
+        if (tmp.alloc(arr.n) != cudaSuccess) return fail(RBX_ERR_CUDA, "cudaMalloc during the re-plan failed");
+        if (launch_gather_rows(tmp.p, arr.p, rows, ld, count, idx, ebytes, st))
+            return fail(RBX_ERR_CUDA, "re-plan gather failed: %s", cudaGetErrorString(cudaGetLastError()));
+        arr.swap(tmp);
+        old.take(tmp);
+        return RBX_OK;
+    };
+    int rc = regather(h->d_state, h->prec == PREC_DOUBLE ? 14 : 28, nbp, nb, idx_body, es);
+    if (!rc && h->prec == PREC_DOUBLE) rc = regather(h->d_invm, 1, nbp, nb, idx_body, 8);
+    if (!rc && h->prec == PREC_DOUBLE) rc = regather(h->d_invI, 3, nbp, nb, idx_body, 8);
+    if (!rc && h->prec != PREC_DOUBLE) rc = regather(h->d_bconst, kBconstRows, nbp, nb, idx_body, 4);
+    if (!rc) rc = regather(h->d_cls, 1, nbp, nb, idx_body, 1);
+    if (!rc) rc = regather(h->d_I, 3, nbp, nb, idx_body, 8);
+    if (!rc) rc = regather(h->d_dof, 1, nbp, nb, idx_body, 4);
+    if (!rc) rc = regather(h->d_fixed, 3, nbap, nba, idx_atom, es);
+    if (!rc) rc = regather(h->d_bmass, 1, nbap, nba, idx_atom, 8);
+    if (!rc && h->d_ref_start.p) {
+        // body rows then free-atom rows of one allocation each: gather both parts into a new one
+        DevArray<unsigned char> s2;
+        DevArray<float> o2;
+        if (s2.alloc(h->d_ref_start.n) != cudaSuccess || o2.alloc(h->d_ref_out.n) != cudaSuccess)
+            return fail(RBX_ERR_CUDA, "cudaMalloc during the re-plan failed");
+        unsigned char* fs_old = h->d_ref_start.p + 7 * nbp * es;
+        unsigned char* fs_new = s2.p + 7 * nbp * es;
+        if (launch_gather_rows(s2.p, h->d_ref_start.p, 7, nbp, nb, idx_body, es, st) ||
+            launch_gather_rows(fs_new, fs_old, 3, nfp, nf, idx_free, es, st) ||
+            launch_gather_rows(o2.p, h->d_ref_out.p, 3, nbp, nb, idx_body, 4, st) ||
+            launch_gather_rows(o2.p + 3 * nbp, h->d_ref_out.p + 3 * nbp, 2, nfp, nf, idx_free, 4, st))
+            return fail(RBX_ERR_CUDA, "re-plan gather failed: %s", cudaGetErrorString(cudaGetLastError()));
+        h->d_ref_start.swap(s2);
+        h->d_ref_out.swap(o2);
+        old.take(s2);
+        old.take(o2);
+    }
+    if (rc) return rc;
+    // the plan itself
+    h->lib_body.swap(lib_body);
+    pack_tiles(h);
+    CUDA_TRY(cudaStreamSynchronize(st));  // gathers done before the old arrays are freed below
+    h->d_atom0.swap(atom0);
+    h->d_atom_loc.swap(atom_loc);
+    h->d_free_loc.swap(free_loc);
+    h->d_lib_pos.swap(lib_pos);
+    h->d_free_index.swap(free_index);
+    h->d_free_atoms.swap(h->r_free);
+    h->c_loc.swap(h->r_loc);
+    if ((rc = upload(h->d_tiles, h->tile_body0))) return rc;
+    h->max_location = nslots - 1;
+    h->host_plan_valid = false;
+    return RBX_OK;
 }
 
 }  // namespace
@@ -540,33 +689,17 @@ int rbx_set_atom_locations(rbx_integrator* h, const int* location) {
     int rc = check(h);
     if (rc) return rc;
     if (!location) return fail(RBX_ERR_INVALID_ARGUMENT, "null location array");
-    std::vector<char> seen(h->natoms, 0);
+    int lo = INT32_MAX, hi = -1;
     for (int i = 0; i < h->natoms; i++) {
-        if (location[i] < 0) return fail(RBX_ERR_INVALID_ARGUMENT, "negative location for atom %d", i);
-        if (location[i] < h->natoms) {
-            if (seen[location[i]]) return fail(RBX_ERR_INVALID_ARGUMENT, "slot %d assigned twice", location[i]);
-            seen[location[i]] = 1;
-        }
+        lo = std::min(lo, location[i]);
+        hi = std::max(hi, location[i]);
+    }
+    if (lo < 0) {
+        const int i = (int)(std::find_if(location, location + h->natoms, [](int s) { return s < 0; }) - location);
+        return fail(RBX_ERR_INVALID_ARGUMENT, "negative location for atom %d", i);
     }
     CUDA_TRY(cudaSetDevice(h->device));
-    if ((rc = ensure_host_geometry(h))) return rc;  // read in the current order, re-uploaded below
-    h->location.assign(location, location + h->natoms);
-    h->max_location = *std::max_element(h->location.begin(), h->location.end());
-    // Re-plan the library order for the new slots and carry the body state (and constants)
-    // over to it; the raw rows are permuted, so the float-float state moves bit for bit.
-    const std::vector<int> old_pos = h->lib_pos, old_free = h->free_atoms;
-    plan_order(h);
-    if ((rc = upload_layout(h))) return rc;
-    if (h->refined && h->ref_phase != 0 && (rc = move_refined(h, old_pos, old_free))) return rc;
-    if (!h->have_state || h->nb == 0 || old_pos == h->lib_pos) return RBX_OK;
-    const size_t rows = h->prec == PREC_DOUBLE ? 14 : 28, es = h->prec == PREC_DOUBLE ? 8 : 4, nbp = h->nb_pad;
-    std::vector<unsigned char> in(rows * nbp * es), out(rows * nbp * es, 0);
-    CUDA_TRY(cudaMemcpy(in.data(), h->d_state.p, in.size(), cudaMemcpyDeviceToHost));
-    for (size_t r = 0; r < rows; r++)
-        for (int L = 0; L < h->nb; L++)
-            std::memcpy(&out[(r * nbp + L) * es], &in[(r * nbp + old_pos[h->lib_body[L]]) * es], es);
-    CUDA_TRY(cudaMemcpy(h->d_state.p, out.data(), out.size(), cudaMemcpyHostToDevice));
-    return upload_bodies(h);
+    return replan_device(h, location, hi + 1);
 }
 
 // Body state rows (14 per body, library order) -> device layout of the integrator's precision:
@@ -604,6 +737,7 @@ int rbx_upload_state(rbx_integrator* h, const double* positions, const double* v
     int rc = check(h);
     if (rc) return rc;
     if (!positions || !velocities) return fail(RBX_ERR_INVALID_ARGUMENT, "null positions or velocities");
+    if ((rc = ensure_host_plan(h))) return rc;
     const int nb = h->nb, nbp = h->nb_pad;
     std::vector<double> state((size_t)14 * nbp, 0.0);
     int ndof = 3 * h->nf;  // three per free atom (RigidBodySystem.cpp:130 counts one: defect D8)
@@ -782,6 +916,7 @@ int rbx_get_body_state(rbx_integrator* h, double* state) {
     int rc = check(h);
     if (rc) return rc;
     if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body state");
+    if ((rc = ensure_host_plan(h))) return rc;
     std::vector<double> s;
     CUDA_TRY(cudaSetDevice(h->device));
     if ((rc = get_state(h, s))) return rc;
@@ -794,6 +929,7 @@ int rbx_set_body_state(rbx_integrator* h, const double* state) {
     int rc = check(h);
     if (rc) return rc;
     if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body geometry: call rbx_upload_state first");
+    if ((rc = ensure_host_plan(h))) return rc;
     std::vector<double> s((size_t)14 * h->nb_pad, 0.0);
     for (int b = 0; b < h->nb; b++)
         for (int k = 0; k < 14; k++) s[h->lib_pos[b] + (size_t)k * h->nb_pad] = state[14 * (size_t)b + k];

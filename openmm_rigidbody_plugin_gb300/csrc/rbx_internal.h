@@ -157,6 +157,53 @@ struct SetupOut {
 int launch_setup_bodies(int prec, const DevSys& s, const DevBuf& b, const double* bmass, const SetupOut& out,
                         void* stream);
 
+// Re-planning the library order on the device (rbx_plan.cu). launch_plan_order checks that the
+// new slots are distinct (status != 0 otherwise; non-negative slots below nslots are the caller's
+// check) and sorts bodies by the lowest slot of their atoms and free atoms by slot.
+struct PlanOrder {
+    int nb, nf, natoms, nslots;  // nslots = largest slot + 1
+    const int* ref_first;        // [nb+1] reference order
+    const int* ref_atoms;        // [nba]
+    const int* loc;              // [natoms] new slots
+    const int* free_old;         // [nf] free atoms (user indices) in any order
+    unsigned int* seen;          // scratch [(nslots + 31) / 32]
+    int* status;                 // [1]
+    int *mark_body, *mark_free;  // scratch [nslots] each
+    int* scan;                   // scratch [nslots]
+    int* aux;                    // scratch [scan_aux_len(max(nslots, nb + 1))]
+    int* lib_body_new;           // [nb] out: library position -> reference body
+    int* free_new;               // [nf] out: free atoms in slot order
+};
+// launch_plan_maps derives, for the new order, where every body, body atom and free atom comes
+// from in the current arrays (idx_*), and the new first-atom, slot and inverse maps.
+struct PlanMaps {
+    int nb, nf;
+    const int* ref_first;
+    const int* ref_atoms;
+    const int* loc;
+    const int* lib_body_new;
+    const int* lib_pos_old;      // [nb] reference body -> current library position
+    const int* atom0_old;        // [nb+1]
+    const int* free_new;
+    const int* free_index_old;   // [natoms] free atom (user index) -> current free position
+    int* lib_pos_new;            // [nb]
+    int* atom0_new;              // [nb+1]
+    int* idx_body;               // [nb]  new library position -> current library position
+    int* idx_atom;               // [nba] new body-atom index -> current body-atom index
+    int* atom_loc_new;           // [nba]
+    int* idx_free;               // [nf]  new free position -> current free position
+    int* free_loc_new;           // [nf]
+    int* free_index_new;         // [natoms]
+    int* aux;                    // scan scratch
+};
+size_t scan_aux_len(int n);
+int device_exclusive_scan(int* data, int n, int* aux, void* stream);
+int launch_plan_order(const PlanOrder& P, void* stream);
+int launch_plan_maps(const PlanMaps& M, void* stream);
+// dst[r * ld + i] = src[r * ld + idx[i]] for rows r < rows, i < n; elements of 1, 4 or 8 bytes.
+int launch_gather_rows(void* dst, const void* src, int rows, size_t ld, int n, const int* idx, int elem_bytes,
+                       void* stream);
+
 // Internal views of an integrator for the batched driver (defined in rbx_host.cpp).
 DevSys device_system(const rbx_integrator* h);
 // Host copies of the body geometry, fetched from the device after a device-side setup (all of
@@ -166,8 +213,8 @@ int sync_host_dof(rbx_integrator* h);
 // For systems whose atoms occupy consecutive device-slot ranges [slot_offsets[s],
 // slot_offsets[s+1]): the library-order ranges of their bodies (body0[S+1]) and free atoms
 // (free0[S+1]), and their degrees of freedom (dof[S]).
-void system_ranges(const rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
-                   std::vector<int>& free0, std::vector<int>& dof);
+int system_ranges(rbx_integrator* h, const std::vector<int>& slot_offsets, std::vector<int>& body0,
+                  std::vector<int>& free0, std::vector<int>& dof);
 // Body-atom positions rebuilt from the stored body state (the step kernels' arithmetic).
 int launch_sync_positions(int prec, const DevSys& s, const DevBuf& b, void* stream);
 // Scale the body COM velocities and quaternion momenta and the free atoms' velocities.

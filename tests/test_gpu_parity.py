@@ -221,6 +221,64 @@ def test_reordering_mid_run_is_bit_exact(rbx, prec):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("prec", ["mixed", "double"])
+def test_reordering_into_padded_slots_is_bit_exact(rbx, prec):
+    """OpenMM pads its atom buffers: slots above the atom count, and gaps between used slots. The
+    re-plan on the device sorts by slot across the whole slot range."""
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    s = W.mixed_system(n_bodies=2000, n_free=300, seed=17)
+    n = s.num_atoms
+    F = W.gaussian_forces(n, seed=6, sd=50.0)
+    runs = []
+    for move in (False, True):
+        k = rbx.IntegratorKernel(s.masses, s.body_indices, rotation_mode=4, precision=prec)
+        buf = rbx.DeviceBuffers(n, precision=prec, stride=3 * n + 32)
+        buf.set_positions(s.positions)
+        buf.set_velocities(s.velocities, s.masses)
+        k.upload_state(s.positions, s.velocities)
+        buf.set_forces(F)
+        rng = np.random.default_rng(5)
+        for step in range(9):
+            if move and step % 3 == 1:
+                loc = rng.choice(3 * n + 32, size=n, replace=False)
+                buf.relocate(loc)
+                k.set_atom_locations(loc)
+            k.part1(buf, 0.002)
+            k.part2(buf, 0.002)
+        runs.append((buf.get_positions(), buf.get_velocities(), k.body_state(), k.kinetic_energies(buf)))
+    for a, b in zip(runs[0][:3], runs[1][:3]):
+        assert np.array_equal(a, b)
+    # the energy sums run in library order, which the re-plan changes: equal to rounding
+    np.testing.assert_allclose(runs[1][3], runs[0][3], rtol=1e-13)
+
+
+def test_invalid_locations_are_rejected_and_change_nothing(rbx):
+    from openmm_rigidbody_plugin_gb300 import _lib
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    s = W.mixed_system(n_bodies=500, n_free=50, seed=19)
+    n = s.num_atoms
+    F = W.gaussian_forces(n, seed=7, sd=50.0)
+    runs = []
+    for bad in (False, True):
+        k, buf = make(rbx, s.masses, s.body_indices, s.positions, s.velocities, 0, "mixed")
+        buf.set_forces(F)
+        for step in range(4):
+            if bad and step == 2:
+                dup = np.arange(n)
+                dup[7] = dup[3]  # one slot for two atoms
+                with pytest.raises(_lib.RbxError, match="two atoms"):
+                    k.set_atom_locations(dup)
+                neg = np.arange(n)
+                neg[11] = -1
+                with pytest.raises(_lib.RbxError, match="negative location for atom 11"):
+                    k.set_atom_locations(neg)
+            k.part1(buf, 0.002)
+            k.part2(buf, 0.002)
+        runs.append((buf.get_positions(), buf.get_velocities(), k.body_state()))
+    for a, b in zip(runs[0], runs[1]):
+        assert np.array_equal(a, b)
+
+
 @pytest.mark.parametrize("prec", ["single", "mixed", "double"])
 def test_host_buffer_step(rbx, golden, prec):
     """rbx_step_host (host arrays in, host arrays out) against the reference."""
