@@ -547,9 +547,9 @@ int replan_device(rbx_integrator* h, const int* location, int nslots) {
         DevArray<float> o2;
         if (s2.alloc(h->d_ref_start.n) != cudaSuccess || o2.alloc(h->d_ref_out.n) != cudaSuccess)
             return fail(RBX_ERR_CUDA, "cudaMalloc during the re-plan failed");
-        unsigned char* fs_old = h->d_ref_start.p + 7 * nbp * es;
-        unsigned char* fs_new = s2.p + 7 * nbp * es;
-        if (launch_gather_rows(s2.p, h->d_ref_start.p, 7, nbp, nb, idx_body, es, st) ||
+        unsigned char* fs_old = h->d_ref_start.p + kRefBodyRows * nbp * es;
+        unsigned char* fs_new = s2.p + kRefBodyRows * nbp * es;
+        if (launch_gather_rows(s2.p, h->d_ref_start.p, kRefBodyRows, nbp, nb, idx_body, es, st) ||
             launch_gather_rows(fs_new, fs_old, 3, nfp, nf, idx_free, es, st) ||
             launch_gather_rows(o2.p, h->d_ref_out.p, 3, nbp, nb, idx_body, 4, st) ||
             launch_gather_rows(o2.p + 3 * nbp, h->d_ref_out.p + 3 * nbp, 2, nfp, nf, idx_free, 4, st))
@@ -842,7 +842,7 @@ int rbx_set_compute_refined_energies(rbx_integrator* h, int compute) {
     if (!h->refined || h->d_ref_start.p) return RBX_OK;
     CUDA_TRY(cudaSetDevice(h->device));
     const size_t es = h->prec == PREC_DOUBLE ? sizeof(double) : sizeof(float);
-    const size_t start = (7 * (size_t)h->nb_pad + 3 * (size_t)h->nf_pad) * es;
+    const size_t start = (kRefBodyRows * (size_t)h->nb_pad + 3 * (size_t)h->nf_pad) * es;
     const size_t terms = 3 * (size_t)h->nb_pad + 2 * (size_t)h->nf_pad;
     const int blocks = refined_blocks(h->sys());
     if (h->d_ref_start.alloc(start) != cudaSuccess || h->d_ref_out.alloc(terms) != cudaSuccess ||

@@ -15,10 +15,12 @@
 //   atom_loc     int [nba]: device slot of each body atom (library order)
 //   free_loc     int [nf]:  device slot of each free atom
 //   tile_body0   int [n_body_tiles+1]: bodies of tile t are [tile_body0[t], tile_body0[t+1])
-//   ref_start    refined energies only: the stencil sums that part1 and fused steps start and
-//                part2 completes. Bodies: 7 rows of nb_pad (F h/m, then the quaternion stencil
-//                0.5 [q(t-h) - q(t)] + 2.5 [q(t+h) - q(t)]); then free atoms: 3 rows of nf_pad
-//                (F h/m). float (single, mixed) or double (double precision).
+//   ref_start    refined energies only: what part1 and fused steps record for part2 to close
+//                the stencils. Bodies: kRefBodyRows rows of nb_pad: F h/m [3], then, single/mixed,
+//                q(t+h) - q(t) [4] and the body angular momentum L(t-h/2) of the backward virtual
+//                rotation [3], or, double, the quaternion stencil 0.5 [q(t-h) - q(t)] + 2.5
+//                [q(t+h) - q(t)] [4]; then free atoms: 3 rows of nf_pad (F h/m). float (single,
+//                mixed) or double (double precision).
 //   ref_out      refined energies only, float, written by part2. Bodies: 3 rows of nb_pad (KE_t
 //                correction, KE_r correction, |F|^2/m + tau.I^-1.tau); then free atoms: 2 rows of
 //                nf_pad (KE_t correction, |F|^2/m).
@@ -45,6 +47,7 @@ constexpr int kThreadsF = 256;
 constexpr int kTileBodiesF = 256;
 constexpr int kTileAtomsF = 1024;
 constexpr int kBconstRows = 11;     // rows of the FP32 body-constant table (single/mixed)
+constexpr int kRefBodyRows = 10;    // rows of ref_start per body
 
 inline int tile_atoms(int prec) { return prec == PREC_DOUBLE ? kTileAtomsD : kTileAtomsF; }
 inline int tile_bodies(int prec) { return prec == PREC_DOUBLE ? kTileBodies : kTileBodiesF; }

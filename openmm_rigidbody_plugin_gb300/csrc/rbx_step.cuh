@@ -158,7 +158,7 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
     V3<T> dv = F * (w * halfDt);
     if (KIND != STEP_PART1) v = v + dv;  // second half kick of step n (rigidbodyintegrator.cu:351-358)
     if (REF && KIND == STEP_PART2) {
-        const RS* st = (const RS*)S.ref_start + 7 * (size_t)S.nb_pad;
+        const RS* st = (const RS*)S.ref_start + kRefBodyRows * (size_t)S.nb_pad;
         const V3<T> al = v3<T>((T)st[j], (T)st[j + S.nf_pad], (T)st[j + 2 * S.nf_pad]);
         float* out = S.ref_out + 3 * (size_t)S.nb_pad;
         out[j] = w != T(0) ? (float)(dot(v, al - dv * T(2)) / (T(12) * w)) : 0.0f;
@@ -166,7 +166,7 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
     }
     if (KIND != STEP_PART2) {            // first half kick and drift of the next step (:302-310)
         if (REF) {
-            RS* st = (RS*)S.ref_start + 7 * (size_t)S.nb_pad;
+            RS* st = (RS*)S.ref_start + kRefBodyRows * (size_t)S.nb_pad;
             st[j] = (RS)(dv.x * T(2)); st[j + S.nf_pad] = (RS)(dv.y * T(2)); st[j + 2 * S.nf_pad] = (RS)(dv.z * T(2));
         }
         v = v + dv;
@@ -537,16 +537,23 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
                 // body's terms of refinedKineticEnergies / potentialEnergyRefinement (:433-469), as
                 // corrections: KE_t: (m/12) v.(alpha - beta), alpha = F(t) h/m, beta = F(t+h) h/m
                 // (equal to rdot.v m/(6h) - m|v|^2/2 for the reference's position stencil); KE_r:
-                // qdot.pi/(6h) - L.I^-1.L/2, qdot the quaternion stencil closed by q(t+2h) - q(t+h)
-                // = q (x) dr of the virtual rotation from (q(t+h), pi(t+h) + C(q,tau) h) (:238-243),
-                // projected off q; and |F|^2/m + tau.I^-1.tau in the body frame.
+                // qdot.pi/(6h) - L.I^-1.L/2 with the quaternion stencil
+                //   qdot = 0.5 [q(t-h) - q(t)] + 2.5 [q(t+h) - q(t)] + [q(t+2h) - q(t+h)],
+                // q(t-h) - q(t) = q(t) (x) dr_b, the virtual rotation by -h from (q(t), pi(t-h/2))
+                // (:318-321), taken as the rotation by +h with the angular momentum reversed (the free
+                // rotor is time-reversible); q(t+2h) - q(t+h) = q (x) dr_f, the virtual rotation from
+                // (q(t+h), pi(t+h) + C(q,tau) h) (:238-243); qdot projected off q; and
+                // |F|^2/m + tau.I^-1.tau in the body frame. Both virtual rotations run here, once per
+                // part2, rather than in every fused step.
                 const float* rs = (const float*)S.ref_start;
                 const V3<float> al = v3<float>(rs[b], rs[b + nbp], rs[b + 2 * nbp]);
-                Q4<float> qd = q4<float>(rs[b + 3 * nbp], rs[b + 4 * nbp], rs[b + 5 * nbp], rs[b + 6 * nbp]);
+                const Q4<float> dqn = q4<float>(rs[b + 3 * nbp], rs[b + 4 * nbp], rs[b + 5 * nbp], rs[b + 6 * nbp]);
+                const V3<float> Lb = v3<float>(rs[b + 7 * nbp], rs[b + 8 * nbp], rs[b + 9 * nbp]);
                 const V3<float> vh = v3<float>(x[3].hi, x[4].hi, x[5].hi);
                 const float dkt = dot(vh, al - Fa * (invm * dt)) / (12.0f * invm);
+                const Q4<float> drb = rotation_increment<EXACT>(S, b, Lb * -1.0f, R, dt);
                 const Q4<float> drf = rotation_increment<EXACT>(S, b, qBt(qh, ph + Ctau) * 0.5f, R, dt);
-                qd = qd + qmul(qh, drf);
+                Q4<float> qd = qmul(qh - dqn, drb) * 0.5f + dqn * 2.5f + qmul(qh, drf);
                 qd = qd - qh * dot(qd, qh);
                 const V3<float> L = qBt(qh, ph) * 0.5f;
                 const float dkr = dot(qd, ph) / (6.0f * dt) - 0.5f * dot(L, mul(R.invI, L));
@@ -582,18 +589,18 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
                 x[c] = ff_norm(ff_acc(x[c], ren[c - 6]));
             }
             if (REF) {
-                // start of the stencils at t (rigidbodyintegrator.cu:318-321): alpha = F(t) h/m and
-                // 0.5 [q(t-h) - q(t)] + 2.5 [q(t+h) - q(t)]. q(t+h) - q(t) is the increment just
-                // applied (dq plus the renormalisation); q(t-h) - q(t) = q (x) dr_b, the virtual
-                // rotation by -h from (q(t), pi(t) - C(q,tau) h), taken as the rotation by +h with
-                // the momentum reversed (the free rotor is time-reversible).
+                // start of the stencils at t (rigidbodyintegrator.cu:318-321): alpha = F(t) h/m, the
+                // increment q(t+h) - q(t) just applied (dq plus the renormalisation), and the body
+                // angular momentum L(t-h/2) = Bt(q(t), pi(t) - C(q,tau) h)/2 of the backward virtual
+                // rotation, which part2 performs
                 const Q4<float> pib = KIND == STEP_FUSED ? pin : pin - Ctau;
-                const Q4<float> drb = rotation_increment<EXACT>(S, b, qBt(qh, pib) * -0.5f, R, dt);
-                const Q4<float> sq = qmul(qh, drb) * 0.5f + (dq + q4<float>(ren[0], ren[1], ren[2], ren[3])) * 2.5f;
+                const V3<float> Lb = qBt(qh, pib) * 0.5f;
+                const Q4<float> dqn = dq + q4<float>(ren[0], ren[1], ren[2], ren[3]);
                 const V3<float> al = Fa * (invm * dt);
                 float* rs = (float*)S.ref_start;
                 rs[b] = al.x; rs[b + nbp] = al.y; rs[b + 2 * nbp] = al.z;
-                rs[b + 3 * nbp] = sq.w; rs[b + 4 * nbp] = sq.x; rs[b + 5 * nbp] = sq.y; rs[b + 6 * nbp] = sq.z;
+                rs[b + 3 * nbp] = dqn.w; rs[b + 4 * nbp] = dqn.x; rs[b + 5 * nbp] = dqn.y; rs[b + 6 * nbp] = dqn.z;
+                rs[b + 7 * nbp] = Lb.x; rs[b + 8 * nbp] = Lb.y; rs[b + 9 * nbp] = Lb.z;
             }
 #pragma unroll
             for (int c = 0; c < 3; c++) {
