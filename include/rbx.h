@@ -119,6 +119,31 @@ int rbx_integrate_part2(rbx_integrator* h, void* stream, const rbx_buffers* buf,
 int rbx_integrate_fused(rbx_integrator* h, void* stream, const rbx_buffers* buf, double dt);
 
 /*
+ * Constraints between free atoms (bond-length constraints that OpenMM's solvers enforce).
+ * rbx_set_constraints checks the System's constraints, atom pairs [2*num_constraints], as
+ * RigidBodySystem::initialize does (openmmapi/src/RigidBodySystem.cpp:107-113: "Constraints
+ * involving rigid-body atoms are not allowed"); each removes one degree of freedom
+ * (RigidBodySystem.cpp:130).
+ * A step with constrained free atoms replaces rbx_integrate_part1 by three calls, the protocol of
+ * CudaRigidBodyKernels.cpp:405-419 around OpenMM's posDelta buffer (mixed4 per slot: float4 in
+ * single precision, double4 in mixed and double):
+ *   rbx_free_atoms_delta      pos_delta <- h (v + F/m h/2) for every free atom (freeAtomsDelta,
+ *                             rigidbodyintegrator.cu:270-279);
+ *   (OpenMM's applyConstraints corrects pos_delta);
+ *   rbx_integrate_part1_delta bodies as rbx_integrate_part1; free atoms move by the corrected
+ *                             pos_delta and take it over h as their mid-step velocity.
+ * Then forces, rbx_integrate_part2 and OpenMM's applyVelocityConstraints. The velocity follows the
+ * Reference platform (RigidBodySystem.cpp:172-176, :197: the (R - savedPos)/dt correction after
+ * SHAKE); the CUDA reference saves the position after the constraints, so its correction is zero.
+ * Fused steps skip the constraints and must not be used with them. Refined energies are not
+ * available with constrained free atoms (RBX_ERR_UNSUPPORTED).
+ */
+int rbx_set_constraints(rbx_integrator* h, int num_constraints, const int* atom_pairs);
+int rbx_free_atoms_delta(rbx_integrator* h, void* stream, const rbx_buffers* buf, void* pos_delta, double dt);
+int rbx_integrate_part1_delta(rbx_integrator* h, void* stream, const rbx_buffers* buf, const void* pos_delta,
+                              double dt);
+
+/*
  * Translational and rotational kinetic energy [KE_t, KE_r] in kJ/mol, reduced on the device in
  * FP64 in a fixed order; synchronises `stream`. Replaces the kineticEnergies kernel plus host
  * summation (rigidbodyintegrator.cu:416-427, CudaRigidBodyKernels.cpp:118-163) and

@@ -44,6 +44,9 @@ SIGNATURES = [
     ("rbx_integrate_part2", ctypes.c_int, [_vp, _vp, _bp, ctypes.c_double]),
     ("rbx_integrate_fused", ctypes.c_int, [_vp, _vp, _bp, ctypes.c_double]),
     ("rbx_kinetic_energies", ctypes.c_int, [_vp, _vp, _bp, _dp]),
+    ("rbx_set_constraints", ctypes.c_int, [_vp, ctypes.c_int, _ip]),
+    ("rbx_free_atoms_delta", ctypes.c_int, [_vp, _vp, _bp, _vp, ctypes.c_double]),
+    ("rbx_integrate_part1_delta", ctypes.c_int, [_vp, _vp, _bp, _vp, ctypes.c_double]),
     ("rbx_set_compute_refined_energies", ctypes.c_int, [_vp, ctypes.c_int]),
     ("rbx_get_compute_refined_energies", ctypes.c_int, [_vp, _ip]),
     ("rbx_refined_kinetic_energies", ctypes.c_int, [_vp, _vp, _bp, _dp]),

@@ -17,6 +17,9 @@
 forces), the integrator, positions, velocities and a force provider, a callable positions ->
 (forces, potential energy) evaluated on the host between the two halves of each step, the way the
 Reference platform drives RigidBodySystem::integratePart1/2 (RigidBodySystem.cpp:170-204).
+Constraints between free atoms are enforced, as OpenMM's solvers do, by ``shake`` after part1 and
+``rattle_velocities`` after part2 (ReferenceRigidBodyKernels.cpp:82-108); constraints on body atoms
+are rejected (RigidBodySystem.cpp:107-113).
 Refined ("shadow") energies: setComputeRefinedEnergies before the integrator is bound, then
 getRefinedKineticEnergies / getPotentialEnergyRefinement after a step (RigidBodyIntegrator.cpp:
 34-38, 84-90), computed on the device by the step kernels.
@@ -30,11 +33,51 @@ from . import kernel as _kernel
 from .workloads import KB
 
 __all__ = ["System", "NonbondedForce", "CMMotionRemover", "Topology", "Context", "RigidBodyIntegrator",
-           "RigidBodySystem", "serialize", "deserialize", "ForceField", "StateDataReporter"]
+           "RigidBodySystem", "serialize", "deserialize", "ForceField", "StateDataReporter", "shake",
+           "rattle_velocities"]
 
 
 class OpenMMException(RuntimeError):
     """The plugin's misuse errors (OpenMMException in the reference)."""
+
+
+# --------------------------------------------------------------------------------------------
+# Constraint solvers of the Context stand-in (OpenMM's own enforce constraints in a real Context)
+# --------------------------------------------------------------------------------------------
+def shake(x_old, x, inv_mass, pairs, dist, tol=1e-5, max_iter=200):
+    """Positions x with |x_i - x_j| = d for every constrained pair, corrected along the bonds of
+    x_old (SHAKE, Ryckaert, Ciccotti and Berendsen 1977); tol is relative, as OpenMM's."""
+    x = np.array(x, dtype=np.float64)
+    i, j = pairs[:, 0], pairs[:, 1]
+    wi, wj = inv_mass[i], inv_mass[j]
+    r0 = x_old[i] - x_old[j]
+    d2 = dist * dist
+    for _ in range(max_iter):
+        rij = x[i] - x[j]
+        diff = d2 - np.einsum("ij,ij->i", rij, rij)
+        if np.all(np.abs(diff) <= 2.0 * tol * d2):
+            break
+        g = diff / (2.0 * np.einsum("ij,ij->i", rij, r0) * (wi + wj))
+        np.add.at(x, i, (g * wi)[:, None] * r0)
+        np.subtract.at(x, j, (g * wj)[:, None] * r0)
+    return x
+
+
+def rattle_velocities(x, v, inv_mass, pairs, tol=1e-5, max_iter=200):
+    """Velocities v with no relative component along any constrained bond (RATTLE, Andersen 1983)."""
+    v = np.array(v, dtype=np.float64)
+    i, j = pairs[:, 0], pairs[:, 1]
+    wi, wj = inv_mass[i], inv_mass[j]
+    rij = x[i] - x[j]
+    r2 = np.einsum("ij,ij->i", rij, rij)
+    for _ in range(max_iter):
+        rv = np.einsum("ij,ij->i", rij, v[i] - v[j])
+        if np.all(np.abs(rv) <= tol * r2):
+            break
+        k = rv / (r2 * (wi + wj))
+        np.subtract.at(v, i, (k * wi)[:, None] * rij)
+        np.add.at(v, j, (k * wj)[:, None] * rij)
+    return v
 
 
 # --------------------------------------------------------------------------------------------
@@ -169,6 +212,7 @@ class RigidBodyIntegrator:
         self._refined = False
         self._context = None
         self._kernel = None
+        self._cons = None
 
     # parameters (RigidBodyIntegrator.cpp:18-38)
     def getStepSize(self):
@@ -214,6 +258,20 @@ class RigidBodyIntegrator:
         self._kernel = _kernel.IntegratorKernel(context.system.masses, self._bodyIndices, rotation_mode=self._mode,
                                                 precision=context.precision, device=context.device)
         self._kernel.set_compute_refined_energies(self._refined)
+        cons = context.system.constraints
+        if cons:
+            if self._refined:
+                raise OpenMMException("Refined energies are not available with constrained free atoms")
+            try:
+                self._kernel.set_constraints([(c[0], c[1]) for c in cons])
+            except RuntimeError as e:
+                raise OpenMMException(str(e).split(" [")[0]) from None
+            m = np.asarray(context.system.masses, dtype=np.float64)
+            self._cons = (np.array([(c[0], c[1]) for c in cons], dtype=np.int64),
+                          np.array([c[2] for c in cons], dtype=np.float64),
+                          np.where(m > 0, 1.0 / np.where(m > 0, m, 1.0), 0.0))
+        else:
+            self._cons = None
 
     def getRigidBodySystem(self):
         self._require()
@@ -225,15 +283,29 @@ class RigidBodyIntegrator:
             raise OpenMMException("This Integrator is not bound to a context")
 
     def step(self, steps):
-        """`steps` velocity-Verlet steps: part1, forces at the new positions, part2."""
+        """`steps` velocity-Verlet steps: part1, forces at the new positions, part2; with constraints,
+        SHAKE after part1 with the (R - savedPos)/dt velocity correction and RATTLE after part2
+        (ReferenceRigidBodyKernels.cpp:82-108, RigidBodySystem.cpp:170-204)."""
         self._require()
         c, k = self._context, self._kernel
         c._ensure_state()
+        dt = self._dt
         for _ in range(int(steps)):
-            k.context_step("part1", self._dt)
-            x, _ = k.context_get_state()
+            if self._cons is not None:
+                x0, _ = k.context_get_state()
+            k.context_step("part1", dt)
+            x, v = k.context_get_state()
+            if self._cons is not None:
+                pairs, dist, w = self._cons
+                xc = shake(x0, x, w, pairs, dist, self._tol)
+                v = v + (xc - x) / dt
+                k.context_load(xc, v)
+                x = xc
             c._apply_forces(x)
-            k.context_step("part2", self._dt)
+            k.context_step("part2", dt)
+            if self._cons is not None:
+                x, v = k.context_get_state()
+                k.context_load(x, rattle_velocities(x, v, self._cons[2], self._cons[0], self._tol))
         c._stale = True
 
     def getKineticEnergies(self):

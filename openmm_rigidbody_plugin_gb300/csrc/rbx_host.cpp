@@ -60,6 +60,7 @@ int rbx::set_error(int code, const char* fmt, ...) {
 struct rbx_integrator {
     int natoms = 0, nb = 0, nf = 0, nba = 0, ndof = 0, mode = 0, prec = PREC_MIXED, device = 0;
     int max_location = 0;  // largest device slot in use; every buffer stride must exceed it
+    int ncons = 0;         // constraints between free atoms (each removes one degree of freedom)
     int nb_pad = 0, nba_pad = 0, nf_pad = 0, n_body_tiles = 0, n_free_tiles = 0;
     bool have_state = false;
     int last_launches = 0;
@@ -800,7 +801,53 @@ int rbx_get_num_dof(const rbx_integrator* h, int* out) {
     int rc = check(h);
     if (rc) return rc;
     if (!h->have_state) return fail(RBX_ERR_STATE, "degrees of freedom are known after rbx_upload_state");
-    *out = h->ndof;
+    *out = h->ndof - h->ncons;  // numDOF = free - constraints + body dof (RigidBodySystem.cpp:130)
+    return RBX_OK;
+}
+
+int rbx_set_constraints(rbx_integrator* h, int num_constraints, const int* atom_pairs) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (num_constraints < 0 || (num_constraints > 0 && !atom_pairs))
+        return fail(RBX_ERR_INVALID_ARGUMENT, "need a non-negative count and the atom pairs");
+    std::vector<char> in_body(h->natoms, 0);
+    for (int a : h->ref_atoms) in_body[a] = 1;
+    for (int k = 0; k < 2 * num_constraints; k++) {
+        const int a = atom_pairs[k];
+        if (a < 0 || a >= h->natoms) return fail(RBX_ERR_INVALID_ARGUMENT, "constraint %d: atom %d out of range", k / 2, a);
+        if (in_body[a]) return fail(RBX_ERR_INVALID_ARGUMENT, "Constraints involving rigid-body atoms are not allowed");
+    }
+    h->ncons = num_constraints;
+    return RBX_OK;
+}
+
+int rbx_free_atoms_delta(rbx_integrator* h, void* stream, const rbx_buffers* buf, void* pos_delta, double dt) {
+    int rc = check_ready(h, buf);
+    if (rc) return rc;
+    if (!pos_delta) return fail(RBX_ERR_INVALID_ARGUMENT, "null posDelta buffer");
+    if (!(dt == dt) || dt == 0.0) return fail(RBX_ERR_INVALID_ARGUMENT, "step size must be finite and non-zero");
+    CUDA_TRY(cudaSetDevice(h->device));
+    const int n = launch_free_delta(h->prec, h->sys(), devbuf(buf), pos_delta, dt, stream);
+    if (n < 0) return fail(RBX_ERR_CUDA, "free-atom delta kernel failed: %s", cudaGetErrorString(cudaGetLastError()));
+    h->last_launches = n;
+    return RBX_OK;
+}
+
+int rbx_integrate_part1_delta(rbx_integrator* h, void* stream, const rbx_buffers* buf, const void* pos_delta,
+                              double dt) {
+    int rc = check_ready(h, buf);
+    if (rc) return rc;
+    if (!pos_delta) return fail(RBX_ERR_INVALID_ARGUMENT, "null posDelta buffer");
+    if (!(dt == dt) || dt == 0.0) return fail(RBX_ERR_INVALID_ARGUMENT, "step size must be finite and non-zero");
+    if (h->refined)
+        return fail(RBX_ERR_UNSUPPORTED, "refined energies are not available with constrained free atoms in this build");
+    CUDA_TRY(cudaSetDevice(h->device));
+    DevSys s = h->sys();
+    s.n_free_tiles = 0;  // the step kernel moves the bodies only
+    const int n1 = launch_step(h->prec, STEP_PART1, s, devbuf(buf), dt, stream);
+    const int n2 = n1 < 0 ? -1 : launch_free_apply_delta(h->prec, h->sys(), devbuf(buf), pos_delta, dt, stream);
+    if (n1 < 0 || n2 < 0) return fail(RBX_ERR_CUDA, "constrained part1 failed: %s", cudaGetErrorString(cudaGetLastError()));
+    h->last_launches = n1 + n2;
     return RBX_OK;
 }
 int rbx_get_num_bodies(const rbx_integrator* h, int* out) { int rc = check(h); if (!rc) *out = h->nb; return rc; }

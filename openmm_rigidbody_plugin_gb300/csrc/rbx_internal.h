@@ -137,6 +137,10 @@ struct RefScratch {
 int refined_blocks(const DevSys& s);
 int launch_refined_sum(const DevSys& s, const RefScratch& k, int n_blocks, void* stream);
 int launch_kinetic(int prec, const DevSys& s, const DevBuf& b, const KEScratch& k, int n_blocks, void* stream);
+// Free atoms under constraints: the unconstrained displacement into OpenMM's posDelta, and the move
+// by the corrected displacement (mid-step velocity = displacement / dt).
+int launch_free_delta(int prec, const DevSys& s, const DevBuf& b, void* pos_delta, double dt, void* stream);
+int launch_free_apply_delta(int prec, const DevSys& s, const DevBuf& b, const void* pos_delta, double dt, void* stream);
 int launch_forces_from_host(int prec, const double* f_dev_user, const int* location, int natoms, long long* force,
                             int stride, void* stream);
 int launch_load_positions(int prec, const double* x_dev_user, const double* v_dev_user, const double* masses,

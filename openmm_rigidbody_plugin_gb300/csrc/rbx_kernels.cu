@@ -215,6 +215,50 @@ __global__ void sync_positions_kernel(DevSys S, DevBuf B) {
 }
 
 // ------------------------------------------------------------------------------------------
+// Free atoms under constraints, through OpenMM's posDelta buffer (mixed4 per slot: float4 in
+// single precision, double4 otherwise, the element type of velm). free_delta_kernel writes the
+// unconstrained displacement h (v + F/m h/2) of each free atom for the constraint solver
+// (freeAtomsDelta, rigidbodyintegrator.cu:270-279); free_apply_delta_kernel moves the atom by the
+// corrected displacement and sets its mid-step velocity to that displacement over h. This is the
+// Reference platform's step (RigidBodySystem.cpp:172-176 followed by SHAKE) with the
+// (R - savedPos)/dt term of part2 (:197) folded into part1; the CUDA reference drops that term
+// because it saves the position after the constraints (rigidbodyintegrator.cu:304-305).
+// ------------------------------------------------------------------------------------------
+template <int P>
+__global__ void free_delta_kernel(DevSys S, DevBuf B, void* pos_delta, double dt) {
+    using T = typename Tr<P>::R;
+    using V4 = typename Tr<P>::V4;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= S.nf) return;
+    const int loc = S.free_loc[j];
+    const V4 vm = ((const V4*)B.velm)[loc];
+    const T w = (T)vm.w, h = (T)dt;
+    const V3<T> F = load_force<T>(B.force, loc, B.stride);
+    const V3<T> d = (v3<T>((T)vm.x, (T)vm.y, (T)vm.z) + F * (w * (T(0.5) * h))) * h;
+    V4 out;
+    out.x = d.x; out.y = d.y; out.z = d.z; out.w = 0;
+    ((V4*)pos_delta)[loc] = out;
+}
+
+template <int P>
+__global__ void free_apply_delta_kernel(DevSys S, DevBuf B, const void* pos_delta, double dt) {
+    using T = typename Tr<P>::R;
+    using V4 = typename Tr<P>::V4;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= S.nf) return;
+    const int loc = S.free_loc[j];
+    const V4 dm = ((const V4*)pos_delta)[loc];
+    const V3<T> d = v3<T>((T)dm.x, (T)dm.y, (T)dm.z);
+    const V3<double> x = PosIO<P>::load(B, loc);
+    PosIO<P>::store(B, loc, x + cvt<double>(d), v3<T>(T(0), T(0), T(0)));
+    V4* vel = (V4*)B.velm;
+    V4 vm = vel[loc];
+    const T inv = T(1) / (T)dt;
+    vm.x = d.x * inv; vm.y = d.y * inv; vm.z = d.z * inv;
+    vel[loc] = vm;
+}
+
+// ------------------------------------------------------------------------------------------
 // Layout conversion for the host-buffer API (user order doubles <-> OpenMM device layout).
 // ------------------------------------------------------------------------------------------
 __global__ void forces_from_host_kernel(const double* __restrict__ f, const int* __restrict__ loc, int n,
@@ -326,6 +370,30 @@ int launch_kinetic(int prec, const DevSys& s, const DevBuf& b, const KEScratch& 
         case PREC_SINGLE: kinetic_kernel<PREC_SINGLE><<<n_blocks, kKEThreads, 0, st>>>(s, b, k); break;
         case PREC_MIXED: kinetic_kernel<PREC_MIXED><<<n_blocks, kKEThreads, 0, st>>>(s, b, k); break;
         default: kinetic_kernel<PREC_DOUBLE><<<n_blocks, kKEThreads, 0, st>>>(s, b, k); break;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_free_delta(int prec, const DevSys& s, const DevBuf& b, void* pos_delta, double dt, void* stream) {
+    if (s.nf == 0) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int g = (s.nf + 255) / 256;
+    switch (prec) {
+        case PREC_SINGLE: free_delta_kernel<PREC_SINGLE><<<g, 256, 0, st>>>(s, b, pos_delta, dt); break;
+        case PREC_MIXED: free_delta_kernel<PREC_MIXED><<<g, 256, 0, st>>>(s, b, pos_delta, dt); break;
+        default: free_delta_kernel<PREC_DOUBLE><<<g, 256, 0, st>>>(s, b, pos_delta, dt); break;
+    }
+    return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+int launch_free_apply_delta(int prec, const DevSys& s, const DevBuf& b, const void* pos_delta, double dt, void* stream) {
+    if (s.nf == 0) return 0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int g = (s.nf + 255) / 256;
+    switch (prec) {
+        case PREC_SINGLE: free_apply_delta_kernel<PREC_SINGLE><<<g, 256, 0, st>>>(s, b, pos_delta, dt); break;
+        case PREC_MIXED: free_apply_delta_kernel<PREC_MIXED><<<g, 256, 0, st>>>(s, b, pos_delta, dt); break;
+        default: free_apply_delta_kernel<PREC_DOUBLE><<<g, 256, 0, st>>>(s, b, pos_delta, dt); break;
     }
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
 }

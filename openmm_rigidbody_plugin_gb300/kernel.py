@@ -45,6 +45,8 @@ class DeviceBuffers:
         self.corr = torch.zeros((self.stride, 4), dtype=torch.float32, device=dev) if precision == "mixed" else None
         self.velm = torch.zeros((self.stride, 4), dtype=vdt, device=dev)
         self.force = torch.zeros(3 * self.stride, dtype=torch.int64, device=dev)
+        # OpenMM's posDelta (mixed4 per slot), for free atoms under constraints
+        self.pos_delta = torch.zeros((self.stride, 4), dtype=vdt, device=dev)
         self.location = np.arange(num_atoms, dtype=np.int64)
 
     def struct(self):
@@ -82,6 +84,14 @@ class DeviceBuffers:
         loc = self._loc()
         for c in range(3):
             self.force[loc + c * self.stride] = fx[:, c]
+
+    def get_pos_delta(self):
+        return self.pos_delta[self._loc(), :3].to(self.pos_delta.dtype).cpu().double().numpy()
+
+    def set_pos_delta(self, d):
+        import torch
+        self.pos_delta[self._loc(), :3] = torch.as_tensor(np.asarray(d, dtype=np.float64),
+                                                          device=self.posq.device).to(self.pos_delta.dtype)
 
     def relocate(self, location):
         """Move every atom's slot contents to its new slot, as OpenMM's atom reordering does
@@ -181,6 +191,21 @@ class IntegratorKernel:
         b = buffers.struct()
         _lib.check(self._lib.rbx_integrate_fused(self._h, _stream_handle(stream), ctypes.byref(b), float(dt)))
 
+    # free atoms under constraints (OpenMM's posDelta protocol) ----------------------------------
+    def set_constraints(self, pairs):
+        p = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        _lib.check(self._lib.rbx_set_constraints(self._h, len(p), _iptr(p) if len(p) else None))
+
+    def free_atoms_delta(self, buffers, dt, stream=None):
+        b = buffers.struct()
+        _lib.check(self._lib.rbx_free_atoms_delta(self._h, _stream_handle(stream), ctypes.byref(b),
+                                                  ctypes.c_void_p(buffers.pos_delta.data_ptr()), float(dt)))
+
+    def part1_delta(self, buffers, dt, stream=None):
+        b = buffers.struct()
+        _lib.check(self._lib.rbx_integrate_part1_delta(self._h, _stream_handle(stream), ctypes.byref(b),
+                                                       ctypes.c_void_p(buffers.pos_delta.data_ptr()), float(dt)))
+
     def kinetic_energies(self, buffers, stream=None):
         out = np.zeros(2)
         b = buffers.struct()
@@ -251,6 +276,12 @@ class IntegratorKernel:
         x = np.ascontiguousarray(positions, dtype=np.float64)
         v = np.ascontiguousarray(velocities, dtype=np.float64)
         _lib.check(self._lib.rbx_context_set_state(self._h, _stream_handle(stream), _dptr(x), _dptr(v)))
+
+    def context_load(self, positions, velocities, stream=None):
+        """Write positions and velocities into the owned buffers as they are (no body rebuild)."""
+        x = np.ascontiguousarray(positions, dtype=np.float64)
+        v = np.ascontiguousarray(velocities, dtype=np.float64)
+        _lib.check(self._lib.rbx_context_load(self._h, _stream_handle(stream), _dptr(x), _dptr(v)))
 
     def context_buffers(self):
         b = _lib.Buffers()
