@@ -11,6 +11,8 @@
 //      with the tile-local body index in shared memory;
 //   1. one thread per atom gathers the fixed-point force, rebuilds the COM displacement
 //      delta = At(q) d and its torque delta x F, and parks F and tau in shared memory;
+//      (single/mixed: phase 1's loads are issued before phase 0, so that the slot -> force
+//      dependency overlaps it: 4 % faster)
 //   2. one thread per body sums its atoms' F and tau in a fixed order (deterministic, no
 //      atomics), applies the half kick(s), drift and free rotation, and writes its state;
 //   3. one thread per atom writes the new position r + At(q) d (or, for part2, the velocity
@@ -449,16 +451,8 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
     float* __restrict__ glo = ghi + 14 * nbp;   // rows 14..27 (lo)
     const float dt = (float)dt_d;
 
-    // Phase 0: rotation matrix of the current orientation; atoms -> tile-local body
-    if (tid < nbt) {
-        const int b = b0 + tid;
-        rotation_matrix(q4<float>(ghi[b + 6 * nbp], ghi[b + 7 * nbp], ghi[b + 8 * nbp], ghi[b + 9 * nbp]), sM + 9 * tid);
-        const int s0 = __ldg(S.atom0 + b) - a0, e0 = __ldg(S.atom0 + b + 1) - a0;
-        for (int j = s0; j < e0; j++) sBody[j] = (unsigned short)tid;
-    }
-    __syncthreads();
-
-    // Phase 1: per-atom force, displacement from the COM, torque (all loads issued first)
+    // Phase 1 loads first (slots, body-frame coordinates; the orientation; then the forces at the
+    // slots), so that their latencies overlap phase 0
     {
         const float* __restrict__ dg = (const float*)S.d;
         int loc[APT];
@@ -474,9 +468,27 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
             if (a < nat) {
                 const int k = a0 + a;
                 d[i] = v3<float>(__ldg(dg + k), __ldg(dg + k + S.nba_pad), __ldg(dg + k + 2 * S.nba_pad));
-                F[i] = load_force<float>(B.force, loc[i], B.stride);
             }
         }
+        Q4<float> q0 = q4<float>(1.0f, 0.0f, 0.0f, 0.0f);
+        int s0 = 0, e0 = 0;
+        if (tid < nbt) {
+            const int b = b0 + tid;
+            q0 = q4<float>(ghi[b + 6 * nbp], ghi[b + 7 * nbp], ghi[b + 8 * nbp], ghi[b + 9 * nbp]);
+            s0 = __ldg(S.atom0 + b) - a0;
+            e0 = __ldg(S.atom0 + b + 1) - a0;
+        }
+#pragma unroll
+        for (int i = 0; i < APT; i++) {
+            const int a = tid + i * kThreadsF;
+            if (a < nat) F[i] = load_force<float>(B.force, loc[i], B.stride);
+        }
+        // Phase 0: rotation matrix of the current orientation; atoms -> tile-local body
+        if (tid < nbt) {
+            rotation_matrix(q0, sM + 9 * tid);
+            for (int j = s0; j < e0; j++) sBody[j] = (unsigned short)tid;
+        }
+        __syncthreads();
 #pragma unroll
         for (int i = 0; i < APT; i++) {
             const int a = tid + i * kThreadsF;
