@@ -180,21 +180,12 @@ struct ESum {
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
-// One pair term: accumulates the force on i and (energy evaluations) the pair energy, formed in
-// FP32 and summed with compensation. The cutoff test comes first and the neighbour's parameters
-// are read from shared memory only for pairs within it (about 15 % of the candidates of 27 cells).
+// The pair's force on i and (energy evaluations) its energy, formed in FP32 and summed with
+// compensation, for a pair known to be within the cutoff and not excluded.
 template <bool ENERGY>
-__device__ __forceinline__ void pair_term(const FFSys& S, const FFDev& D, float4 xi, float4 pi, float4 xq,
-                                          const float4* __restrict__ pqp, float dx, float dy, float dz, float& fx,
-                                          float& fy, float& fz, ESum& e) {
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    if (r2 >= S.rc2) return;
-    const float4 pq = *pqp;
-    // the atom itself (same slot); ids are compared as integers: as floats they are denormals,
-    // which flush-to-zero arithmetic would make all equal
-    if (__float_as_int(pi.w) == __float_as_int(pq.w)) return;
-    const int body = __float_as_int(pi.z);
-    if (body > 0 && __float_as_int(pq.z) == body) return;
+__device__ __forceinline__ void pair_interact(const FFSys& S, const FFDev& D, float4 xi, float4 pi, float4 xq, float4 pq,
+                                              float dx, float dy, float dz, float r2, float& fx, float& fy, float& fz,
+                                              ESum& e) {
     if (D.fcap > 0.0f && r2 < 1e-8f) return;  // relaxation: coincident atoms have no direction
     const float inv_r2 = 1.0f / r2, inv_r = rsqrtf(r2);
     const float qq = xi.w * xq.w;
@@ -205,6 +196,40 @@ __device__ __forceinline__ void pair_term(const FFSys& S, const FFDev& D, float4
     fy = fmaf(g, dy, fy);
     fz = fmaf(g, dz, fz);
     if (ENERGY) e.add(qq * (inv_r + S.krf * r2 - S.crf) + 4.0f * eps * (s6 * s6 - s6));
+}
+
+// Excluded pairs: the atom itself (same slot) and atoms of the same rigid body. Ids are compared
+// as integers: as floats they are denormals, which flush-to-zero arithmetic would make all equal.
+__device__ __forceinline__ bool excluded(float4 pi, float4 pq) {
+    if (__float_as_int(pi.w) == __float_as_int(pq.w)) return true;
+    const int body = __float_as_int(pi.z);
+    return body > 0 && __float_as_int(pq.z) == body;
+}
+
+// Cell kernel (many warps per SM): the cutoff test first, and the neighbour's parameters read from
+// shared memory only for pairs within it (about 15 % of the candidates of 27 cells).
+template <bool ENERGY>
+__device__ __forceinline__ void pair_term_cutoff_first(const FFSys& S, const FFDev& D, float4 xi, float4 pi, float4 xq,
+                                                       const float4* __restrict__ pqp, float dx, float dy, float dz,
+                                                       float& fx, float& fy, float& fz, ESum& e) {
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (r2 >= S.rc2) return;
+    const float4 pq = *pqp;
+    if (excluded(pi, pq)) return;
+    pair_interact<ENERGY>(S, D, xi, pi, xq, pq, dx, dy, dz, r2, fx, fy, fz, e);
+}
+
+// Single-box kernel (few warps, each thread a long loop): the parameters loaded with the position
+// and the exclusions tested first keep the loop's dependent chain short (measured on 512 waters:
+// 0.19 ms per evaluation against 0.25 ms with the cutoff test first).
+template <bool ENERGY>
+__device__ __forceinline__ void pair_term_exclusions_first(const FFSys& S, const FFDev& D, float4 xi, float4 pi,
+                                                           float4 xq, float4 pq, float dx, float dy, float dz,
+                                                           float& fx, float& fy, float& fz, ESum& e) {
+    if (excluded(pi, pq)) return;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (r2 >= S.rc2) return;
+    pair_interact<ENERGY>(S, D, xi, pi, xq, pq, dx, dy, dz, r2, fx, fy, fz, e);
 }
 
 template <bool ENERGY>
@@ -280,8 +305,8 @@ __global__ void __launch_bounds__(kFC) ff_force_cells(FFDev D, long long* __rest
                             const int m = min(kFC, qe - j0);
                             for (int j = 0; j < m; j++) {
                                 const float4 xq = sx[j];
-                                pair_term<ENERGY>(S, D, xi, pi, xq, sp + j, xi.x - xq.x, xi.y - xq.y, xi.z - xq.z,
-                                                  fx, fy, fz, en);
+                                pair_term_cutoff_first<ENERGY>(S, D, xi, pi, xq, sp + j, xi.x - xq.x, xi.y - xq.y,
+                                                               xi.z - xq.z, fx, fy, fz, en);
                             }
                         }
                     }
@@ -320,7 +345,7 @@ __global__ void __launch_bounds__(kFT) ff_force_box(FFDev D, long long* __restri
                 dx -= S.L * rintf(dx * S.invL);
                 dy -= S.L * rintf(dy * S.invL);
                 dz -= S.L * rintf(dz * S.invL);
-                pair_term<ENERGY>(S, D, xi, pi, xq, sp + j, dx, dy, dz, fx, fy, fz, en);
+                pair_term_exclusions_first<ENERGY>(S, D, xi, pi, xq, sp[j], dx, dy, dz, fx, fy, fz, en);
             }
         }
     }
