@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--bodies", type=int, default=1_000_000)
     p.add_argument("--free", type=int, default=100_000)
     p.add_argument("--e2e-steps", type=int, default=30)
+    p.add_argument("--replan", action="store_true",
+                   help="single: also time rbx_set_atom_locations after OpenMM-style reorderings (key 'replan')")
     p.add_argument("--refined", action="store_true",
                    help="single: refined (shadow) energies on; each fused step also writes the stencil sums")
     p.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -365,7 +367,7 @@ def run_gpu(args, world, rank, local):
     if args.refined:
         refined = {"kinetic": [float(e) for e in k.refined_kinetic_energies(buf, stream)],
                    "potential_refinement": k.potential_energy_refinement(buf, stream)}
-    replan = time_replan(k, buf, s) if not args.refined else None
+    replan = time_replan(k, buf, s) if args.replan else None
     value = world * nb * args.steps / t_dev
     bytes_step = BYTES_PER_BODY[args.precision] * nb + BYTES_PER_BODY_ATOM[args.precision] * nba + BYTES_PER_FREE * nf
     if args.refined:  # stencil sums written by every fused step: 7 values per body, 3 per free atom
