@@ -238,9 +238,19 @@ def cpu_baseline(s, F, args, seconds):
     steps = max(1, min(20000, int(seconds / max(t, 1e-6))))
     t = o.run_fixed_force(0.002, Fs, steps, threads)
     nb = o.num_bodies
+    # one thread, as the Reference platform runs (a smaller sample, about 5 s)
+    sub1 = W.mixed_system(n_bodies=max(1000, int(args.bodies * 0.02)), n_free=int(args.free * 0.02), seed=3)
+    F1 = W.gaussian_forces(sub1.num_atoms, seed=5)
+    o1 = oracle.Oracle(sub1.masses, sub1.body_indices, mode=args.mode, robust=True)
+    o1.setup(sub1.positions, sub1.velocities, F1)
+    t1 = o1.run_fixed_force(0.002, F1, 1, 1)
+    steps1 = max(1, min(20000, int(5.0 / max(t1, 1e-6))))
+    t1 = o1.run_fixed_force(0.002, F1, steps1, 1)
     return {"value": nb * steps / t, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"{nb} bodies + {o.num_free} free atoms of the same mix, {steps} steps "
-                      f"(part1+part2, fixed forces), {t:.1f} s, {threads} threads"}
+                      f"(part1+part2, fixed forces), {t:.1f} s, {threads} threads",
+            "one_thread": {"value": o1.num_bodies * steps1 / t1, "unit": UNIT,
+                           "sample": f"{o1.num_bodies} bodies + {o1.num_free} free atoms, {steps1} steps, {t1:.1f} s"}}
 
 
 def run_reference(args, world, rank):
