@@ -12,6 +12,8 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <memory>
 #include <new>
 #include <string>
 #include <type_traits>
@@ -522,15 +524,24 @@ int replan_device(rbx_integrator* h, const int* location, int nslots) {
 
     const size_t nbp = h->nb_pad, nbap = h->nba_pad, nfp = h->nf_pad;
     const int es = h->prec == PREC_DOUBLE ? 8 : 4;
-    // rows of `count` elements of `ebytes` bytes at stride ld, gathered by idx into a new array
+    // Every array is gathered into a new allocation first; the swaps are applied only when all
+    // gathers are enqueued, so a failure leaves the integrator in its previous plan. The stream is
+    // drained before any allocation touched by a gather is freed.
+    std::vector<std::function<void()>> commit;
+    struct Drain {
+        cudaStream_t st;
+        ~Drain() { cudaStreamSynchronize(st); }
+    } drain{st};
     auto regather = [&](auto& arr, int rows, size_t ld, int count, const int* idx, int ebytes) -> int {
         if (!arr.p || count == 0) return RBX_OK;
-        std::remove_reference_t<decltype(arr)> tmp;
-        if (tmp.alloc(arr.n) != cudaSuccess) return fail(RBX_ERR_CUDA, "cudaMalloc during the re-plan failed");
-        if (launch_gather_rows(tmp.p, arr.p, rows, ld, count, idx, ebytes, st))
+        auto tmp = std::make_shared<std::remove_reference_t<decltype(arr)>>();
+        if (tmp->alloc(arr.n) != cudaSuccess) return fail(RBX_ERR_CUDA, "cudaMalloc during the re-plan failed");
+        if (launch_gather_rows(tmp->p, arr.p, rows, ld, count, idx, ebytes, st))
             return fail(RBX_ERR_CUDA, "re-plan gather failed: %s", cudaGetErrorString(cudaGetLastError()));
-        arr.swap(tmp);
-        old.take(tmp);
+        commit.push_back([&arr, tmp, &old]() {
+            arr.swap(*tmp);
+            old.take(*tmp);
+        });
         return RBX_OK;
     };
     int rc = regather(h->d_state, h->prec == PREC_DOUBLE ? 14 : 28, nbp, nb, idx_body, es);
@@ -544,23 +555,26 @@ int replan_device(rbx_integrator* h, const int* location, int nslots) {
     if (!rc) rc = regather(h->d_bmass, 1, nbap, nba, idx_atom, 8);
     if (!rc && h->d_ref_start.p) {
         // body rows then free-atom rows of one allocation each: gather both parts into a new one
-        DevArray<unsigned char> s2;
-        DevArray<float> o2;
-        if (s2.alloc(h->d_ref_start.n) != cudaSuccess || o2.alloc(h->d_ref_out.n) != cudaSuccess)
+        auto s2 = std::make_shared<DevArray<unsigned char>>();
+        auto o2 = std::make_shared<DevArray<float>>();
+        if (s2->alloc(h->d_ref_start.n) != cudaSuccess || o2->alloc(h->d_ref_out.n) != cudaSuccess)
             return fail(RBX_ERR_CUDA, "cudaMalloc during the re-plan failed");
         unsigned char* fs_old = h->d_ref_start.p + kRefBodyRows * nbp * es;
-        unsigned char* fs_new = s2.p + kRefBodyRows * nbp * es;
-        if (launch_gather_rows(s2.p, h->d_ref_start.p, kRefBodyRows, nbp, nb, idx_body, es, st) ||
+        unsigned char* fs_new = s2->p + kRefBodyRows * nbp * es;
+        if (launch_gather_rows(s2->p, h->d_ref_start.p, kRefBodyRows, nbp, nb, idx_body, es, st) ||
             launch_gather_rows(fs_new, fs_old, 3, nfp, nf, idx_free, es, st) ||
-            launch_gather_rows(o2.p, h->d_ref_out.p, 3, nbp, nb, idx_body, 4, st) ||
-            launch_gather_rows(o2.p + 3 * nbp, h->d_ref_out.p + 3 * nbp, 2, nfp, nf, idx_free, 4, st))
+            launch_gather_rows(o2->p, h->d_ref_out.p, 3, nbp, nb, idx_body, 4, st) ||
+            launch_gather_rows(o2->p + 3 * nbp, h->d_ref_out.p + 3 * nbp, 2, nfp, nf, idx_free, 4, st))
             return fail(RBX_ERR_CUDA, "re-plan gather failed: %s", cudaGetErrorString(cudaGetLastError()));
-        h->d_ref_start.swap(s2);
-        h->d_ref_out.swap(o2);
-        old.take(s2);
-        old.take(o2);
+        commit.push_back([h, s2, o2, &old]() {
+            h->d_ref_start.swap(*s2);
+            h->d_ref_out.swap(*o2);
+            old.take(*s2);
+            old.take(*o2);
+        });
     }
     if (rc) return rc;
+    for (auto& f : commit) f();
     // the plan itself
     h->lib_body.swap(lib_body);
     pack_tiles(h);
