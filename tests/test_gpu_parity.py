@@ -159,6 +159,33 @@ def _mixed_case(seed=3):
     return s, F
 
 
+@pytest.mark.parametrize("prec,size", [("mixed", 1024), ("single", 1024), ("double", 512)])
+def test_largest_body_vs_robust_oracle(rbx, oracle_mod, prec, size):
+    """A body filling a whole tile (1024 atoms in single/mixed, 512 in double), with waters and free
+    atoms around it, against the robust FP64 oracle: 20 steps under sd 50 kJ/mol/nm forces."""
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    rng = np.random.default_rng(31)
+    w = W.water_box(27, seed=3)
+    blob = rng.normal(0, 0.6, (size, 3)) + 5.0
+    masses = np.concatenate([w.masses, rng.uniform(1, 16, size), np.full(7, 39.95)])
+    bidx = np.concatenate([w.body_indices, np.full(size, w.body_indices.max() + 1), np.zeros(7, dtype=int)])
+    R = np.concatenate([w.positions, blob, rng.uniform(0, 3, (7, 3))])
+    V = rng.normal(0, 0.3, R.shape)
+    F = W.gaussian_forces(len(masses), seed=8, sd=50.0)
+    k, buf = make(rbx, masses, bidx, R, V, 0, prec)
+    buf.set_forces(F)
+    o = oracle_mod.Oracle(masses, bidx, mode=0, robust=True)
+    o.setup(R, V, F)
+    for _ in range(20):
+        k.part1(buf, 0.002)
+        k.part2(buf, 0.002)
+        o.part1(0.002, F)
+        o.part2(0.002, F)
+    tol = {"double": 1e-9, "mixed": 1e-6, "single": 2e-4}[prec]
+    assert rel_err(buf.get_positions(), o.R) < tol
+    assert rel_err(buf.get_velocities(), o.V) < 10 * tol
+
+
 @pytest.mark.parametrize("prec", ["double", "mixed"])
 @pytest.mark.parametrize("mode", [0, 10])
 def test_mixed_body_types_vs_robust_oracle(rbx, oracle_mod, mode, prec):

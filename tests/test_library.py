@@ -69,6 +69,26 @@ def test_massless_body_atom_rejected(lib):
     assert b"no mass" in lib.rbx_last_error()
 
 
+@pytest.mark.parametrize("prec,limit", [(1, 1024), (0, 1024), (2, 512)])
+def test_body_larger_than_a_tile_rejected(lib, prec, limit):
+    """A body must fit one tile (1024 atoms in single/mixed, 512 in double): RBX_ERR_UNSUPPORTED,
+    before any device call."""
+    rc, _ = _create(lib, np.ones(limit + 1), np.ones(limit + 1, dtype=np.int32), prec=prec)
+    assert rc == 4
+    assert b"exceeds" in lib.rbx_last_error()
+
+
+def test_new_entry_points_reject_a_null_handle(lib):
+    """Constraints, refined energies and the posDelta steps validate their handle first."""
+    pairs = np.array([0, 1], dtype=np.int32)
+    assert lib.rbx_set_constraints(None, 1, pairs.ctypes.data_as(ctypes.POINTER(ctypes.c_int))) == 1
+    assert lib.rbx_set_compute_refined_energies(None, 1) == 1
+    out = np.zeros(2)
+    assert lib.rbx_refined_kinetic_energies(None, None, None, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))) == 1
+    assert lib.rbx_free_atoms_delta(None, None, None, None, 0.002) == 1
+    assert lib.rbx_integrate_part1_delta(None, None, None, None, 0.002) == 1
+
+
 def test_null_handle_calls_fail_cleanly(lib):
     out = ctypes.c_int()
     assert lib.rbx_get_num_bodies(None, ctypes.byref(out)) == 1
