@@ -77,6 +77,8 @@ def parse():
     p.add_argument("--systems", type=int, default=4096, help="batched: number of systems")
     p.add_argument("--relax-steps", type=int, default=400, help="batched/water: relaxation before dynamics")
     p.add_argument("--graph-steps", type=int, default=50, help="batched/water: steps per captured CUDA graph")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="batched/water: keep --graph-steps and the default cell-kernel block size")
     p.add_argument("--plain-systems", type=int, default=32, help="batched: systems run one per launch")
     p.add_argument("--pbodies", type=int, default=8192, help="precision: near-degenerate bodies")
     p.add_argument("--pwaters", type=int, default=20000, help="precision: waters")
@@ -530,6 +532,12 @@ def run_batched(args, world, rank, local):
     setup_s = time.perf_counter() - t0
     dof = b.num_dof
     b.step(max(args.warmup, 3), dt)
+    # the autotuner picks the schedule on this batch (and restores its state exactly)
+    tuning = b.autotune(dt, trial_steps=3) if not args.no_autotune else None
+    if tuning:
+        name = name.replace(f"{args.graph_steps} steps per captured CUDA graph",
+                            f"autotuned schedule: {tuning['graph_steps']} steps per captured CUDA graph, "
+                            f"{tuning['cell_threads']}-thread cell force blocks")
     x0, v0 = b.get_state()
     b.set_state(x0, v0)  # both arms start here
     e_pre = b.energies()
@@ -620,7 +628,7 @@ def run_batched(args, world, rank, local):
            "config": {"workload": name, "systems_per_gpu": len(systems), "bodies_per_gpu": nb, "atoms_per_gpu": na,
                       "relax_steps": args.relax_steps, "setup_seconds": setup_s,
                       "l2": "working set > 129 MB L2" if na * 120 > 129e6 else "working set fits in L2",
-                      "parallelism": f"{world} independent replicas"},
+                      "parallelism": f"{world} independent replicas", "autotune": tuning},
            "energy_drift": drift, "plain": plain,
            "speedup_vs_plain": (value / world / plain["value"]) if plain else None,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -79,6 +79,8 @@ SIGNATURES = [
     ("rbx_batch_step", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double]),
     ("rbx_batch_relax", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("rbx_batch_energies", ctypes.c_int, [_vp, _vp, _dp]),
+    ("rbx_batch_autotune", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_int, _ip]),
+    ("rbx_batch_set_tuning", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     ("rbx_batch_forces", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_batch_get_num_dof", ctypes.c_int, [_vp, _ip]),
     ("rbx_batch_set_graph_steps", ctypes.c_int, [_vp, ctypes.c_int]),

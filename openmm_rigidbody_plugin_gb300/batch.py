@@ -156,6 +156,17 @@ class BatchedSystems:
     def set_graph_steps(self, k):
         _lib.check(self._lib.rbx_batch_set_graph_steps(self._h, int(k)))
 
+    def autotune(self, dt=0.002, trial_steps=3, stream=None):
+        """Pick the cell force kernel's block size and the steps per captured graph by timing them on
+        this batch; the state is restored exactly afterwards. Returns the choice."""
+        out = np.zeros(2, dtype=np.int32)
+        _lib.check(self._lib.rbx_batch_autotune(self._h, _stream(stream), float(dt), int(trial_steps),
+                                                out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return {"cell_threads": int(out[0]), "graph_steps": int(out[1])}
+
+    def set_tuning(self, cell_threads, graph_steps):
+        _lib.check(self._lib.rbx_batch_set_tuning(self._h, int(cell_threads), int(graph_steps)))
+
     def set_timing(self, on):
         _lib.check(self._lib.rbx_batch_set_timing(self._h, int(bool(on))))
 

@@ -324,6 +324,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     D.e_atom = b->d_e_atom.p;
     D.energy = b->d_energy.p;
     D.fcap = 0.0f;
+    D.cell_threads = 128;
     D.n_mc = (int)mc_cell.size();
     D.n_sc = (int)sc_sys.size();
     D.mc_cell = b->d_mc_cell.p;
@@ -501,6 +502,98 @@ int rbx_batch_get_num_dof(rbx_batch* b, int* dof) {
     if (rc) return rc;
     if (b->dof.empty()) return set_error(RBX_ERR_STATE, "degrees of freedom are known after rbx_batch_set_state");
     std::copy(b->dof.begin(), b->dof.end(), dof);
+    return RBX_OK;
+}
+
+int rbx_batch_autotune(rbx_batch* b, void* stream, double dt, int trial_steps, int* chosen) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
+    if (trial_steps < 1) return set_error(RBX_ERR_INVALID_ARGUMENT, "trial_steps must be >= 1");
+    if (!(dt == dt) || dt == 0.0) return set_error(RBX_ERR_INVALID_ARGUMENT, "step size must be finite and non-zero");
+    BATCH_TRY(cudaSetDevice(b->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    // the exact state, restored after the trials (they only change how the work is scheduled)
+    int nb = 0;
+    if ((rc = rbx_get_num_bodies(b->integ, &nb))) return rc;
+    std::vector<double> body((size_t)nb * 14 + 1), x((size_t)3 * b->natoms), v((size_t)3 * b->natoms);
+    if ((rc = rbx_batch_get_body_state(b, body.data())) || (rc = rbx_batch_get_state(b, stream, x.data(), v.data())))
+        return rc;
+    const bool timing = b->timing;
+    b->timing = false;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    BATCH_TRY(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return set_error(RBX_ERR_CUDA, "cudaEventCreate failed");
+    }
+    // milliseconds per step of `n` steps after one untimed call of the same length
+    auto per_step = [&](int n, float& ms) -> int {
+        int r = rbx_batch_step(b, stream, n, dt);
+        if (!r && cudaEventRecord(e0, st) != cudaSuccess) r = set_error(RBX_ERR_CUDA, "event record failed");
+        if (!r) r = rbx_batch_step(b, stream, n, dt);
+        if (!r && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                   cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+            r = set_error(RBX_ERR_CUDA, "event timing failed");
+        ms /= (float)n;
+        return r;
+    };
+    const int k0 = b->graph_k;
+    int best_ct = b->ff.cell_threads, best_k = k0;
+    float best = 0.0f, ms = 0.0f;
+    // 1. block size of the cell force kernel, direct launches
+    b->graph_k = 0;
+    b->drop_graph();
+    const int cts[3] = {64, 128, 256};
+    for (int i = 0; i < 3 && !rc; i++) {
+        if (!b->ff.n_mc && cts[i] != best_ct) continue;
+        b->ff.cell_threads = cts[i];
+        if ((rc = per_step(trial_steps, ms))) break;
+        if (i == 0 || ms < best || !b->ff.n_mc) {
+            best = ms;
+            best_ct = cts[i];
+        }
+    }
+    b->ff.cell_threads = best_ct;
+    // 2. steps per captured graph, where launch overhead matters (steps under 1 ms)
+    if (!rc && best < 1.0f) {
+        const int ks[3] = {0, 10, 50};
+        float best_g = 0.0f;
+        for (int i = 0; i < 3 && !rc; i++) {
+            b->graph_k = ks[i];
+            b->drop_graph();
+            if ((rc = per_step(ks[i] ? 2 * ks[i] + 1 : trial_steps, ms))) break;
+            if (i == 0 || ms < best_g) {
+                best_g = ms;
+                best_k = ks[i];
+            }
+        }
+    } else if (!rc) {
+        best_k = k0 > 0 ? k0 : 50;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->graph_k = best_k;
+    b->drop_graph();
+    b->timing = timing;
+    const int rc2 = rbx_batch_restore(b, stream, body.data(), x.data(), v.data());
+    if (rc) return rc;
+    if (rc2) return rc2;
+    if (chosen) {
+        chosen[0] = best_ct;
+        chosen[1] = best_k;
+    }
+    return RBX_OK;
+}
+
+int rbx_batch_set_tuning(rbx_batch* b, int cell_threads, int graph_steps) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (cell_threads != 64 && cell_threads != 128 && cell_threads != 256)
+        return set_error(RBX_ERR_INVALID_ARGUMENT, "cell kernel block size must be 64, 128 or 256");
+    if ((rc = rbx_batch_set_graph_steps(b, graph_steps))) return rc;
+    if (cell_threads != b->ff.cell_threads) b->drop_graph();
+    b->ff.cell_threads = cell_threads;
     return RBX_OK;
 }
 

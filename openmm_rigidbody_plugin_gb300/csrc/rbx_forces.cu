@@ -165,9 +165,7 @@ __global__ void ff_gather(FFDev D, DevBuf B, int prec) {
     D.cpar[p] = make_float4(q.y, q.z, q.w, __int_as_float(slot));
 }
 
-constexpr int kFT = 64;   // threads of a single-box force block; also its staged chunk of atoms
-constexpr int kFC = 128;  // threads of a cell block (one pass for cells of up to 128 atoms: a cell
-                          // of at least a cutoff per edge holds 73 or more atoms at liquid density)
+constexpr int kFT = 64;  // threads of a single-box force block; also its staged chunk of atoms
 
 // Compensated FP32 accumulator (Knuth's two-sum): the running sum keeps its rounding error in `lo`.
 struct ESum {
@@ -256,11 +254,13 @@ __device__ __forceinline__ void store_force(const FFDev& D, long long* __restric
     if (ENERGY) D.e_atom[p] = 0.5 * e.value();
 }
 
-// Multi-cell boxes: one block per cell. The block's threads take the cell's atoms (128 at a time);
-// each of the 27 neighbour cells is staged in shared memory, 128 atoms at a time, with its periodic
+// Multi-cell boxes: one block per cell. The block's kFC threads take the cell's atoms (kFC at a
+// time: 64, 128 or 256, chosen by the batch's autotuner; a cell of at least a cutoff per edge
+// holds 73 or more atoms at liquid density); each of the 27 neighbour cells is staged in shared
+// memory, kFC atoms at a time, with its periodic
 // image shift applied once (exact for pairs within the cutoff: the cell edge is at least the
 // cutoff and there are at least three cells per edge).
-template <bool ENERGY>
+template <bool ENERGY, int kFC>
 __global__ void __launch_bounds__(kFC) ff_force_cells(FFDev D, long long* __restrict__ force, int stride) {
     __shared__ float4 sx[kFC], sp[kFC];
     const int c = D.mc_cell[blockIdx.x];
@@ -397,8 +397,20 @@ int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* 
     n++;
     long long* f = const_cast<long long*>(B.force);
     if (D.n_mc) {
-        if (energy) ff_force_cells<true><<<D.n_mc, kFC, 0, st>>>(D, f, B.stride);
-        else ff_force_cells<false><<<D.n_mc, kFC, 0, st>>>(D, f, B.stride);
+        // block size: results do not depend on it (each atom's pairs are summed in the same order)
+        switch (D.cell_threads) {
+            case 64:
+                if (energy) ff_force_cells<true, 64><<<D.n_mc, 64, 0, st>>>(D, f, B.stride);
+                else ff_force_cells<false, 64><<<D.n_mc, 64, 0, st>>>(D, f, B.stride);
+                break;
+            case 256:
+                if (energy) ff_force_cells<true, 256><<<D.n_mc, 256, 0, st>>>(D, f, B.stride);
+                else ff_force_cells<false, 256><<<D.n_mc, 256, 0, st>>>(D, f, B.stride);
+                break;
+            default:
+                if (energy) ff_force_cells<true, 128><<<D.n_mc, 128, 0, st>>>(D, f, B.stride);
+                else ff_force_cells<false, 128><<<D.n_mc, 128, 0, st>>>(D, f, B.stride);
+        }
         n++;
     }
     if (D.n_sc) {

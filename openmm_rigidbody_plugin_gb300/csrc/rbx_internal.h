@@ -105,6 +105,7 @@ struct FFDev {
     double* e_atom;       // [n_int] half pair-energy sums (energy evaluations)
     double* energy;       // [S] potential energy per system (kJ/mol)
     float fcap;           // > 0: each atom's force is scaled down to at most this magnitude
+    int cell_threads;     // block size of the cell kernel: 64, 128 (default) or 256
     // work lists of the force kernels (static): every cell of the multi-cell boxes with its
     // system, and every 64-atom chunk (start in the interacting-atom list) of the single-cell boxes
     int n_mc, n_sc;

@@ -143,3 +143,26 @@ def test_water_full_steps_track_the_fp64_oracle(B, oracle_mod):
     assert abs(e_gpu[0] - e_orc[0]) < 1e-5 * abs(e_orc[0])  # after 10 steps: same state
     drift_gpu, drift_orc = abs(e_gpu[-1] - e_gpu[0]), abs(e_orc[-1] - e_orc[0])
     assert drift_gpu <= 1.25 * drift_orc + 1.0, (e_gpu, e_orc)
+
+
+def test_autotune_changes_no_result(B):
+    """The autotuner times schedules on the batch and restores its state exactly; every block size
+    of the cell kernel and every graph run length gives the same trajectory bit for bit."""
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    systems = W.batch_systems(6, lo=300, hi=2500, seed=14)
+    runs = []
+    for how in ("plain", "autotuned", 64, 256):
+        b = B.BatchedSystems.from_systems(systems, relax_steps=50)
+        x0, v0 = b.get_state()
+        b.set_state(x0, v0)
+        b.step(3, 0.002)
+        if how == "autotuned":
+            choice = b.autotune(0.002, trial_steps=2)
+            assert choice["cell_threads"] in (64, 128, 256) and choice["graph_steps"] in (0, 10, 50)
+        elif how != "plain":
+            b.set_tuning(how, 10)
+        b.step(25, 0.002)
+        runs.append((b.get_state(), b.energies()))
+    for (x, v), e in runs[1:]:
+        assert np.array_equal(x, runs[0][0][0]) and np.array_equal(v, runs[0][0][1])
+        assert np.array_equal(e, runs[0][1])
