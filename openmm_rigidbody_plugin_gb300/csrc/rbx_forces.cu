@@ -318,19 +318,24 @@ __global__ void __launch_bounds__(kFC) ff_force_cells(FFDev D, long long* __rest
 }
 
 // Single-cell boxes (fewer than three cutoffs across): one block per 64 atoms of the box, all
-// atoms of the box streamed through shared memory, minimum image per pair.
+// atoms of the box streamed through shared memory, minimum image per pair. Each atom has kFK
+// threads (consecutive lanes), each taking every kFK-th staged neighbour; their partial sums are
+// combined by a fixed butterfly of shuffles, so the order of every sum is fixed. Small boxes are
+// latency bound: kFK threads per atom give kFK times the parallelism and 1/kFK of the loop.
+constexpr int kFK = 8;
 template <bool ENERGY>
-__global__ void __launch_bounds__(kFT) ff_force_box(FFDev D, long long* __restrict__ force, int stride) {
-    __shared__ float4 sx[kFT], sp[kFT];
+__global__ void __launch_bounds__(kFT * kFK) ff_force_box(FFDev D, long long* __restrict__ force, int stride) {
+    constexpr int NT = kFT * kFK;  // threads, and staged neighbours per barrier pair
+    __shared__ float4 sx[NT], sp[NT];
     const FFSys S = D.sys[D.sc_sys[blockIdx.x]];
-    const int t = threadIdx.x;
-    const int p = D.sc_i0[blockIdx.x] + t;
+    const int t = threadIdx.x, k = t % kFK;
+    const int p = D.sc_i0[blockIdx.x] + t / kFK;
     const bool mine = p < S.i1;
     const float4 xi = mine ? D.cpos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 pi = mine ? D.cpar[p] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
     float fx = 0.f, fy = 0.f, fz = 0.f;
     ESum en;
-    for (int j0 = S.i0; j0 < S.i1; j0 += kFT) {
+    for (int j0 = S.i0; j0 < S.i1; j0 += NT) {
         __syncthreads();
         if (j0 + t < S.i1) {
             sx[t] = D.cpos[j0 + t];
@@ -338,8 +343,8 @@ __global__ void __launch_bounds__(kFT) ff_force_box(FFDev D, long long* __restri
         }
         __syncthreads();
         if (mine) {
-            const int m = min(kFT, S.i1 - j0);
-            for (int j = 0; j < m; j++) {
+            const int m = min(NT, S.i1 - j0);
+            for (int j = k; j < m; j += kFK) {
                 const float4 xq = sx[j];
                 float dx = xi.x - xq.x, dy = xi.y - xq.y, dz = xi.z - xq.z;
                 dx -= S.L * rintf(dx * S.invL);
@@ -349,7 +354,17 @@ __global__ void __launch_bounds__(kFT) ff_force_box(FFDev D, long long* __restri
             }
         }
     }
-    if (mine) store_force<ENERGY>(D, force, stride, p, pi, fx, fy, fz, en);
+#pragma unroll
+    for (int o = kFK / 2; o > 0; o >>= 1) {
+        fx += __shfl_xor_sync(0xffffffffu, fx, o);
+        fy += __shfl_xor_sync(0xffffffffu, fy, o);
+        fz += __shfl_xor_sync(0xffffffffu, fz, o);
+        if (ENERGY) {
+            en.hi += __shfl_xor_sync(0xffffffffu, en.hi, o);
+            en.lo += __shfl_xor_sync(0xffffffffu, en.lo, o);
+        }
+    }
+    if (mine && k == 0) store_force<ENERGY>(D, force, stride, p, pi, fx, fy, fz, en);
 }
 
 __global__ void ff_energy(FFDev D) {
@@ -414,8 +429,8 @@ int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* 
         n++;
     }
     if (D.n_sc) {
-        if (energy) ff_force_box<true><<<D.n_sc, kFT, 0, st>>>(D, f, B.stride);
-        else ff_force_box<false><<<D.n_sc, kFT, 0, st>>>(D, f, B.stride);
+        if (energy) ff_force_box<true><<<D.n_sc, kFT * kFK, 0, st>>>(D, f, B.stride);
+        else ff_force_box<false><<<D.n_sc, kFT * kFK, 0, st>>>(D, f, B.stride);
         n++;
     }
     if (energy) {
