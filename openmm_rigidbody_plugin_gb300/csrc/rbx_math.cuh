@@ -210,12 +210,30 @@ template <class T> RBX_HD T omega_term(T x, T n, T m) {
     return (T(-1) / T(3)) * n * x * x2 * carlson_rj(T(1) - x2, T(1) - m * x2, T(1), T(1) + n * x2);
 }
 
+// sin x and cos x. Rotation angles of one step are small: for |x| <= 1/4 the Maclaurin series to
+// x^13 and x^14 (truncation below 3e-21 relative, under FP64 rounding) replaces the general-range
+// functions, whose argument reduction is costly on GB300's narrow FP64 pipe; larger arguments take
+// sincos.
+template <class T> RBX_HD void sin_cos(T x, T& s, T& c) {
+    const T x2 = x * x;
+    if (x2 <= T(0.0625)) {
+        s = x * (T(1) + x2 * (T(-1) / T(6) + x2 * (T(1) / T(120) + x2 * (T(-1) / T(5040) + x2 * (T(1) / T(362880) +
+              x2 * (T(-1) / T(39916800) + x2 * (T(1) / T(6227020800))))))));
+        c = T(1) + x2 * (T(-1) / T(2) + x2 * (T(1) / T(24) + x2 * (T(-1) / T(720) + x2 * (T(1) / T(40320) +
+              x2 * (T(-1) / T(3628800) + x2 * (T(1) / T(479001600) + x2 * (T(-1) / T(87178291200))))))));
+        return;
+    }
+    s = sin(x);
+    c = cos(x);
+}
+
 // Rotation about principal axis k by the angle pi implies (RigidBody.cpp:189-214).
 template <class T> RBX_HD void uniaxial(int k, V3<T> invI, Q4<T>& q, Q4<T>& pi, T dt) {
     Q4<T> Bq = qBk(k, q);
     T ik = k == 0 ? invI.x : (k == 1 ? invI.y : invI.z);
     T phi = T(0.25) * dot(pi, Bq) * dt * ik;
-    T s = sin(phi), c = cos(phi);
+    T s, c;
+    sin_cos(phi, s, c);
     Q4<T> Bpi = qBk(k, pi);
     q = q * c + Bq * s;
     pi = pi * c + Bpi * s;
@@ -249,18 +267,23 @@ template <class T> RBX_HD void symmetric_top_rotation(int k, T invIp, T invIk, V
         V3<T> w = mul(invI, L);
         T wn = sqrt(dot(w, w));
         if (wn > T(0)) {
-            T a = T(0.5) * wn * dt, s = sin(a) / wn;
-            r = q4<T>(cos(a), w.x * s, w.y * s, w.z * s);
+            T a = T(0.5) * wn * dt, sa, ca;
+            sin_cos(a, sa, ca);
+            const T s = sa / wn;
+            r = q4<T>(ca, w.x * s, w.y * s, w.z * s);
         }
     } else {
         T Ln = sqrt(dot(L, L));
         if (Ln > T(0)) {
-            T a = T(0.5) * Ln * invIp * dt, s = sin(a) / Ln;
-            Q4<T> r1 = q4<T>(cos(a), L.x * s, L.y * s, L.z * s);
+            T a = T(0.5) * Ln * invIp * dt, sa, ca;
+            sin_cos(a, sa, ca);
+            const T s = sa / Ln;
+            Q4<T> r1 = q4<T>(ca, L.x * s, L.y * s, L.z * s);
             T Lk = k == 0 ? L.x : L.z;
             T b = T(0.5) * (invIk - invIp) * Lk * dt;
-            T sb = sin(b);
-            Q4<T> r2 = k == 0 ? q4<T>(cos(b), sb, T(0), T(0)) : q4<T>(cos(b), T(0), T(0), sb);
+            T sb, cb;
+            sin_cos(b, sb, cb);
+            Q4<T> r2 = k == 0 ? q4<T>(cb, sb, T(0), T(0)) : q4<T>(cb, T(0), T(0), sb);
             r = qmul(r1, r2);
         }
     }
@@ -332,7 +355,8 @@ template <class T> RBX_HD void exact_rotation_asymmetric(V3<T> I, V3<T> invI, Q4
     }
     dF *= T(1) + eta;
     T theta = (Lsq * (u - u0) + r3 * dF) / (T(2) * L * I.x * wp);
-    T ct = cos(theta), st = sin(theta);
+    T ct, st;
+    sin_cos(theta, st, ct);
     Q4<T> z = q4<T>(Iw.z * ct + (-Iw.y) * st, Iw.y * ct + Iw.z * st, (L - Iw.x) * ct + T(0) * st,
                     T(0) * ct + (L - Iw.x) * st);
     // q <- q (x) conj(z0) (x) z, written as z <z0,q> + C(z, Ct(z0, q)) (RigidBody.cpp:305)
