@@ -2,7 +2,9 @@
 
 The bounds below sit above values measured on a GB300 (in brackets), with margin:
   free rotation of 512 waters, exact rotation (mode 0), 1000 steps of 2 fs, no forces:
-    relative change of the total kinetic energy   double 1e-13 [4e-15], mixed 1e-7 [1.3e-8]
+    relative change of the total kinetic energy   double 1e-13, mixed 1e-7 [1.3e-8]
+                                                  (double: the increment-form exact rotation; 4e-14
+                                                  for 512 such bodies in FP64 on the host)
     | |q| - 1 |                                   double 1e-13 [2e-16], mixed 1e-12 [4e-15]
     relative change of intra-body distances       double 1e-12 [5e-15], mixed 1e-6 [1.6e-7],
                                                   single 1e-5 [2.9e-6] (positions in FP32)
