@@ -18,8 +18,8 @@
 //   3. one thread per atom writes the new position r + At(q) d (or, for part2, the velocity
 //      v + omega x delta) to its device slot.
 // Free atoms live in separate tiles of the same launch (velocity Verlet).
-// step_kernel_d runs double precision in FP64 throughout (the reference formulas, the parity
-// anchor). step_kernel_f runs single and mixed precision on the FP32 pipe: float-float body
+// step_kernel_d runs double precision in FP64 throughout (the exact rotation in increment form,
+// rbx_math.cuh). step_kernel_f runs single and mixed precision on the FP32 pipe: float-float body
 // state, FP32 rotation increments (rbx_fast.cuh), FP32 per-atom work.
 #pragma once
 
