@@ -13,6 +13,8 @@ of step n+1) over all bodies and free atoms with every input resident in HBM; th
   e2e     the same metric through the host-buffer C ABI call (rbx_step_host): per step the
           forces go host->device from pinned memory and positions and velocities come back
   roofline  algorithmic bytes of the step kernel / its average launch time vs measured HBM peak
+  e2e.host_link  the same bytes by plain pinned copies (both directions at once): the e2e step's
+          bound, since the host link is far slower than HBM
   cpu_baseline  the CPU port of the reference integrator (oracle) on the machine's host cores
 
 --impl reference times the CPU implementation of the same step (the oracle port of the
@@ -133,6 +135,45 @@ def peaks():
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def host_link(h2d, d2h, device, reps=10):
+    """The host-link bound of an e2e step: the same bytes moved by plain pinned-memory copies
+    (cudaMemcpyAsync through torch), host->device and device->host each alone and both at once on
+    two streams, timed with CUDA events. The e2e step cannot beat `copies_both_ms`."""
+    import torch
+    dev_in = torch.empty(h2d, dtype=torch.uint8, device=device)
+    dev_out = torch.zeros(d2h, dtype=torch.uint8, device=device)
+    h_in = torch.zeros(h2d, dtype=torch.uint8).pin_memory()
+    h_out = torch.empty(d2h, dtype=torch.uint8).pin_memory()
+    s_in, s_out = torch.cuda.Stream(device), torch.cuda.Stream(device)
+
+    def run(which):
+        cur = torch.cuda.current_stream(device)
+        s_in.wait_stream(cur)
+        s_out.wait_stream(cur)
+        if which != "out":
+            with torch.cuda.stream(s_in):
+                dev_in.copy_(h_in, non_blocking=True)
+        if which != "in":
+            with torch.cuda.stream(s_out):
+                h_out.copy_(dev_out, non_blocking=True)
+        cur.wait_stream(s_in)
+        cur.wait_stream(s_out)
+
+    ms = {}
+    for which in ("in", "out", "both"):
+        for _ in range(3):
+            run(which)
+        torch.cuda.synchronize(device)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            run(which)
+        b.record()
+        b.synchronize()
+        ms[which] = a.elapsed_time(b) / reps
+    return {"h2d_gbs": h2d / ms["in"] / 1e6, "d2h_gbs": d2h / ms["out"] / 1e6, "copies_both_ms": ms["both"]}
 
 
 def ncu_traffic(mode, precision, bodies):
@@ -413,6 +454,11 @@ def run_gpu(args, world, rank, local):
            "d2h_bytes_per_step": int(2 * s.num_atoms * 3 * 8),
            "call": "rbx_step_host_async per step (forces in, one step = part1 + part2, positions and velocities "
                    "out, pinned host arrays), steps pipelined, rbx_step_host_wait at the end"}
+    link = host_link(e2e["h2d_bytes_per_step"], e2e["d2h_bytes_per_step"], local)
+    link["e2e_ms_per_step"] = 1e3 * t_e2e
+    link["frac"] = link["copies_both_ms"] / link["e2e_ms_per_step"]
+    link["what"] = "the same bytes by plain pinned copies, both directions at once: the bound of the e2e step"
+    e2e["host_link"] = link
 
     if rank != 0:
         return

@@ -17,7 +17,8 @@
 //      atomics), applies the half kick(s), drift and free rotation, and writes its state;
 //   3. one thread per atom writes the new position r + At(q) d (or, for part2, the velocity
 //      v + omega x delta) to its device slot.
-// Free atoms live in separate tiles of the same launch (velocity Verlet).
+// Free atoms live in separate tiles of the same launch (velocity Verlet), interleaved with the
+// body tiles (block_tile).
 // step_kernel_d runs double precision in FP64 throughout (the exact rotation in increment form,
 // rbx_math.cuh). step_kernel_f runs single and mixed precision on the FP32 pipe: float-float body
 // state, FP32 rotation increments (rbx_fast.cuh), FP32 per-atom work.
@@ -186,6 +187,21 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
     vel[loc] = vm;
 }
 
+// Tile of this block: the body tile (>= 0) or -1 - the free-atom tile. Free-atom tiles are spread
+// evenly over the grid (every s-th block, s = floor(tiles / free-atom tiles)) rather than placed
+// after the body tiles: in mixed precision their velocity arithmetic is FP64 (OpenMM's velm), and
+// GB300's narrow FP64 pipe turned them into a tail at the end of the grid (100,000 free atoms cost
+// 15 us of a 0.144 ms step, for 2 % of its bytes). Interleaved, that work overlaps the body tiles'
+// memory traffic. The mapping is a bijection onto [0, body tiles) and [0, free-atom tiles).
+__device__ __forceinline__ int block_tile(const DevSys& S) {
+    const int i = (int)blockIdx.x, nf = S.n_free_tiles;
+    if (nf == 0) return i;
+    const int s = (S.n_body_tiles + nf) / nf;
+    const int j = i / s;
+    if (i % s == s - 1 && j < nf) return -1 - j;
+    return i - min(nf, (i + 1) / s);
+}
+
 // Shared-memory carve-up common to both step kernels.
 template <class A> struct StepSmem {
     A *sF, *sT, *sX, *sQ, *sW;
@@ -291,15 +307,16 @@ template <int KIND, bool EXACT, bool REF>
 __global__ void __launch_bounds__(kThreads) step_kernel_d(DevSys S, DevBuf B, double dt) {
     constexpr int P = PREC_DOUBLE;
     constexpr int TA = kTileAtomsD, TB = kTileBodies;
-    if ((int)blockIdx.x >= S.n_body_tiles) {
-        free_atom_tile<P, KIND, REF>(S, B, dt, (int)blockIdx.x - S.n_body_tiles);
+    const int tile = block_tile(S);
+    if (tile < 0) {
+        free_atom_tile<P, KIND, REF>(S, B, dt, -1 - tile);
         return;
     }
     extern __shared__ __align__(16) unsigned char smem[];
     StepSmem<double> sm;
     sm.carve<TA, TB>(smem);
     const int tid = threadIdx.x;
-    const int b0 = __ldg(S.tile_body0 + blockIdx.x), b1 = __ldg(S.tile_body0 + blockIdx.x + 1);
+    const int b0 = __ldg(S.tile_body0 + tile), b1 = __ldg(S.tile_body0 + tile + 1);
     const int nbt = b1 - b0;
     const int a0 = __ldg(S.atom0 + b0), nat = __ldg(S.atom0 + b1) - a0;
     const int nbp = S.nb_pad;
@@ -437,8 +454,9 @@ template <int P, int KIND, bool EXACT, bool REF>
 __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B, double dt_d) {
     constexpr int TA = kTileAtomsF;
     constexpr int APT = TA / kThreadsF;
-    if ((int)blockIdx.x >= S.n_body_tiles) {
-        free_atom_tile<P, KIND, REF>(S, B, dt_d, (int)blockIdx.x - S.n_body_tiles);
+    const int tile = block_tile(S);
+    if (tile < 0) {
+        free_atom_tile<P, KIND, REF>(S, B, dt_d, -1 - tile);
         return;
     }
     extern __shared__ __align__(16) float fsm[];
@@ -449,7 +467,7 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
     float* sW = fsm + FSmem::SW;
     unsigned short* sBody = (unsigned short*)(fsm + FSmem::SB);
     const int tid = threadIdx.x;
-    const int b0 = __ldg(S.tile_body0 + blockIdx.x), b1 = __ldg(S.tile_body0 + blockIdx.x + 1);
+    const int b0 = __ldg(S.tile_body0 + tile), b1 = __ldg(S.tile_body0 + tile + 1);
     const int nbt = b1 - b0;
     const int a0 = __ldg(S.atom0 + b0), nat = __ldg(S.atom0 + b1) - a0;
     const int nbp = S.nb_pad;
