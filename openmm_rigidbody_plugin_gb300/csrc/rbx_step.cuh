@@ -26,6 +26,8 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "rbx_fast.cuh"
 #include "rbx_internal.h"
 #include "rbx_math.cuh"
@@ -710,14 +712,21 @@ template <int KIND, bool EXACT, bool REF> struct StepKernel<PREC_DOUBLE, KIND, E
 
 template <int P, int KIND, bool EXACT, bool REF>
 int launch_step_t(const DevSys& s, const DevBuf& b, double dt, cudaStream_t stream) {
-    static bool configured = false;
     const size_t smem = P == PREC_DOUBLE ? step_smem_d() : step_smem_f();
     const int threads = P == PREC_DOUBLE ? kThreads : kThreadsF;
     auto kernel = StepKernel<P, KIND, EXACT, REF>::fn();
-    if (!configured) {
-        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return -1;
-        configured = true;
+    if (smem > 48 * 1024) {
+        // The opt-in above 48 KB of dynamic shared memory is a per-device attribute: remember the
+        // devices that have it (one bit each; devices past 63 set it on every launch).
+        static std::atomic<unsigned long long> configured{0};
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+        const unsigned long long bit = dev < 64 ? 1ull << dev : 0ull;
+        if (!bit || !(configured.load(std::memory_order_acquire) & bit)) {
+            if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return -1;
+            configured.fetch_or(bit, std::memory_order_release);
+        }
     }
     const int tiles = s.n_body_tiles + s.n_free_tiles;
     if (tiles == 0) return 0;
