@@ -1187,17 +1187,21 @@ int rbx_step_host_async(rbx_integrator* h, void* stream, int nsteps, double dt, 
     if ((rc = ensure_context(h))) return rc;
     CUDA_TRY(cudaSetDevice(h->device));
     const size_t n3 = (size_t)3 * h->natoms;
-    if (!h->p_in) {
+    if (!h->p_out) {
+        // First use: staging buffers, events and copy streams. Each piece is made only if it is
+        // missing, so a call after a failure here completes the setup without leaking; p_out is
+        // created last and marks it complete.
         for (int s = 0; s < 2; s++) {
-            if (h->p_f[s].alloc(n3) != cudaSuccess || h->p_x[s].alloc(n3) != cudaSuccess || h->p_v[s].alloc(n3) != cudaSuccess)
+            if ((!h->p_f[s].p && h->p_f[s].alloc(n3) != cudaSuccess) || (!h->p_x[s].p && h->p_x[s].alloc(n3) != cudaSuccess) ||
+                (!h->p_v[s].p && h->p_v[s].alloc(n3) != cudaSuccess))
                 return fail(RBX_ERR_CUDA, "cudaMalloc of pipeline staging failed");
-            CUDA_TRY(cudaEventCreateWithFlags(&h->p_in_done[s], cudaEventDisableTiming));
-            CUDA_TRY(cudaEventCreateWithFlags(&h->p_compute_done[s], cudaEventDisableTiming));
-            CUDA_TRY(cudaEventCreateWithFlags(&h->p_out_done[s], cudaEventDisableTiming));
+            if (!h->p_in_done[s]) CUDA_TRY(cudaEventCreateWithFlags(&h->p_in_done[s], cudaEventDisableTiming));
+            if (!h->p_compute_done[s]) CUDA_TRY(cudaEventCreateWithFlags(&h->p_compute_done[s], cudaEventDisableTiming));
+            if (!h->p_out_done[s]) CUDA_TRY(cudaEventCreateWithFlags(&h->p_out_done[s], cudaEventDisableTiming));
             CUDA_TRY(cudaEventRecord(h->p_compute_done[s], (cudaStream_t)stream));
             CUDA_TRY(cudaEventRecord(h->p_out_done[s], (cudaStream_t)stream));
         }
-        CUDA_TRY(cudaStreamCreateWithFlags(&h->p_in, cudaStreamNonBlocking));
+        if (!h->p_in) CUDA_TRY(cudaStreamCreateWithFlags(&h->p_in, cudaStreamNonBlocking));
         CUDA_TRY(cudaStreamCreateWithFlags(&h->p_out, cudaStreamNonBlocking));
     }
     const int s = (int)(h->p_calls & 1);
