@@ -66,7 +66,9 @@ int rbx_version(void);
  *   rotation_mode 0 = exact (Jacobi elliptic), n > 0 = NO-SQUISH with n substeps.
  *   precision     enum rbx_precision; device = CUDA device ordinal.
  * Errors: RBX_ERR_INVALID_ARGUMENT for a negative mode (RigidBodyIntegrator.cpp:28-29), a bad
- * count, or a massless body atom.
+ * count, or a massless body atom. RBX_ERR_UNSUPPORTED for a body larger than a tile (1024 atoms
+ * in single and mixed precision, 512 in double) or a system beyond 32-bit device indexing (about
+ * 76 million bodies, or 715 million body atoms or free atoms; the buffer stride likewise).
  */
 int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, const double* masses,
                int rotation_mode, int precision, int device);

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdarg>
 #include <cstdint>
@@ -422,6 +423,8 @@ int check_ready(const rbx_integrator* h, const rbx_buffers* buf) {
     if (h->prec == PREC_MIXED && !buf->posq_correction)
         return fail(RBX_ERR_INVALID_ARGUMENT, "mixed precision needs posq_correction");
     if (buf->stride < h->natoms) return fail(RBX_ERR_INVALID_ARGUMENT, "stride %d < number of atoms %d", buf->stride, h->natoms);
+    if (3LL * buf->stride > INT_MAX)  // force rows are indexed slot + 2 x stride in 32 bits
+        return fail(RBX_ERR_UNSUPPORTED, "stride %d exceeds the 32-bit device indexing of this build", buf->stride);
     if (h->max_location >= buf->stride)
         return fail(RBX_ERR_INVALID_ARGUMENT, "device slot %d outside buffers of stride %d", h->max_location, buf->stride);
     return RBX_OK;
@@ -657,6 +660,14 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
     h->nb_pad = ((std::max(nb, 1) + 31) / 32) * 32;
     h->nba_pad = ((std::max(h->nba, 1) + 31) / 32) * 32;
     h->nf_pad = ((std::max(h->nf, 1) + 31) / 32) * 32;
+    // Device indices are 32-bit: the largest are row 27 of the float-float body state
+    // (28 x nb_pad) and row 2 of the body-frame coordinates and of the free-atom rows.
+    if (28LL * h->nb_pad > INT_MAX || 3LL * h->nba_pad > INT_MAX || 3LL * h->nf_pad > INT_MAX) {
+        const int nba = h->nba, nf = h->nf;
+        delete h;
+        return fail(RBX_ERR_UNSUPPORTED, "%d bodies, %d body atoms and %d free atoms exceed the 32-bit device indexing of this build",
+                    nb, nba, nf);
+    }
     h->I.assign((size_t)nb * 3, 0.0);
     h->dfix.assign((size_t)h->nba * 3, 0.0);
     h->invm.assign(nb, 0.0);
@@ -790,6 +801,8 @@ int rbx_upload_state_device(rbx_integrator* h, void* stream, const rbx_buffers* 
         return fail(RBX_ERR_INVALID_ARGUMENT, "mixed precision needs posq_correction");
     if (buf->stride < h->natoms || h->max_location >= buf->stride)
         return fail(RBX_ERR_INVALID_ARGUMENT, "device slots outside buffers of stride %d", buf->stride);
+    if (3LL * buf->stride > INT_MAX)
+        return fail(RBX_ERR_UNSUPPORTED, "stride %d exceeds the 32-bit device indexing of this build", buf->stride);
     CUDA_TRY(cudaSetDevice(h->device));
     if (!h->d_I.p && (h->d_I.alloc((size_t)3 * h->nb_pad) != cudaSuccess || h->d_dof.alloc(std::max(h->nb, 1)) != cudaSuccess ||
                       h->d_setup_counts.alloc(2) != cudaSuccess))
@@ -1027,7 +1040,10 @@ static int ensure_context(rbx_integrator* h) {
         return RBX_OK;
     }
     CUDA_TRY(cudaSetDevice(h->device));
-    h->stride = ((std::max(h->natoms, h->max_location + 1) + 31) / 32) * 32;
+    const long long stride = ((std::max<long long>(h->natoms, h->max_location + 1LL) + 31) / 32) * 32;
+    if (3 * stride > INT_MAX)
+        return fail(RBX_ERR_UNSUPPORTED, "%d atoms exceed the 32-bit device indexing of this build", h->natoms);
+    h->stride = (int)stride;
     const size_t p4 = h->prec == PREC_DOUBLE ? 32 : 16, v4 = h->prec == PREC_SINGLE ? 16 : 32;
     if (h->c_posq.alloc(p4 * h->stride) != cudaSuccess || h->c_velm.alloc(v4 * h->stride) != cudaSuccess ||
         h->c_force.alloc((size_t)3 * h->stride) != cudaSuccess || h->c_x.alloc((size_t)3 * h->natoms) != cudaSuccess ||
