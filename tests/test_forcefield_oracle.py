@@ -5,7 +5,6 @@ discontinuity of the unshifted LJ term), sum to zero in each box (pair forces ar
 opposite), leave pairs of one rigid body out, and not depend on the other systems of a batch.
 """
 import numpy as np
-import pytest
 
 from openmm_rigidbody_plugin_gb300 import workloads as W
 
