@@ -146,6 +146,98 @@ constexpr size_t step_smem_d() {
            3 * TB * sizeof(double) + TA * sizeof(unsigned short) + 64;
 }
 
+// ------------------------------------------------------------------------------------------
+// Mixed-precision free atoms in float-float on the FP32 pipe
+// ------------------------------------------------------------------------------------------
+// Float-float from a double by integer operations: hi is the double truncated to 24 significant
+// bits, lo the 29-bit remainder rounded to a float (|hi + lo - d| <= 2^-47 |d|). Zero is exact.
+// Returns false for |d| outside [2^-74, 2^127) (the remainder or hi would leave the normal float
+// range), infinities and NaN.
+__device__ __forceinline__ bool ff_from_double(double d, ff& out) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    const unsigned int e = (unsigned int)(u >> 52) & 0x7FFu;
+    const unsigned long long m = u & 0xFFFFFFFFFFFFFull;
+    const unsigned int sign = (unsigned int)(u >> 32) & 0x80000000u;
+    if (e == 0u && m == 0ull) {
+        out = ff{__uint_as_float(sign), 0.0f};
+        return true;
+    }
+    if (e < 949u || e > 1150u) return false;
+    const float hi = __uint_as_float(sign | ((e - 896u) << 23) | (unsigned int)(m >> 29));  // exponent e-1023+127
+    const float scale = __uint_as_float((e - 948u) << 23);                                   // 2^(e-1075)
+    const float lo = __fmul_rn((float)(unsigned int)(m & 0x1FFFFFFFull), scale);
+    out = ff{hi, sign ? -lo : lo};
+    return true;
+}
+
+// a + b as an exact float-float (two-sum).
+__device__ __forceinline__ ff ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return ff{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+// a * b in float-float (the exact product of the high words by FMA, plus the cross terms).
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    const float hi = __fadd_rn(p, e);
+    return ff{hi, __fsub_rn(e, __fsub_rn(hi, p))};
+}
+
+__device__ __forceinline__ ff ff_add_ff(ff a, ff b) { return ff_add(ff_add(a, b.hi), b.lo); }
+
+// Fixed-point force (scale 2^32) as float-float: the high word, the top 24 bits of the low word
+// and its last 8 bits are each exact floats (the first for |F| < 2^24 kJ/mol/nm).
+__device__ __forceinline__ ff fixed_to_ff(long long v) {
+    const int hi = (int)(v >> 32);
+    const unsigned int lo = (unsigned int)v;
+    return ff_add(ff_two_sum((float)hi, __fmul_rn((float)(lo >> 8), 0x1p-24f)), __fmul_rn((float)(lo & 0xFFu), 0x1p-32f));
+}
+
+// The free atom's velocity Verlet in mixed precision (rigidbodyintegrator.cu:302-310, :351-358)
+// in float-float arithmetic. velm is double4 in OpenMM's mixed mode: its words are split by
+// ff_from_double and the new velocity is joined by one FP64 add per component, so an atom issues
+// 9 FP64 instructions instead of about 47 on GB300's narrow FP64 pipe. With the free-atom tiles
+// interleaved, this measured 0.1374 against 0.1383 ms per step at 1e6 bodies, within run-to-run
+// variation: the FP64 pipe no longer limited them. Positions are the
+// float-float pair posq + posqCorrection. Returns false, having written nothing, when a velocity,
+// 1/m or the step lies outside the split's range; the caller then runs the FP64 form.
+template <int KIND>
+__device__ __forceinline__ bool free_atom_ff(const DevBuf& B, double dt_d, int loc) {
+    dq4* vel = (dq4*)B.velm;
+    dq4 vm = vel[loc];
+    ff v[3], w, dt;
+    if (!ff_from_double(vm.x, v[0]) || !ff_from_double(vm.y, v[1]) || !ff_from_double(vm.z, v[2]) ||
+        !ff_from_double(vm.w, w) || !ff_from_double(dt_d, dt))
+        return false;
+    const ff wh = ff_mul(w, ff{0.5f * dt.hi, 0.5f * dt.lo});  // (1/m) dt/2; halving is exact
+    const long long f[3] = {__ldg(B.force + loc), __ldg(B.force + loc + B.stride), __ldg(B.force + loc + 2 * B.stride)};
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+        const ff dv = ff_mul(fixed_to_ff(f[c]), wh);
+        if (KIND != STEP_PART1) v[c] = ff_add_ff(v[c], dv);  // second half kick of step n
+        if (KIND != STEP_PART2) v[c] = ff_add_ff(v[c], dv);  // first half kick of the next step
+    }
+    if (KIND != STEP_PART2) {  // drift: posq + posqCorrection += v dt
+        float4* pq = (float4*)B.posq;
+        float4 p = pq[loc];
+        const float4 cr = ((const float4*)B.corr)[loc];
+        const ff x0 = ff_add_ff(ff{p.x, cr.x}, ff_mul(v[0], dt));
+        const ff x1 = ff_add_ff(ff{p.y, cr.y}, ff_mul(v[1], dt));
+        const ff x2 = ff_add_ff(ff{p.z, cr.z}, ff_mul(v[2], dt));
+        p.x = x0.hi; p.y = x1.hi; p.z = x2.hi;
+        pq[loc] = p;
+        ((float4*)B.corr)[loc] = make_float4(x0.lo, x1.lo, x2.lo, 0.0f);
+    }
+    vm.x = (double)v[0].hi + (double)v[0].lo;
+    vm.y = (double)v[1].hi + (double)v[1].lo;
+    vm.z = (double)v[2].hi + (double)v[2].lo;
+    vel[loc] = vm;
+    return true;
+}
+
 // Free atoms (velocity Verlet). With REF, part1 and fused steps store alpha = F(t) h/m, and part2
 // writes the free atom's refined-energy terms at t+h (the freeAtomsDot stencil of
 // CudaRigidBodyKernels.cpp:406-438 and the refinedKineticEnergies / potentialEnergyRefinement
@@ -160,6 +252,9 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
     const int j = ft * (int)blockDim.x + (int)threadIdx.x;
     if (j >= S.nf) return;
     const int loc = __ldg(S.free_loc + j);
+    if constexpr (P == PREC_MIXED && !REF) {
+        if (free_atom_ff<KIND>(B, dt, loc)) return;
+    }
     V4* vel = (V4*)B.velm;
     V4 vm = vel[loc];
     V3<T> v = v3<T>((T)vm.x, (T)vm.y, (T)vm.z);
@@ -191,10 +286,11 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
 
 // Tile of this block: the body tile (>= 0) or -1 - the free-atom tile. Free-atom tiles are spread
 // evenly over the grid (every s-th block, s = floor(tiles / free-atom tiles)) rather than placed
-// after the body tiles: in mixed precision their velocity arithmetic is FP64 (OpenMM's velm), and
-// GB300's narrow FP64 pipe turned them into a tail at the end of the grid (100,000 free atoms cost
-// 15 us of a 0.144 ms step, for 2 % of its bytes). Interleaved, that work overlaps the body tiles'
-// memory traffic. The mapping is a bijection onto [0, body tiles) and [0, free-atom tiles).
+// after the body tiles, where their FP64 velocity arithmetic (then used in mixed precision) queued
+// on GB300's narrow FP64 pipe as a tail at the end of the grid: 100,000 free atoms cost 15 us of a
+// 0.144 ms step, for 2 % of its bytes. Interleaved, that work overlaps the body tiles' memory
+// traffic (0.1437 -> 0.1383 ms). The mapping is a bijection onto [0, body tiles) and [0, free-atom
+// tiles).
 __device__ __forceinline__ int block_tile(const DevSys& S) {
     const int i = (int)blockIdx.x, nf = S.n_free_tiles;
     if (nf == 0) return i;
