@@ -36,8 +36,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "body-steps/s batched/served vs plain at equal energy drift; p50/p99 latency"
 UNIT = "body-steps/s"
-WORKLOAD = ("single large system: 1,000,000 rigid bodies (70% 3-site water, 20% 5-atom tetrahedra, "
-            "10% 12-atom rings) + 100,000 free LJ atoms; integrator-only, fixed seeded Gaussian forces "
+def workload_name(bodies, free):
+    """The single-system workload as benched (1,000,000 bodies and 100,000 free atoms by default)."""
+    return (f"single large system: {bodies:,} rigid bodies (70% 3-site water, 20% 5-atom tetrahedra, "
+            f"10% 12-atom rings) + {free:,} free LJ atoms; integrator-only, fixed seeded Gaussian forces "
             "sd 500 kJ/mol/nm; dt 2 fs")
 # Algorithmic bytes of one fused step (drop-in OpenMM layout, atom velocities not materialised):
 #   per body   273 B (single/mixed): r, v, q, pi float-float read + write (224) + 1/m and 1/I as
@@ -331,7 +333,7 @@ def run_reference(args, world, rank):
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD + f"; rotation mode {args.mode}", "bodies": nb,
+           "config": {"workload": workload_name(args.bodies, args.free) + f"; rotation mode {args.mode}", "bodies": nb,
                       "atoms": int(s.num_atoms), "implementation": "CPU port of RigidBodySystem::integratePart1/2 "
                       "(robust variant: the reference's own eigen-solver and exact rotation produce NaN for the "
                       "tetrahedra and rings of this mix)"},
@@ -470,7 +472,7 @@ def run_gpu(args, world, rank, local):
            "scaling": "weak", "vs_baseline": None,
            "dtype": {"mixed": "f32 atoms + f64 body state", "double": "f64", "single": "f32"}[args.precision],
            "data": "synthetic",
-           "config": {"workload": WORKLOAD + f"; rotation mode {args.mode}; {args.precision} precision"
+           "config": {"workload": workload_name(args.bodies, args.free) + f"; rotation mode {args.mode}; {args.precision} precision"
                                   + ("; refined energies on" if args.refined else ""),
                       "bodies_per_gpu": nb, "body_atoms_per_gpu": nba, "free_atoms_per_gpu": nf,
                       "l2": "working set > 129 MB L2 (no flush needed)", "parallelism": f"{world} independent replicas"},
