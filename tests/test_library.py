@@ -94,3 +94,26 @@ def test_null_handle_calls_fail_cleanly(lib):
     assert lib.rbx_get_num_bodies(None, ctypes.byref(out)) == 1
     assert lib.rbx_destroy(None) == 0
     assert lib.rbx_last_launch_count(None) == 0
+
+
+def test_header_is_plain_c_and_links_from_c(lib, tmp_path):
+    """include/rbx.h compiles as pedantic C99, and a C program links librbx.so and calls it (no GPU
+    call): the boundary a cgo, JNI or ctypes binding sees."""
+    import shutil
+    import subprocess
+    from openmm_rigidbody_plugin_gb300 import _lib
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not found")
+    src = tmp_path / "use_rbx.c"
+    src.write_text('#include "rbx.h"\n#include <stdio.h>\n'
+                   'int main(void) { rbx_integrator* h = 0;\n'
+                   '  int rc = rbx_create(&h, 0, 0, 0, 0, RBX_PRECISION_MIXED, 0);\n'
+                   '  printf("%d %d\\n", rbx_version(), rc); return rc == RBX_ERR_INVALID_ARGUMENT ? 0 : 1; }\n')
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    exe = tmp_path / "use_rbx"
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-lrbx", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert int(r.stdout.split()[0]) == lib.rbx_version()
