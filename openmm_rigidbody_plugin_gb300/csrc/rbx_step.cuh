@@ -52,7 +52,7 @@ template <> struct Tr<PREC_SINGLE> {
 };
 template <> struct Tr<PREC_MIXED> {
     using A = float;
-    using R = double;  // free-atom arithmetic (velm is FP64)
+    using R = double;  // FP64 free-atom form (velm is FP64): refined-energy kernels, free_atom_ff's fallback
     using D = float;
     using P4 = float4;
     using V4 = dq4;
