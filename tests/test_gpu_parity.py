@@ -152,6 +152,40 @@ def test_single_bond_free_atoms(rbx, golden):
     np.testing.assert_allclose(buf.get_velocities(), g["V"][-1], atol=1e-9)
 
 
+@pytest.mark.parametrize("prec", ["single", "mixed", "double"])
+def test_single_bond_known_answer_in_every_precision(rbx, golden, prec):
+    """The reference's testSingleBond (tests/TestRigidBodyIntegrator.h:49-83), which its CUDA tests
+    run in single, mixed and double precision (platforms/cuda/tests/CMakeLists.txt:20-22): two free
+    atoms of mass 2 on a harmonic bond (r0 1.5, k 1) against the analytic oscillator, positions and
+    velocities within 0.02 and energy within 0.01 at every step, 1000 steps of 0.01 (time 10.0)."""
+    g = golden("single_bond")
+    k, buf = make(rbx, g["masses"], g["body_indices"], g["R0"], g["V0"], 0, prec)
+    dt, nsteps, m = float(g["dt"]), int(g["nsteps"]), np.asarray(g["masses"])
+
+    def force(x):
+        d = x[1] - x[0]
+        r = np.linalg.norm(d)
+        f = -1.0 * (r - 1.5) * d / r
+        return np.array([-f, f])
+
+    def energy(x, v):
+        return 0.5 * (np.linalg.norm(x[1] - x[0]) - 1.5) ** 2 + 0.5 * np.sum(m[:, None] * v ** 2)
+
+    e0 = energy(g["R0"], g["V0"])
+    buf.set_forces(force(g["R0"]))
+    for n in range(nsteps):
+        k.part1(buf, dt)
+        buf.set_forces(force(buf.get_positions()))
+        k.part2(buf, dt)
+        x, v = buf.get_positions(), buf.get_velocities()
+        t = (n + 1) * dt
+        dist, speed = 1.5 + 0.5 * np.cos(t), -0.5 * np.sin(t)
+        np.testing.assert_allclose(x, [[-0.5 * dist, 0, 0], [0.5 * dist, 0, 0]], atol=0.02)
+        np.testing.assert_allclose(v, [[-0.5 * speed, 0, 0], [0.5 * speed, 0, 0]], atol=0.02)
+        assert abs(energy(x, v) - e0) < 0.01
+    assert abs(nsteps * dt - 10.0) < 1e-12
+
+
 def _mixed_case(seed=3):
     from openmm_rigidbody_plugin_gb300 import workloads as W
     s = W.mixed_system(n_bodies=300, n_free=40, fractions=(0.5, 0.3, 0.2), seed=seed)
