@@ -1,26 +1,35 @@
 """Benchmark of the rigid-body integration step (one JSON line on rank 0).
 
-Workload (the single-large-system configuration): 1,000,000 rigid bodies (70 % 3-site waters,
-20 % 5-atom tetrahedra, 10 % 12-atom planar rings) plus 100,000 free LJ atoms, seeded random
-orientations and 300 K velocities, integrator-only with fixed seeded Gaussian forces
-(sd 500 kJ/mol/nm), rotation mode 0 (exact), mixed precision, dt 2 fs. One step is one fused
-kernel pass (second half kick of step n + first half kick, drift, rotation and position rebuild
-of step n+1) over all bodies and free atoms with every input resident in HBM; the working set
-(~0.6 GB) exceeds the 129 MB L2, so no flush is needed between steps.
+Default workload (the batched-replicas configuration): 4096 independent systems per GPU, body
+counts log-uniform in [64, 4096] (70 % 3-site waters, 20 % 5-atom tetrahedra, 10 % 12-atom planar
+rings), each in its own periodic box at 1 g/cm^3, cutoff LJ + reaction-field forces from the
+library's cell-list kernel, 300 K, dt 2 fs, rotation mode 0, mixed precision. One step is one full
+velocity-Verlet step of every system (forces, then the integrator), all systems in one launch per
+kernel, runs of steps replayed from captured CUDA graphs. The working set (about 1 GB) exceeds the
+129 MB L2, so no flush is needed between steps.
 
-  value   body-steps/s = bodies x steps / device time (CUDA events on the launching stream,
-          max over ranks)
-  e2e     the same metric through the host-buffer C ABI call (rbx_step_host): per step the
-          forces go host->device from pinned memory and positions and velocities come back
-  roofline  algorithmic bytes of the step kernel / its average launch time vs measured HBM peak
-  e2e.host_link  the same bytes by plain pinned copies (both directions at once): the e2e step's
-          bound, since the host link is far slower than HBM
-  cpu_baseline  the CPU port of the reference integrator (oracle) on the machine's host cores
+  value   body-steps/s = bodies x steps / device time of exactly --steps steps (CUDA events on the
+          launching stream, max over ranks), inputs resident in HBM
+  plain / speedup_vs_plain  the same systems stepped one system per launch (one handle each, the
+          plain drop-in way), from the same exact state, and the ratio; both energy drifts, and
+          whether the final energies of the two arms are bit-equal
+  e2e     the same metric through the public API with host buffers: positions and velocities in
+          (set_state), the steps in chunks of 10 with the energies read back after each, positions
+          and velocities out
+  roofline  the integrator launches of the batched step (algorithmic bytes / event-timed launch
+          time) against the measured HBM peak; the force kernels' share of the step beside it
+  single_system  the single-large-system integrator step (1,000,000 bodies + 100,000 free atoms,
+          fixed seeded forces sd 500 kJ/mol/nm, the fused step kernel), with its own roofline, e2e
+          through the host-buffer C ABI and CPU baseline
+  cpu_baseline  the CPU port of the reference integrator (oracle) with FP64 all-pairs forces on the
+          box's host cores, on the four smallest systems
+  clocks  nvidia-smi samples over the timed steps and repeats of them (a window of at least 1.5 s)
 
---impl reference times the CPU implementation of the same step (the oracle port of the
-reference's RigidBodySystem::integratePart1/2 with all host threads) on the same workload.
-Multi-GPU (torchrun): every rank integrates its own full-size system (weak scaling, no collective
-on the data path); timings are max-reduced over ranks.
+--workload single|served|water|precision selects the other workloads (their own lines).
+--impl reference times the CPU implementation of the same workload on the host cores.
+Multi-GPU (torchrun): world x --systems systems are generated once and assigned to ranks by body
+count (partition.assign_systems); every rank steps its own share (weak scaling, no collective on
+the data path); timings are max-reduced over ranks.
 """
 import argparse
 import json
@@ -58,7 +67,7 @@ BYTES_PER_FREE = 128
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=2000)
+    p.add_argument("--steps", type=int, default=200)
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", default="rbx", choices=["rbx", "reference"])
     p.add_argument("--mode", type=int, default=0, help="rotation mode: 0 exact, n NO-SQUISH substeps")
@@ -74,11 +83,15 @@ def parse():
     p.add_argument("--reference-seconds", type=float, default=90.0,
                    help="bound on the timed CPU work of --impl reference")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--workload", default="single", choices=["single", "batched", "water", "served", "precision"],
-                   help="single: the 1e6-body integrator step (default); batched: many independent systems, "
-                        "full steps with the cell-list force field, against one system per launch; water: "
-                        "512 rigid waters, full steps")
-    p.add_argument("--systems", type=int, default=4096, help="batched: number of systems")
+    p.add_argument("--workload", default="batched", choices=["single", "batched", "water", "served", "precision"],
+                   help="batched (default): many independent systems, full steps with the cell-list force field, "
+                        "against one system per launch, with the single-system figures as an extra key; single: "
+                        "the 1e6-body integrator step; water: 512 rigid waters, full steps")
+    p.add_argument("--systems", type=int, default=4096, help="batched: number of systems per GPU")
+    p.add_argument("--min-bodies", type=int, default=64, help="batched: smallest system (bodies)")
+    p.add_argument("--max-bodies", type=int, default=4096, help="batched: largest system (bodies)")
+    p.add_argument("--no-single", action="store_true", help="batched: skip the single-system figures")
+    p.add_argument("--single-steps", type=int, default=500, help="batched: timed steps of the single-system figures")
     p.add_argument("--relax-steps", type=int, default=400, help="batched/water: relaxation before dynamics")
     p.add_argument("--graph-steps", type=int, default=50, help="batched/water: steps per captured CUDA graph")
     p.add_argument("--no-autotune", action="store_true",
@@ -305,7 +318,7 @@ def run_reference(args, world, rank):
     if rank != 0:
         return
     if args.workload in ("batched", "water"):
-        return run_reference_full_steps(args)
+        return run_reference_full_steps(args, world)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
@@ -374,11 +387,15 @@ def time_replan(k, buf, s, repeats=3):
                     "OpenMM itself does (torch indexing here)"}
 
 
-def run_gpu(args, world, rank, local):
+def measure_single(args, world, rank, local, with_cpu=True, steps=None):
+    """The single-large-system integrator step (the drop-in path): the fused step kernel timed over
+    `steps` launches, its roofline, e2e through the host-buffer C ABI, and the CPU port beside it.
+    Returns the JSON object (rank 0) or None."""
     import torch
     from openmm_rigidbody_plugin_gb300 import build, kernel
     torch.cuda.set_device(local)
     build.build_library()
+    steps = steps or args.steps
     s, F = build_workload(args, seed_offset=0)
     dt = 0.002
     k = kernel.IntegratorKernel(s.masses, s.body_indices, rotation_mode=args.mode, precision=args.precision,
@@ -406,12 +423,18 @@ def run_gpu(args, world, rank, local):
         torch.cuda.synchronize()
         clocks.mark_start()
         start.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             k.fused(buf, dt, stream)
         end.record(stream)
         torch.cuda.synchronize()
+        repeats = 0
+        while time.perf_counter() - clocks.t0 < 1.0:  # clock window of at least 1 s
+            for _ in range(steps):
+                k.fused(buf, dt, stream)
+            torch.cuda.synchronize()
+            repeats += 1
         clocks.mark_end()
-    launches = args.steps
+    launches = steps
     t_dev = start.elapsed_time(end) / 1e3
     t_dev = max_over_ranks(t_dev, world)
     k.part2(buf, dt, stream)
@@ -423,12 +446,12 @@ def run_gpu(args, world, rank, local):
         refined = {"kinetic": [float(e) for e in k.refined_kinetic_energies(buf, stream)],
                    "potential_refinement": k.potential_energy_refinement(buf, stream)}
     replan = time_replan(k, buf, s) if args.replan else None
-    value = world * nb * args.steps / t_dev
+    value = world * nb * steps / t_dev
     bytes_step = BYTES_PER_BODY[args.precision] * nb + BYTES_PER_BODY_ATOM[args.precision] * nba + BYTES_PER_FREE * nf
     if args.refined:  # stencil sums written by every fused step: 7 values per body, 3 per free atom
         es = 8 if args.precision == "double" else 4
         bytes_step += 7 * es * nb + 3 * es * nf
-    per_launch = t_dev / args.steps
+    per_launch = t_dev / steps
     peak, peak_kind = peaks()
     achieved = bytes_step / per_launch / 1e9
     traffic = None if args.refined else ncu_traffic(args.mode, args.precision, nb)  # captured for the plain kernel
@@ -463,12 +486,12 @@ def run_gpu(args, world, rank, local):
     e2e["host_link"] = link
 
     if rank != 0:
-        return
+        return None
     cpu = None
-    if not args.no_cpu:
+    if with_cpu:
         cpu = cpu_baseline(s, F, args, args.cpu_seconds)
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None,
            "dtype": {"mixed": "f32 atoms + f64 body state", "double": "f64", "single": "f32"}[args.precision],
            "data": "synthetic",
@@ -479,13 +502,20 @@ def run_gpu(args, world, rank, local):
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes_per_launch": bytes_step,
                         "kernel": "rbx::step_kernel (fused)"},
-           "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(), "gpu_launches": launches,
+           "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+           "clocks": dict(clocks.summary(), window=f"the timed {steps} steps plus {repeats} repeats of them (at least 1 s)"),
            "kinetic_energy_after": [float(ke[0]), float(ke[1])]}
     if refined is not None:
         out["refined_after"] = refined
     if replan is not None:
         out["replan"] = replan
-    print(json.dumps(out), flush=True)
+    return out
+
+
+def run_gpu(args, world, rank, local):
+    out = measure_single(args, world, rank, local, with_cpu=not args.no_cpu)
+    if out is not None:
+        print(json.dumps(out), flush=True)
 
 
 def _drift(e_pre, e_post, steps, dt, dof):
@@ -528,34 +558,65 @@ def cpu_full_steps(systems, x, v, offsets, seconds):
                       f"(integrator + FP64 all-pairs LJ/RF forces on {threads} threads), {t:.1f} s"}
 
 
-def run_reference_full_steps(args):
+def run_reference_full_steps(args, world):
     """CPU full steps (oracle integrator + FP64 LJ/RF forces, all host threads) on the batched or
-    water workload: the smallest systems of the batch (a bounded sample; the starting structures
-    are the generated ones, not relaxed, since the relaxation runs on the GPU)."""
+    water workload: the four smallest systems of the batch (a bounded sample; the starting
+    structures are the generated ones, not relaxed, since the relaxation runs on the GPU)."""
     from openmm_rigidbody_plugin_gb300 import workloads as W
     if args.workload == "water":
         systems = [W.water_box(512, seed=1)]
+        config = {"workload": "512 rigid 3-site waters, cubic box at 1 g/cm3, cutoff 0.9 nm LJ + reaction field, "
+                              "dt 2 fs, rotation mode 0, mixed precision, full steps",
+                  "parallelism": f"{world} independent replicas"}
     else:
-        allsys = W.batch_systems(args.systems, lo=64, hi=4096, seed=6)
-        systems = [allsys[k] for k in np.argsort([s.num_bodies for s in allsys])[:4]]
+        counts = W.batch_body_counts(args.systems * world, lo=args.min_bodies, hi=args.max_bodies, seed=6)
+        pick = np.argsort(counts, kind="stable")[:4]
+        systems = W.batch_systems(args.systems * world, lo=args.min_bodies, hi=args.max_bodies, seed=6, only=pick)
+        config = batched_config(args, world)
     x = np.concatenate([s.positions for s in systems])
     v = np.concatenate([s.velocities for s in systems])
     offs = np.concatenate([[0], np.cumsum([s.num_atoms for s in systems])])
     r = cpu_full_steps(systems, x, v, offs, args.reference_seconds / 3)
     out = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": args.workload, "implementation": "CPU port of RigidBodySystem::integratePart1/2 "
-                      "(robust variant) + FP64 all-pairs cutoff LJ/RF forces"},
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config,
+           "implementation": "CPU port of RigidBodySystem::integratePart1/2 (robust variant) + FP64 all-pairs "
+                             "cutoff LJ/RF forces",
            "cpu_baseline": r, "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                                       "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
+def batched_systems_for_rank(args, world, rank):
+    """The rank's share of the batched-replicas workload: world x --systems systems (seeded once),
+    assigned to ranks by their body counts (partition.assign_systems, longest first), so every rank
+    holds about --systems systems' worth of bodies (weak scaling) and no system is on two ranks."""
+    from openmm_rigidbody_plugin_gb300 import partition
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    counts = W.batch_body_counts(args.systems * world, lo=args.min_bodies, hi=args.max_bodies, seed=6)
+    owner, _ = partition.assign_systems(counts, world)
+    mine = np.flatnonzero(owner == rank)
+    return mine, W.batch_systems(args.systems * world, lo=args.min_bodies, hi=args.max_bodies, seed=6, only=mine)
+
+
+def batched_config(args, world):
+    """The `config` of the batched workload, identical in both arms."""
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    counts = W.batch_body_counts(args.systems * world, lo=args.min_bodies, hi=args.max_bodies, seed=6)
+    return {"workload": (f"batched replicas: {args.systems} independent systems per GPU, body counts "
+                         f"log-uniform in [{args.min_bodies}, {args.max_bodies}] (70% 3-site water, 20% 5-atom "
+                         "tetrahedra, 10% 12-atom rings), each in its own cubic box at 1 g/cm3, cutoff 0.9 nm "
+                         "(0.49 box below 1.84 nm) LJ + reaction field, 300 K, dt 2 fs, rotation mode 0, mixed "
+                         "precision, full steps (forces + integrator)"),
+            "systems_per_gpu": args.systems, "bodies_total": int(counts.sum()), "steps": args.steps,
+            "parallelism": f"{world} rank(s); systems assigned to ranks by body count, no collective on the data path",
+            "l2": "working set (about 1 GB per GPU) > 129 MB L2, no flush needed"}
+
+
 def run_batched(args, world, rank, local):
-    """Many independent systems stepped together (full steps: cell-list forces + integrator, runs of
-    graph_steps steps replayed from one captured CUDA graph), against the same systems stepped one
-    system per launch."""
+    """Many independent systems stepped together (full steps: cell-list forces + integrator, one
+    launch per kernel per step, runs of steps replayed from captured CUDA graphs), against the same
+    systems stepped one system per launch (the plain drop-in way), at equal energy drift."""
     import torch
     from openmm_rigidbody_plugin_gb300 import batch, build
     from openmm_rigidbody_plugin_gb300 import workloads as W
@@ -564,14 +625,12 @@ def run_batched(args, world, rank, local):
     dt = 0.002
     if args.workload == "water":
         systems = [W.water_box(512, seed=1 + 1000 * rank)]
-        name = ("512 rigid 3-site waters, cubic box at 1 g/cm3, cutoff 0.9 nm LJ + reaction field, "
-                "dt 2 fs, rotation mode 0, mixed precision, full steps")
+        config = {"workload": "512 rigid 3-site waters, cubic box at 1 g/cm3, cutoff 0.9 nm LJ + reaction field, "
+                              "dt 2 fs, rotation mode 0, mixed precision, full steps",
+                  "parallelism": f"{world} independent replicas"}
     else:
-        systems = W.batch_systems(args.systems, lo=64, hi=4096, seed=6 + 1000 * rank)
-        name = (f"batched replicas: {args.systems} independent systems, body counts log-uniform in [64, 4096] "
-                "(70% water, 20% tetrahedra, 10% rings), each in its own box at 1 g/cm3, cutoff 0.9 nm "
-                "(0.49 box below 1.84 nm) LJ + reaction field, dt 2 fs, rotation mode 0, mixed precision, "
-                f"full steps, {args.graph_steps} steps per captured CUDA graph")
+        _, systems = batched_systems_for_rank(args, world, rank)
+        config = batched_config(args, world)
     nb = sum(s.num_bodies for s in systems)
     na = sum(s.num_atoms for s in systems)
     t0 = time.perf_counter()
@@ -582,12 +641,13 @@ def run_batched(args, world, rank, local):
     b.step(max(args.warmup, 3), dt)
     # the autotuner picks the schedule on this batch (and restores its state exactly)
     tuning = b.autotune(dt, trial_steps=3) if not args.no_autotune else None
-    if tuning:
-        name = name.replace(f"{args.graph_steps} steps per captured CUDA graph",
-                            f"autotuned schedule: {tuning['graph_steps']} steps per captured CUDA graph, "
-                            f"{tuning['cell_threads']}-thread cell force blocks")
     x0, v0 = b.get_state()
-    b.set_state(x0, v0)  # both arms start here
+    b.set_state(x0, v0)
+    # warm-up: at least W steps, and enough for the first CUDA-graph capture to happen here; both
+    # arms then start from the exact state after it (checkpoint / restore)
+    graph_k = tuning["graph_steps"] if tuning else args.graph_steps
+    b.step(max(args.warmup, graph_k + 1), dt)
+    ckpt = b.checkpoint()
     e_pre = b.energies()
     stream = torch.cuda.current_stream()
     torch.cuda.synchronize()
@@ -601,10 +661,17 @@ def run_batched(args, world, rank, local):
         b.step(args.steps, dt)
         end.record(stream)
         torch.cuda.synchronize()
+        launches = b.last_launch_count
+        e_post = b.energies()
+        # the clocks are sampled over the timed steps and over repeats of them until the window
+        # lasts at least 1.5 s, so that a short timed region still has its own clock record
+        repeats = 0
+        while time.perf_counter() - clocks.t0 < 1.5:
+            b.step(args.steps, dt)
+            torch.cuda.synchronize()
+            repeats += 1
         clocks.mark_end()
-    launches = b.last_launch_count
     t_dev = max_over_ranks(start.elapsed_time(end) / 1e3, world)
-    e_post = b.energies()
     value = world * nb * args.steps / t_dev
     drift = _drift(e_pre, e_post, args.steps, dt, dof)
 
@@ -618,17 +685,30 @@ def run_batched(args, world, rank, local):
     peak, peak_kind = peaks()
     achieved = bytes_step / t_int / 1e9
 
-    # e2e: the public call a user makes, chunks of 10 steps, energies read back per chunk
-    chunks = 3
+    # e2e through the public API with host buffers: the systems' positions and velocities go in
+    # from pinned host memory (set_state, which also builds every body on the device), the steps
+    # run in chunks of 10 with the energies read back after each chunk, and the final positions
+    # and velocities come back to pinned host memory
+    xh = torch.from_numpy(np.ascontiguousarray(x0)).pin_memory().numpy()
+    vh = torch.from_numpy(np.ascontiguousarray(v0)).pin_memory().numpy()
+    chunk = 10
+    nchunks = max(1, args.steps // chunk)
     torch.cuda.synchronize()
+    barrier(world)
     t0 = time.perf_counter()
-    for _ in range(chunks):
-        b.step(10, dt)
+    b.set_state(xh, vh)
+    for _ in range(nchunks):
+        b.step(chunk, dt)
         b.energies()
-    t_e2e = max_over_ranks((time.perf_counter() - t0) / (10 * chunks), world)
-    e2e = {"value": world * nb / t_e2e, "unit": UNIT, "h2d_bytes_per_step": 0,
-           "d2h_bytes_per_step": int(24 * len(systems) / 10),
-           "call": "BatchedSystems.step(10) + energies() per chunk (rbx_batch_step, rbx_batch_energies)"}
+    xo, vo = b.get_state()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_steps = nchunks * chunk
+    e2e = {"value": world * nb * e2e_steps / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": int(2 * 24 * na / e2e_steps),
+           "d2h_bytes_per_step": int((2 * 24 * na + 24 * len(systems) * nchunks) / e2e_steps),
+           "call": f"BatchedSystems.set_state (positions and velocities in), {nchunks} x (step({chunk}) + "
+                   "energies()), get_state (positions and velocities out): rbx_batch_set_state, rbx_batch_step, "
+                   "rbx_batch_energies, rbx_batch_get_state; wall clock"}
 
     # the same systems, one system per launch (the plain drop-in way: one context per system)
     plain = None
@@ -636,11 +716,14 @@ def run_batched(args, world, rank, local):
         idx = np.unique(np.linspace(0, len(systems) - 1, min(args.plain_systems, len(systems))).astype(int))
         off = b.offsets
         handles = []
+        plain_steps = args.plain_steps or args.steps
         for k in idx:
             h = batch.BatchedSystems.from_systems([systems[k]], device=local)
+            h.set_graph_steps(graph_k)
             h.set_state(x0[off[k]:off[k + 1]], v0[off[k]:off[k + 1]])
+            h.step(max(args.warmup, graph_k + 1), dt)  # warm-up and the graph capture, untimed
+            h.restore([ckpt[k]])                      # the batched arm's starting state, exactly
             handles.append(h)
-        plain_steps = args.plain_steps or args.steps
         e_pre_p = np.array([h.energies()[0] for h in handles])
         torch.cuda.synchronize()
         pa, pb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -659,12 +742,17 @@ def run_batched(args, world, rank, local):
         if plain_steps == args.steps:  # the same systems inside the batch, over the same steps
             plain["batched_energy_drift_same_systems"] = _drift(e_pre[idx], e_post[idx], args.steps, dt, dof[idx])
             plain["same_final_energies_as_batched"] = bool(np.array_equal(e_post_p, e_post[idx]))
+        del handles
+    single = None
+    if args.workload == "batched" and not args.no_single:
+        del b
+        single = measure_single(args, world, rank, local, with_cpu=not args.no_cpu, steps=args.single_steps)
     if rank != 0:
         return
     cpu = None
     if not args.no_cpu:
         pick = [0] if args.workload == "water" else list(np.argsort([s.num_bodies for s in systems])[:4])
-        off = b.offsets
+        off = np.concatenate([[0], np.cumsum([s.num_atoms for s in systems])])
         sub = [systems[k] for k in pick]
         xs = np.concatenate([x0[off[k]:off[k + 1]] for k in pick])
         vs = np.concatenate([v0[off[k]:off[k + 1]] for k in pick])
@@ -673,18 +761,22 @@ def run_batched(args, world, rank, local):
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32 atoms + f64 body state", "data": "synthetic",
-           "config": {"workload": name, "systems_per_gpu": len(systems), "bodies_per_gpu": nb, "atoms_per_gpu": na,
-                      "relax_steps": args.relax_steps, "setup_seconds": setup_s,
-                      "l2": "working set > 129 MB L2" if na * 120 > 129e6 else "working set fits in L2",
-                      "parallelism": f"{world} independent replicas", "autotune": tuning},
+           "config": config,
+           "setup": {"systems_on_rank0": len(systems), "bodies_on_rank0": nb, "atoms_on_rank0": na,
+                     "relax_steps": args.relax_steps, "seconds": setup_s, "autotune": tuning},
            "energy_drift": drift, "plain": plain,
            "speedup_vs_plain": (value / world / plain["value"]) if plain else None,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "peak_source": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": bytes_step,
-                        "kernel": "rbx::step_kernel (integrator launches of the full step)",
-                        "integrator_ms_per_step": ms_i / 20, "force_ms_per_step": ms_f / 21,
+                        "kernel": "rbx::step_kernel_f (the integrator launches of the batched step: part1, fused, "
+                                  "part2; bytes per fused launch)",
+                        "integrator_ms_per_step": ms_i / 21, "force_ms_per_step": ms_f / 21,
                         "force_share": ms_f / (ms_f + ms_i)},
-           "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks.summary(), "gpu_launches": launches}
+           "cpu_baseline": cpu, "e2e": e2e, "clocks": dict(clocks.summary(), window=(
+               f"the timed {args.steps} steps plus {repeats} repeats of them (at least 1.5 s)")),
+           "gpu_launches": launches}
+    if single is not None:
+        out["single_system"] = single
     print(json.dumps(out), flush=True)
 
 

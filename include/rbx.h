@@ -106,6 +106,21 @@ int rbx_get_num_dof(const rbx_integrator* h, int* out);
 int rbx_get_num_bodies(const rbx_integrator* h, int* out);
 int rbx_get_num_free(const rbx_integrator* h, int* out);
 int rbx_get_rotation_mode(const rbx_integrator* h, int* out);
+/*
+ * The degrees of freedom exactly as the reference counts them, numFree - numConstraints + sum of
+ * body dof (openmmapi/src/RigidBodySystem.cpp:130), for callers that must report the plugin's own
+ * integer (its getNumDOF, and the temperature of its StateDataReporter, python/statedatareporter.py:
+ * 19-28). It differs from rbx_get_num_dof in two ways:
+ *   - a free atom counts 1, not 3;
+ *   - an atom whose body index is used once is a one-atom body in the reference (cleanBodyIndices
+ *     keeps it, RigidBodySystem.cpp:37-47) and counts 5 or 6: 6 when its displacement from its own
+ *     centre of mass, x - (x m)(1/m), is zero in every component, 5 when rounding leaves a residue
+ *     that the collinearity test then accepts (RigidBody.cpp:26-45, :88-107). It is evaluated on the
+ *     positions of the last rbx_upload_state / rbx_upload_state_device, as the reference evaluates it
+ *     on every state update. Massless atoms count nothing.
+ * RBX_ERR_STATE before the first state upload.
+ */
+int rbx_get_num_dof_reference(const rbx_integrator* h, int* out);
 
 /*
  * One half of a step on OpenMM-layout device buffers, enqueued on `stream` (cudaStream_t,
@@ -146,6 +161,18 @@ int rbx_set_constraints(rbx_integrator* h, int num_constraints, const int* atom_
 int rbx_free_atoms_delta(rbx_integrator* h, void* stream, const rbx_buffers* buf, void* pos_delta, double dt);
 int rbx_integrate_part1_delta(rbx_integrator* h, void* stream, const rbx_buffers* buf, const void* pos_delta,
                               double dt);
+
+/*
+ * Failure detector. The reference produces NaN silently when its exact rotation fails
+ * (openmmapi/include/internal/ellipticFunctions.h:38-39, :64-66) and keeps stepping it. Here every
+ * step kernel checks the new state of each body and free atom for a non-finite value (one sum of
+ * values it holds anyway) and flags the ones that fail. rbx_check_state synchronises `stream` and
+ * returns RBX_ERR_NUMERIC, with the counts of flagged bodies and free atoms (either pointer may be
+ * NULL) and a message naming the first of each (bodies in ascending body-index order, free atoms by
+ * user index), when any step since the last state change failed; RBX_OK and zero counts otherwise.
+ * The flags are cleared by rbx_upload_state, rbx_upload_state_device and rbx_set_body_state.
+ */
+int rbx_check_state(rbx_integrator* h, void* stream, int* bad_bodies, int* bad_free);
 
 /*
  * Translational and rotational kinetic energy [KE_t, KE_r] in kJ/mol, reduced on the device in
@@ -232,8 +259,10 @@ int rbx_step_host(rbx_integrator* h, void* stream, int nsteps, double dt, const 
  * For callers that cannot call cudaMalloc: a serving process that has reserved its whole
  * device-memory budget up front and admits work only against that reservation, a host framework
  * whose own pool owns every device allocation, or a latency-sensitive loop that cannot take the
- * device synchronisation an allocation may cause. It computes the same [KE_t, KE_r] as
- * rbx_kinetic_energies, from caller-owned device arrays, and allocates nothing: no cudaMalloc,
+ * device synchronisation an allocation may cause. It computes [KE_t, KE_r] from caller-owned
+ * device arrays; the results agree with rbx_kinetic_energies to rounding (about 1e-12 relative:
+ * the two reductions partition their sums differently) and are identical from call to call on
+ * the same inputs. It allocates nothing: no cudaMalloc,
  * no cudaFree, no allocating library call. Its scratch (block partial sums and a ticket counter)
  * is a fixed static device array of 16 KB + 256 B that every GPU which loads librbx holds until
  * the process exits.
@@ -242,11 +271,14 @@ int rbx_step_host(rbx_integrator* h, void* stream, int nsteps, double dt, const 
  *   inv_mass     [num_bodies] 1/m; inv_inertia [3 * body_stride] rows of 1/I (0 for the axis of a
  *                linear body)
  *   velm         device velm array (float4 for single, double4 otherwise); free_slots
- *                [num_free] device slot of each free atom
+ *                [num_free] device slot of each free atom (a slot whose velm.w = 1/m is 0, a
+ *                massless particle, contributes nothing)
  *   out_device   device double[2] receiving [KE_t, KE_r] (kJ/mol); asynchronous on `stream`.
- * Limit: at most 4,194,304 bodies and 4,194,304 free atoms (1024 block sums of 4096 items);
- * larger systems get RBX_ERR_UNSUPPORTED. The first call on a device looks up the scratch
- * address with that device current; make that first call before any stream capture. All calls
+ * Limit: at most 4,194,304 bodies and 4,194,304 free atoms (1024 block sums of 4096 items), and
+ * body_stride * 14 within 32-bit indexing; larger inputs get RBX_ERR_UNSUPPORTED. Each call
+ * outside stream capture looks up the scratch address on the current device (so a device reset,
+ * which reloads the module, is followed); a call on a capturing stream reuses the address of the
+ * last call on that device, so make the first call on a device before any stream capture. All calls
  * share the one scratch array, so calls that overlap on the GPU (concurrent streams, several host
  * threads) race and must be serialised by the caller.
  */
@@ -322,6 +354,16 @@ int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double ma
 int rbx_batch_energies(rbx_batch* b, void* stream, double* out /* [3*S] */);
 int rbx_batch_forces(rbx_batch* b, void* stream, double* forces /* [N*3], user order */, double* energies /* [S] */);
 int rbx_batch_get_num_dof(rbx_batch* b, int* dof /* [S] */);
+/* Failure status per system (no counterpart in the reference, which has no batched form and lets
+ * NaN through silently). A system fails when a step leaves any of its bodies or free atoms with a
+ * non-finite state (the step kernels' detector, see rbx_check_state) or when the force kernel
+ * meets a non-finite force or one beyond OpenMM's fixed-point range (|F| >= 2^31 kJ/mol/nm, i.e.
+ * overlapping atoms). Synchronises `stream`; system_status [S] (may be NULL) receives RBX_OK or
+ * RBX_ERR_NUMERIC per system, num_failed (may be NULL) their number. Returns RBX_ERR_NUMERIC,
+ * naming the first failed system, when any failed. Systems are independent: a failed system
+ * changes nothing for the others, which keep stepping exactly as they would alone. The status is
+ * cleared by rbx_batch_set_state and rbx_batch_restore. */
+int rbx_batch_status(rbx_batch* b, void* stream, int* system_status, int* num_failed);
 int rbx_batch_set_graph_steps(rbx_batch* b, int k);
 /* Autotuner of the batched step's schedule (no counterpart in the reference, which has no batched
  * form). It times, on the batch itself, the block size of the cell force kernel (64, 128 or 256

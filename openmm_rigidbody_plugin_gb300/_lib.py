@@ -13,6 +13,7 @@ PRECISIONS = {"single": 0, "mixed": 1, "double": 2}
 
 RBX_OK = 0
 STATUS_NAMES = {1: "invalid argument", 2: "CUDA error", 3: "bad call order", 4: "unsupported", 5: "numerical failure"}
+RBX_ERR_NUMERIC = 5
 
 # Every exported symbol of include/rbx.h: (name, restype, argtypes)
 _vp = ctypes.c_void_p
@@ -37,6 +38,8 @@ SIGNATURES = [
     ("rbx_upload_state", ctypes.c_int, [_vp, _dp, _dp]),
     ("rbx_upload_state_device", ctypes.c_int, [_vp, _vp, _bp]),
     ("rbx_get_num_dof", ctypes.c_int, [_vp, _ip]),
+    ("rbx_get_num_dof_reference", ctypes.c_int, [_vp, _ip]),
+    ("rbx_check_state", ctypes.c_int, [_vp, _vp, _ip, _ip]),
     ("rbx_get_num_bodies", ctypes.c_int, [_vp, _ip]),
     ("rbx_get_num_free", ctypes.c_int, [_vp, _ip]),
     ("rbx_get_rotation_mode", ctypes.c_int, [_vp, _ip]),
@@ -83,6 +86,7 @@ SIGNATURES = [
     ("rbx_batch_set_tuning", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     ("rbx_batch_forces", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_batch_get_num_dof", ctypes.c_int, [_vp, _ip]),
+    ("rbx_batch_status", ctypes.c_int, [_vp, _vp, _ip, _ip]),
     ("rbx_batch_set_graph_steps", ctypes.c_int, [_vp, ctypes.c_int]),
     ("rbx_batch_set_timing", ctypes.c_int, [_vp, ctypes.c_int]),
     ("rbx_batch_kernel_times", ctypes.c_int, [_vp, _dp, _dp, _ip]),

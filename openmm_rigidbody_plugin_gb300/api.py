@@ -187,8 +187,12 @@ class RigidBodySystem:
         self._k = k
         self._bidx = np.asarray(body_indices)
 
-    def getNumDOF(self):
-        return self._k.num_dof
+    def getNumDOF(self, reference=False):
+        """Degrees of freedom: three per free atom, and the atoms of unique body indices free (the
+        library's count); with reference=True, the integer RigidBodySystem::getNumDOF reports
+        (openmmapi/src/RigidBodySystem.cpp:130: one per free atom, unique indices as one-atom
+        bodies)."""
+        return self._k.num_dof_reference if reference else self._k.num_dof
 
     def getNumBodies(self):
         return self._k.num_bodies
@@ -528,7 +532,9 @@ class StateDataReporter:
     """Writes one comma-separated line per report: step, potential, kinetic and total energy,
     temperature (rigid-body degrees of freedom, minus 3 with a CMMotionRemover in the System),
     and optionally the translational and rotational kinetic energies and the refined energies, in
-    the column order of python/statedatareporter.py:30-48."""
+    the column order of python/statedatareporter.py:30-48. With referenceDOF=True the temperature
+    divides by the reference's own degree-of-freedom count (getNumDOF(reference=True)), so the
+    column equals the plugin's reporter on the same state."""
 
     _NAMES = {"step": '#"Step"', "potentialEnergy": "Potential Energy (kJ/mole)",
               "kineticEnergy": "Kinetic Energy (kJ/mole)", "totalEnergy": "Total Energy (kJ/mole)",
@@ -544,8 +550,10 @@ class StateDataReporter:
     def __init__(self, file, reportInterval, step=True, potentialEnergy=True, kineticEnergy=True,
                  totalEnergy=True, temperature=True, translationalEnergy=False, rotationalEnergy=False,
                  refinedPotentialEnergy=False, refinedKineticEnergy=False, refinedTotalEnergy=False,
-                 refinedTemperature=False, refinedTranslationalEnergy=False, refinedRotationalEnergy=False):
+                 refinedTemperature=False, refinedTranslationalEnergy=False, refinedRotationalEnergy=False,
+                 referenceDOF=False):
         self._out = file
+        self._reference_dof = bool(referenceDOF)
         self._interval = int(reportInterval)
         self._cols = dict(step=step, potentialEnergy=potentialEnergy, kineticEnergy=kineticEnergy,
                           totalEnergy=totalEnergy, temperature=temperature, translationalEnergy=translationalEnergy,
@@ -561,7 +569,7 @@ class StateDataReporter:
 
     def report(self, context, step):
         if self._dof is None:
-            self._dof = context.integrator.getRigidBodySystem().getNumDOF()
+            self._dof = context.integrator.getRigidBodySystem().getNumDOF(reference=self._reference_dof)
             if any(isinstance(f, CMMotionRemover) for f in context.system.forces):
                 self._dof -= 3
         if not self._header:

@@ -153,6 +153,16 @@ class BatchedSystems:
         _lib.check(self._lib.rbx_batch_get_num_dof(self._h, _i(out)))
         return out
 
+    def status(self, stream=None):
+        """Failure status per system (0, or 5 = RBX_ERR_NUMERIC for a system whose state became
+        non-finite or whose forces left the fixed-point range) since the last set_state/restore."""
+        out = np.zeros(self.num_systems, dtype=np.int32)
+        n = ctypes.c_int()
+        rc = self._lib.rbx_batch_status(self._h, _stream(stream), _i(out), ctypes.byref(n))
+        if rc not in (0, _lib.RBX_ERR_NUMERIC):
+            _lib.check(rc)
+        return out
+
     def set_graph_steps(self, k):
         _lib.check(self._lib.rbx_batch_set_graph_steps(self._h, int(k)))
 

@@ -22,6 +22,7 @@ using namespace rbx;
 namespace {
 
 constexpr double kOne4PiEps0 = 138.935456;  // kJ nm / (mol e^2)
+constexpr double kSkin = 0.1;               // nm: neighbour-list skin
 
 #define BATCH_TRY(call)                                                                             \
     do {                                                                                            \
@@ -51,15 +52,18 @@ struct rbx_batch {
     DevArray<FFSys> d_sys;
     DevArray<int> d_iatom, d_isys, d_cell_of, d_cell_count, d_cell_start, d_cell_cursor, d_cell_list;
     DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_i0;
-    DevArray<float4> d_param, d_cpos, d_cpar;
+    DevArray<float4> d_param, d_cpos, d_cpar, d_xref;
+    DevArray<unsigned char> d_rebuild, d_nbr;  // neighbour lists (FFDev::rebuild, nbr)
+    DevArray<int> d_ncnt;
     DevArray<double> d_e_atom, d_energy;
     FFDev ff{};
     // per-system reductions
     DevArray<int> d_body0, d_free0;
+    std::vector<int> body0_h, free0_h;  // host copies: library-order body / free-atom ranges per system
+    DevArray<unsigned int> d_sys_status;  // [S] force-kernel failures (FFDev::sys_status)
     DevArray<double> d_ke, d_user;
     std::vector<int> dof;
     double* h_out = nullptr;  // pinned [3*S]
-    bool forces_valid = false;
     int last_launches = 0;
     // captured runs of (forces, fused step)
     // optional event timing of the force and integrator launch groups (direct launches only)
@@ -133,6 +137,14 @@ struct Timed {
         b->ev_kind.push_back(kind);
     }
 };
+
+// Every call that evaluates forces starts from freshly built neighbour lists, so that its results
+// depend only on the state it starts from (not on when earlier calls last rebuilt); later
+// evaluations in the call rebuild a system's lists when its atoms have moved half the skin.
+int force_rebuild(rbx_batch* b, void* stream) {
+    BATCH_TRY(cudaMemsetAsync(b->d_rebuild.p, 1, (size_t)b->S, (cudaStream_t)stream));
+    return RBX_OK;
+}
 
 int forces(rbx_batch* b, void* stream, bool energy) {
     Timed t(b, stream, 0);
@@ -239,6 +251,8 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     std::vector<int> iatom, isys;
     std::vector<float4> param;
     int cells = 0;
+    double cap_need = 1.0;
+    int max_sys_atoms = 0;
     for (int s = 0; s < num_systems; s++) {
         FFSys& f = sys[s];
         f.a0 = atom_offsets[s];
@@ -254,9 +268,18 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
         }
         f.i1 = (int)iatom.size();
         const double L = box_edges[s], rc_s = cutoffs[s];
-        int nc = (int)std::floor(L / rc_s);
+        // neighbour-list skin: 0.1 nm, less where the box is too small for a unique minimum image
+        // of every pair within cutoff + skin (cutoff + skin <= L/2)
+        const double skin = std::max(0.0, std::min(kSkin, 0.5 * L - rc_s));
+        const double rl = rc_s + skin;
+        f.rl2 = (float)(rl * rl);
+        f.half_skin2 = (float)(0.25 * skin * skin);
+        int nc = (int)std::floor(L / rl);
         if (nc < 3) nc = 1;
         if (nc > 256) nc = 256;
+        const double dens = (double)(f.i1 - f.i0) / (L * L * L);
+        cap_need = std::max(cap_need, std::min((double)(f.i1 - f.i0), 1.35 * 4.18879 * rl * rl * rl * dens + 32.0));
+        max_sys_atoms = std::max(max_sys_atoms, f.i1 - f.i0);
         f.c0 = cells;
         f.nc = nc;
         cells += nc * nc * nc;
@@ -299,10 +322,30 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
                 b->d_cell_cursor.alloc(cells) != cudaSuccess || b->d_cpos.alloc(std::max(nint, 1)) != cudaSuccess ||
                 b->d_cpar.alloc(std::max(nint, 1)) != cudaSuccess || b->d_e_atom.alloc(std::max(nint, 1)) != cudaSuccess ||
                 b->d_energy.alloc(num_systems) != cudaSuccess || b->d_ke.alloc(2 * (size_t)num_systems) != cudaSuccess ||
-                b->d_user.alloc(3 * (size_t)N) != cudaSuccess))
+                b->d_user.alloc(3 * (size_t)N) != cudaSuccess || b->d_sys_status.alloc(num_systems) != cudaSuccess))
         rc = set_error(RBX_ERR_CUDA, "cudaMalloc of force-field arrays failed");
+    if (!rc && cudaMemset(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)num_systems) != cudaSuccess)
+        rc = set_error(RBX_ERR_CUDA, "cudaMemset of the system status failed");
     if (!rc && cudaMemset(b->d_cell_count.p, 0, sizeof(int) * (size_t)cells) != cudaSuccess)
         rc = set_error(RBX_ERR_CUDA, "cudaMemset of cell counts failed");
+    // neighbour lists: entries per atom from the densest system with a wide margin, in groups of 32
+    // atoms; 16-bit entries when every system has at most 65536 interacting atoms
+    const int cap = std::max(32, ((int)std::ceil(cap_need) + 31) / 32 * 32);
+    const int nbr16 = max_sys_atoms <= 65536 ? 1 : 0;
+    const size_t groups = ((size_t)std::max(nint, 1) + 31) / 32;
+    if (!rc && (b->d_rebuild.alloc(num_systems) != cudaSuccess || b->d_xref.alloc(std::max(nint, 1)) != cudaSuccess ||
+                b->d_ncnt.alloc(std::max(nint, 1)) != cudaSuccess ||
+                b->d_nbr.alloc(groups * 32 * (size_t)cap * (nbr16 ? 2 : 4)) != cudaSuccess))
+        rc = set_error(RBX_ERR_CUDA, "cudaMalloc of the neighbour lists failed (%d entries per atom)", cap);
+    if (!rc) {
+        std::vector<int> iota(std::max(nint, 1));
+        for (int k = 0; k < (int)iota.size(); k++) iota[k] = k;  // a valid list order before the first build
+        if (cudaMemcpy(b->d_cell_list.p, iota.data(), iota.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemset(b->d_rebuild.p, 1, (size_t)num_systems) != cudaSuccess ||
+            cudaMemset(b->d_ncnt.p, 0, sizeof(int) * (size_t)std::max(nint, 1)) != cudaSuccess ||
+            cudaMemset(b->d_cpos.p, 0, sizeof(float4) * (size_t)std::max(nint, 1)) != cudaSuccess)
+            rc = set_error(RBX_ERR_CUDA, "initialisation of the neighbour lists failed");
+    }
     if (!rc && cudaMallocHost((void**)&b->h_out, sizeof(double) * 3 * (size_t)num_systems) != cudaSuccess)
         rc = set_error(RBX_ERR_CUDA, "pinned allocation failed");
     if (rc) { delete b; return rc; }
@@ -324,6 +367,13 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     D.e_atom = b->d_e_atom.p;
     D.energy = b->d_energy.p;
     D.fcap = 0.0f;
+    D.sys_status = b->d_sys_status.p;
+    D.rebuild = b->d_rebuild.p;
+    D.xref = b->d_xref.p;
+    D.nbr = b->d_nbr.p;
+    D.ncnt = b->d_ncnt.p;
+    D.cap = cap;
+    D.nbr16 = nbr16;
     D.cell_threads = 128;
     D.n_mc = (int)mc_cell.size();
     D.n_sc = (int)sc_sys.size();
@@ -359,7 +409,9 @@ int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, con
     std::vector<int> body0, free0;
     if ((rc = system_ranges(b->integ, b->offsets, body0, free0, b->dof))) return rc;
     if ((rc = upload_vec(b->d_body0, body0)) || (rc = upload_vec(b->d_free0, free0))) return rc;
-    b->forces_valid = false;
+    b->body0_h = body0;
+    b->free0_h = free0;
+    BATCH_TRY(cudaMemsetAsync(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)b->S, (cudaStream_t)stream));
     return RBX_OK;
 }
 
@@ -391,7 +443,7 @@ int rbx_batch_restore(rbx_batch* b, void* stream, const double* body_state, cons
     if ((rc = rbx_context_load(b->integ, stream, positions, velocities))) return rc;
     if ((rc = rbx_set_body_state(b->integ, body_state))) return rc;
     if ((rc = rbx_context_sync_bodies(b->integ, stream))) return rc;
-    b->forces_valid = false;
+    BATCH_TRY(cudaMemsetAsync(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)b->S, (cudaStream_t)stream));
     return RBX_OK;
 }
 
@@ -403,7 +455,7 @@ int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
     BATCH_TRY(cudaSetDevice(b->device));
     b->last_launches = 0;
-    if (!b->forces_valid && (rc = forces(b, stream, false))) return rc;
+    if ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, false))) return rc;
     if ((rc = integrate(b, stream, STEP_PART1, dt))) return rc;
     int remaining = nsteps - 1;
     if (b->graph_k > 0 && !b->timing && remaining >= b->graph_k) {
@@ -421,7 +473,6 @@ int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {
     }
     if ((rc = forces(b, stream, false))) return rc;
     if ((rc = integrate(b, stream, STEP_PART2, dt))) return rc;
-    b->forces_valid = true;
     return RBX_OK;
 }
 
@@ -438,6 +489,7 @@ int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double ma
     rbx_context_buffers(b->integ, &rb);
     const DevSys sys = device_system(b->integ);
     b->ff.fcap = (float)max_force;
+    if ((rc = force_rebuild(b, stream))) return rc;
     for (int n = 0; n < nsteps && !rc; n++) {
         rc = forces(b, stream, false);
         if (!rc && launch_scale_momenta(b->prec, sys, buffers(b), damping, stream) < 0)
@@ -448,7 +500,6 @@ int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double ma
     b->ff.fcap = 0.0f;
     if (rc) return rc;
     if (launch_scale_momenta(b->prec, sys, buffers(b), 0.0, stream) < 0) return set_error(RBX_ERR_CUDA, "momentum reset failed");
-    b->forces_valid = false;
     return RBX_OK;
 }
 
@@ -459,8 +510,7 @@ int rbx_batch_energies(rbx_batch* b, void* stream, double* out) {
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
     BATCH_TRY(cudaSetDevice(b->device));
     b->last_launches = 0;
-    if ((rc = forces(b, stream, true))) return rc;  // same forces, plus per-system potential energy
-    b->forces_valid = true;
+    if ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, true))) return rc;  // plus the potential energy
     if (launch_kinetic_systems(b->prec, device_system(b->integ), buffers(b), b->d_body0.p, b->d_free0.p, b->S,
                                b->d_ke.p, stream) < 0)
         return set_error(RBX_ERR_CUDA, "kinetic-energy kernel failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -483,8 +533,7 @@ int rbx_batch_forces(rbx_batch* b, void* stream, double* forces_out, double* ene
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
     BATCH_TRY(cudaSetDevice(b->device));
     b->last_launches = 0;
-    if ((rc = forces(b, stream, true))) return rc;
-    b->forces_valid = true;
+    if ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, true))) return rc;
     cudaStream_t st = (cudaStream_t)stream;
     const DevBuf d = buffers(b);
     if (forces_out) {
@@ -503,6 +552,39 @@ int rbx_batch_get_num_dof(rbx_batch* b, int* dof) {
     if (b->dof.empty()) return set_error(RBX_ERR_STATE, "degrees of freedom are known after rbx_batch_set_state");
     std::copy(b->dof.begin(), b->dof.end(), dof);
     return RBX_OK;
+}
+
+int rbx_batch_status(rbx_batch* b, void* stream, int* system_status, int* num_failed) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (b->body0_h.empty()) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
+    BATCH_TRY(cudaSetDevice(b->device));
+    std::vector<unsigned int> fs(b->S);
+    BATCH_TRY(cudaMemcpyAsync(fs.data(), b->d_sys_status.p, sizeof(unsigned int) * (size_t)b->S, cudaMemcpyDeviceToHost,
+                              (cudaStream_t)stream));
+    std::vector<uint8_t> bb, fb;
+    unsigned int count = 0;
+    if ((rc = failure_flags(b->integ, stream, bb, fb, &count))) return rc;  // synchronises the stream
+    std::vector<int> failed(b->S, 0);
+    for (int s = 0; s < b->S; s++) {
+        bool bad = fs[s] != 0;
+        if (count) {
+            for (int L = b->body0_h[s]; L < b->body0_h[s + 1] && !bad; L++) bad = bb[L] != 0;
+            for (int j = b->free0_h[s]; j < b->free0_h[s + 1] && !bad; j++) bad = fb[j] != 0;
+        }
+        failed[s] = bad ? RBX_ERR_NUMERIC : RBX_OK;
+    }
+    int n = 0, first = -1;
+    for (int s = 0; s < b->S; s++)
+        if (failed[s]) {
+            if (first < 0) first = s;
+            n++;
+        }
+    if (system_status) std::copy(failed.begin(), failed.end(), system_status);
+    if (num_failed) *num_failed = n;
+    if (!n) return RBX_OK;
+    return set_error(RBX_ERR_NUMERIC, "%d of %d systems failed (first: system %d): a non-finite state after a step, "
+                     "or a force beyond the fixed-point range", n, b->S, first);
 }
 
 int rbx_batch_autotune(rbx_batch* b, void* stream, double dt, int trial_steps, int* chosen) {

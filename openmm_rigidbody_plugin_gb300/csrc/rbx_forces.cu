@@ -6,19 +6,25 @@
 //   E = K q_i q_j (1/r + k_rf r^2 - c_rf) + 4 eps_ij ((sig_ij/r)^12 - (sig_ij/r)^6),  r < rc,
 // Lorentz-Berthelot combination, minimum image in a cubic box, pairs of one rigid body excluded.
 //
-// One evaluation, all systems at once:
-//   1. ff_bin      one thread per interacting atom: cell index, cell counts
-//   2. ff_scan     one block per system: exclusive scan of its cells' counts (and count reset)
-//   3. ff_scatter  one thread per interacting atom: slot in its cell (single-cell systems keep
-//                  their atom order and need no atomics)
-//   4. ff_sort     one thread per cell of a multi-cell box: sorts the cell by atom index (the
-//                  cell contents, and so every force sum, are in a fixed order)
-//   5. ff_gather   one thread per atom: cell-ordered copies of positions (wrapped into the box)
-//                  and parameters, so that neighbour loads are contiguous
-//   6. ff_force_cells / ff_force_box  one block per cell (multi-cell boxes) or per 64 atoms of a
-//                  single-cell box: neighbour atoms staged in shared memory, all pairs within the
-//                  cutoff, no atomics; forces written as OpenMM fixed point (2^32) to the slot
-//   7. ff_energy   (energy evaluations only) one block per system: fixed-order FP64 sum.
+// Forces come from neighbour lists (Verlet lists with a skin of up to 0.1 nm) that each system
+// rebuilds when one of its atoms has moved more than half the skin since its last build, and at the
+// first evaluation of every call (so a call's results depend only on the positions it starts from,
+// never on when earlier calls rebuilt). One evaluation, all systems at once:
+//   1. ff_check    one thread per interacting atom: position (wrapped into the box) in the list
+//                  order, and the displacement since the last build (flags the system's rebuild)
+//   then, for the flagged systems only (the kernels return at once for the others):
+//   2. ff_bin      cell index and cell counts, cells of at least cutoff + skin per edge
+//   3. ff_scan     one block per system: exclusive scan of its cells' counts (and count reset)
+//   4. ff_scatter  slot in its cell (single-cell systems keep their atom order and need no atomics)
+//   5. ff_sort     one warp per cell of a multi-cell box: sorts the cell by atom index
+//   6. ff_gather   cell-ordered copies of positions and parameters, and the build positions
+//   7. ff_build_cells / ff_build_box  one block per cell (27 neighbour cells staged in shared
+//                  memory) or per 64 atoms of a single-cell box (all atoms, minimum image): every
+//                  pair within cutoff + skin that is not excluded, in a fixed order, into the lists
+//   8. ff_force_list  one thread per atom (all systems): its list, pairs within the cutoff, no
+//                  atomics; forces written as OpenMM fixed point (2^32) to the slot; the pair terms
+//                  are summed in the list's order, which a call fixes at its first evaluation
+//   9. ff_energy   (energy evaluations only) one block per system: fixed-order FP64 sum.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -49,10 +55,43 @@ __device__ __forceinline__ int wrap_cell(float x, float invL, int nc) {
     return c < 0 ? 0 : (c >= nc ? nc - 1 : c);
 }
 
+// Position of an interacting atom wrapped into [0, L) and its minimum-image displacement.
+__device__ __forceinline__ float3 wrap_box(float3 x, const FFSys& S) {
+    x.x -= S.L * floorf(x.x * S.invL);
+    x.y -= S.L * floorf(x.y * S.invL);
+    x.z -= S.L * floorf(x.z * S.invL);
+    return x;
+}
+__device__ __forceinline__ float3 min_image(float dx, float dy, float dz, const FFSys& S) {
+    return make_float3(dx - S.L * rintf(dx * S.invL), dy - S.L * rintf(dy * S.invL), dz - S.L * rintf(dz * S.invL));
+}
+
+// 1. Current positions in the order of the last build, and the rebuild test. The list order of a
+// system is fixed between its builds, so the p-th entry stays the same atom (cell_list[p]).
+__global__ void ff_check(FFDev D, DevBuf B, int prec) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.n_int) return;
+    const int s = D.isys[p];  // list positions [i0, i1) belong to system s, as the atom indices do
+    const FFSys S = D.sys[s];
+    const int k = D.cell_list[p];
+    const float3 x = wrap_box(atom_position(B, prec, D.iatom[k]), S);
+    float4 c = D.cpos[p];
+    c.x = x.x;
+    c.y = x.y;
+    c.z = x.z;
+    D.cpos[p] = c;
+    if (D.rebuild[s]) return;
+    const float4 r = D.xref[p];
+    const float3 d = min_image(x.x - r.x, x.y - r.y, x.z - r.z, S);
+    if (fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z)) > S.half_skin2) D.rebuild[s] = 1;
+}
+
 __global__ void ff_bin(FFDev D, DevBuf B, int prec) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= D.n_int) return;
-    const FFSys S = D.sys[D.isys[k]];
+    const int s = D.isys[k];
+    if (!D.rebuild[s]) return;
+    const FFSys S = D.sys[s];
     if (S.nc == 1) {
         D.cell_of[k] = S.c0;
         return;
@@ -67,6 +106,7 @@ __global__ void ff_bin(FFDev D, DevBuf B, int prec) {
 // Exclusive scan of one system's cell counts, in chunks of blockDim.x; the counts are reset.
 __global__ void ff_scan(FFDev D) {
     __shared__ int s[256];
+    if (!D.rebuild[blockIdx.x]) return;
     const FFSys S = D.sys[blockIdx.x];
     const int ncell = S.nc * S.nc * S.nc;
     if (S.nc == 1) {
@@ -103,8 +143,9 @@ __global__ void ff_scan(FFDev D) {
 __global__ void ff_scatter(FFDev D) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= D.n_int) return;
-    const FFSys S = D.sys[D.isys[k]];
-    if (S.nc == 1) {
+    const int s = D.isys[k];
+    if (!D.rebuild[s]) return;
+    if (D.sys[s].nc == 1) {
         D.cell_list[k] = k;  // one cell: interacting-atom order
         return;
     }
@@ -113,8 +154,8 @@ __global__ void ff_scatter(FFDev D) {
 }
 
 // Sort each cell of a multi-cell box by interacting-atom index, so that every cell, and so every
-// force sum, is in a fixed order. One warp per cell: the cell is staged in shared memory and each
-// lane ranks its entries against all of them (the entries are distinct, so the ranks are a
+// list, is in a fixed order. One warp per cell: the cell is staged in shared memory and each lane
+// ranks its entries against all of them (the entries are distinct, so the ranks are a
 // permutation); a cell larger than the stage falls back to an insertion sort by one lane. The one
 // cell of a single-cell box is already in order.
 constexpr int kSortWarps = 4, kSortStage = 512;
@@ -123,6 +164,7 @@ __global__ void __launch_bounds__(32 * kSortWarps) ff_sort(FFDev D) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int w = blockIdx.x * kSortWarps + warp;
     if (w >= D.n_mc) return;
+    if (!D.rebuild[D.mc_sys[w]]) return;
     const int c = D.mc_cell[w];
     const int b = D.cell_start[c], e = D.cell_start[c + 1], n = e - b;
     int* s = stage[warp];
@@ -148,52 +190,21 @@ __global__ void __launch_bounds__(32 * kSortWarps) ff_sort(FFDev D) {
     }
 }
 
-// Cell-ordered copies: position wrapped into [0, L) and scaled charge; sigma/2, sqrt(epsilon), body
-// id and device slot.
+// Cell-ordered copies (rebuilt systems): position wrapped into [0, L) and scaled charge; sigma/2,
+// sqrt(epsilon), body id and device slot; the build positions.
 __global__ void ff_gather(FFDev D, DevBuf B, int prec) {
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= D.n_int) return;
+    const int s = D.isys[p];
+    if (!D.rebuild[s]) return;
     const int k = D.cell_list[p];
     const int slot = D.iatom[k];
-    const FFSys S = D.sys[D.isys[k]];
-    float3 x = atom_position(B, prec, slot);
-    x.x -= S.L * floorf(x.x * S.invL);
-    x.y -= S.L * floorf(x.y * S.invL);
-    x.z -= S.L * floorf(x.z * S.invL);
+    const float3 x = wrap_box(atom_position(B, prec, slot), D.sys[s]);
     const float4 q = D.param[k];  // scaled charge, sigma/2, sqrt(eps), body id bits
-    D.cpos[p] = make_float4(x.x, x.y, x.z, q.x);
+    const float4 c = make_float4(x.x, x.y, x.z, q.x);
+    D.cpos[p] = c;
+    D.xref[p] = c;
     D.cpar[p] = make_float4(q.y, q.z, q.w, __int_as_float(slot));
-}
-
-constexpr int kFT = 64;  // threads of a single-box force block; also its staged chunk of atoms
-
-// Compensated FP32 accumulator (Knuth's two-sum): the running sum keeps its rounding error in `lo`.
-struct ESum {
-    float hi = 0.0f, lo = 0.0f;
-    __device__ __forceinline__ void add(float x) {
-        const float s = hi + x, bp = s - hi;
-        lo += (hi - (s - bp)) + (x - bp);
-        hi = s;
-    }
-    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
-};
-
-// The pair's force on i and (energy evaluations) its energy, formed in FP32 and summed with
-// compensation, for a pair known to be within the cutoff and not excluded.
-template <bool ENERGY>
-__device__ __forceinline__ void pair_interact(const FFSys& S, const FFDev& D, float4 xi, float4 pi, float4 xq, float4 pq,
-                                              float dx, float dy, float dz, float r2, float& fx, float& fy, float& fz,
-                                              ESum& e) {
-    if (D.fcap > 0.0f && r2 < 1e-8f) return;  // relaxation: coincident atoms have no direction
-    const float inv_r2 = 1.0f / r2, inv_r = rsqrtf(r2);
-    const float qq = xi.w * xq.w;
-    const float sig = pi.x + pq.x, eps = pi.y * pq.y;
-    const float s2 = sig * sig * inv_r2, s6 = s2 * s2 * s2;
-    const float g = qq * (inv_r * inv_r2 - 2.0f * S.krf) + 4.0f * eps * (12.0f * s6 * s6 - 6.0f * s6) * inv_r2;
-    fx = fmaf(g, dx, fx);
-    fy = fmaf(g, dy, fy);
-    fz = fmaf(g, dz, fz);
-    if (ENERGY) e.add(qq * (inv_r + S.krf * r2 - S.crf) + 4.0f * eps * (s6 * s6 - s6));
 }
 
 // Excluded pairs: the atom itself (same slot) and atoms of the same rigid body. Ids are compared
@@ -204,67 +215,32 @@ __device__ __forceinline__ bool excluded(float4 pi, float4 pq) {
     return body > 0 && __float_as_int(pq.z) == body;
 }
 
-// Cell kernel (many warps per SM): the cutoff test first, and the neighbour's parameters read from
-// shared memory only for pairs within it (about 15 % of the candidates of 27 cells).
-template <bool ENERGY>
-__device__ __forceinline__ void pair_term_cutoff_first(const FFSys& S, const FFDev& D, float4 xi, float4 pi, float4 xq,
-                                                       const float4* __restrict__ pqp, float dx, float dy, float dz,
-                                                       float& fx, float& fy, float& fz, ESum& e) {
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    if (r2 >= S.rc2) return;
-    const float4 pq = *pqp;
-    if (excluded(pi, pq)) return;
-    pair_interact<ENERGY>(S, D, xi, pi, xq, pq, dx, dy, dz, r2, fx, fy, fz, e);
-}
-
-// Single-box kernel (few warps, each thread a long loop): the parameters loaded with the position
-// and the exclusions tested first keep the loop's dependent chain short (measured on 512 waters:
-// 0.19 ms per evaluation against 0.25 ms with the cutoff test first).
-template <bool ENERGY>
-__device__ __forceinline__ void pair_term_exclusions_first(const FFSys& S, const FFDev& D, float4 xi, float4 pi,
-                                                           float4 xq, float4 pq, float dx, float dy, float dz,
-                                                           float& fx, float& fy, float& fz, ESum& e) {
-    if (excluded(pi, pq)) return;
-    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    if (r2 >= S.rc2) return;
-    pair_interact<ENERGY>(S, D, xi, pi, xq, pq, dx, dy, dz, r2, fx, fy, fz, e);
-}
-
-template <bool ENERGY>
-__device__ __forceinline__ void store_force(const FFDev& D, long long* __restrict__ force, int stride, int p, float4 pi,
-                                            float fx, float fy, float fz, const ESum& e) {
-    if (D.fcap > 0.0f) {  // relaxation: cap the magnitude
-        const float f2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
-        if (f2 > D.fcap * D.fcap) {
-            const float s = D.fcap * rsqrtf(f2);
-            fx *= s;
-            fy *= s;
-            fz *= s;
-        }
+// Appends neighbour j (list position) to atom p's list; a full list marks the system as failed
+// (the capacity is sized from the densest system with a wide margin, so this does not happen in a
+// liquid).
+template <class IDX>
+__device__ __forceinline__ void list_append(const FFDev& D, int p, int s, int i0, int& n, int j) {
+    if (n < D.cap) {
+        IDX* nb = (IDX*)D.nbr + (size_t)(p >> 5) * 32 * D.cap + (p & 31);
+        nb[(size_t)n * 32] = (IDX)(j - i0);
+    } else if (n == D.cap && D.sys_status) {
+        atomicOr(D.sys_status + s, 2u);
     }
-    // keep each component inside the 2^32 fixed-point range (|F| < 2^31 kJ/mol/nm)
-    const float kMaxF = 2.0e9f;
-    fx = fminf(fmaxf(fx, -kMaxF), kMaxF);
-    fy = fminf(fmaxf(fy, -kMaxF), kMaxF);
-    fz = fminf(fmaxf(fz, -kMaxF), kMaxF);
-    const int slot = __float_as_int(pi.w);
-    force[slot] = __float2ll_rn(fx * 0x1p32f);
-    force[slot + stride] = __float2ll_rn(fy * 0x1p32f);
-    force[slot + 2 * stride] = __float2ll_rn(fz * 0x1p32f);
-    if (ENERGY) D.e_atom[p] = 0.5 * e.value();
+    n++;
 }
 
-// Multi-cell boxes: one block per cell. The block's kFC threads take the cell's atoms (kFC at a
-// time: 64, 128 or 256, chosen by the batch's autotuner; a cell of at least a cutoff per edge
-// holds 73 or more atoms at liquid density); each of the 27 neighbour cells is staged in shared
-// memory, kFC atoms at a time, with its periodic
-// image shift applied once (exact for pairs within the cutoff: the cell edge is at least the
-// cutoff and there are at least three cells per edge).
-template <bool ENERGY, int kFC>
-__global__ void __launch_bounds__(kFC) ff_force_cells(FFDev D, long long* __restrict__ force, int stride) {
+// 7a. Lists of multi-cell boxes: one block per cell; its atoms kFC at a time, each of the 27
+// neighbour cells staged in shared memory kFC atoms at a time with its periodic image shift applied
+// once (exact for pairs within cutoff + skin: the cell edge is at least that and there are at
+// least three cells per edge).
+template <int kFC, class IDX>
+__global__ void __launch_bounds__(kFC) ff_build_cells(FFDev D) {
     __shared__ float4 sx[kFC], sp[kFC];
-    const int c = D.mc_cell[blockIdx.x];
-    const FFSys S = D.sys[D.mc_sys[blockIdx.x]];
+    const int w = blockIdx.x;
+    const int s = D.mc_sys[w];
+    if (!D.rebuild[s]) return;
+    const int c = D.mc_cell[w];
+    const FFSys S = D.sys[s];
     const int b = D.cell_start[c], e = D.cell_start[c + 1];
     const int local = c - S.c0, nc = S.nc;
     const int cx = local % nc, cy = (local / nc) % nc, cz = local / (nc * nc);
@@ -274,8 +250,7 @@ __global__ void __launch_bounds__(kFC) ff_force_cells(FFDev D, long long* __rest
         const bool mine = p < e;
         const float4 xi = mine ? D.cpos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
         const float4 pi = mine ? D.cpar[p] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        ESum en;
+        int n = 0;
         for (int oz = -1; oz <= 1; oz++) {
             int z = cz + oz;
             const float shz = z < 0 ? -S.L : (z >= nc ? S.L : 0.f);
@@ -288,8 +263,8 @@ __global__ void __launch_bounds__(kFC) ff_force_cells(FFDev D, long long* __rest
                     int x = cx + ox;
                     const float shx = x < 0 ? -S.L : (x >= nc ? S.L : 0.f);
                     x = x < 0 ? x + nc : (x >= nc ? x - nc : x);
-                    const int n = S.c0 + (z * nc + y) * nc + x;
-                    const int qb = D.cell_start[n], qe = D.cell_start[n + 1];
+                    const int cn = S.c0 + (z * nc + y) * nc + x;
+                    const int qb = D.cell_start[cn], qe = D.cell_start[cn + 1];
                     for (int j0 = qb; j0 < qe; j0 += kFC) {
                         __syncthreads();
                         if (j0 + t < qe) {
@@ -305,37 +280,35 @@ __global__ void __launch_bounds__(kFC) ff_force_cells(FFDev D, long long* __rest
                             const int m = min(kFC, qe - j0);
                             for (int j = 0; j < m; j++) {
                                 const float4 xq = sx[j];
-                                pair_term_cutoff_first<ENERGY>(S, D, xi, pi, xq, sp + j, xi.x - xq.x, xi.y - xq.y,
-                                                               xi.z - xq.z, fx, fy, fz, en);
+                                const float dx = xi.x - xq.x, dy = xi.y - xq.y, dz = xi.z - xq.z;
+                                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                                if (r2 < S.rl2 && !excluded(pi, sp[j])) list_append<IDX>(D, p, s, S.i0, n, j0 + j);
                             }
                         }
                     }
                 }
             }
         }
-        if (mine) store_force<ENERGY>(D, force, stride, p, pi, fx, fy, fz, en);
+        if (mine) D.ncnt[p] = min(n, D.cap);
     }
 }
 
-// Single-cell boxes (fewer than three cutoffs across): one block per 64 atoms of the box, all
-// atoms of the box streamed through shared memory, minimum image per pair. Each atom has kFK
-// threads (consecutive lanes), each taking every kFK-th staged neighbour; their partial sums are
-// combined by a fixed butterfly of shuffles, so the order of every sum is fixed. Small boxes are
-// latency bound: kFK threads per atom give kFK times the parallelism and 1/kFK of the loop.
-constexpr int kFK = 8;
-template <bool ENERGY>
-__global__ void __launch_bounds__(kFT * kFK) ff_force_box(FFDev D, long long* __restrict__ force, int stride) {
-    constexpr int NT = kFT * kFK;  // threads, and staged neighbours per barrier pair
-    __shared__ float4 sx[NT], sp[NT];
-    const FFSys S = D.sys[D.sc_sys[blockIdx.x]];
-    const int t = threadIdx.x, k = t % kFK;
-    const int p = D.sc_i0[blockIdx.x] + t / kFK;
+// 7b. Lists of single-cell boxes (fewer than three list cells per edge): one block per 64 atoms, all
+// atoms of the box streamed through shared memory, minimum image per pair.
+constexpr int kBT = 64;
+template <class IDX>
+__global__ void __launch_bounds__(kBT) ff_build_box(FFDev D) {
+    __shared__ float4 sx[kBT], sp[kBT];
+    const int s = D.sc_sys[blockIdx.x];
+    if (!D.rebuild[s]) return;
+    const FFSys S = D.sys[s];
+    const int t = threadIdx.x;
+    const int p = D.sc_i0[blockIdx.x] + t;
     const bool mine = p < S.i1;
     const float4 xi = mine ? D.cpos[p] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 pi = mine ? D.cpar[p] : make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    ESum en;
-    for (int j0 = S.i0; j0 < S.i1; j0 += NT) {
+    int n = 0;
+    for (int j0 = S.i0; j0 < S.i1; j0 += kBT) {
         __syncthreads();
         if (j0 + t < S.i1) {
             sx[t] = D.cpos[j0 + t];
@@ -343,28 +316,95 @@ __global__ void __launch_bounds__(kFT * kFK) ff_force_box(FFDev D, long long* __
         }
         __syncthreads();
         if (mine) {
-            const int m = min(NT, S.i1 - j0);
-            for (int j = k; j < m; j += kFK) {
+            const int m = min(kBT, S.i1 - j0);
+            for (int j = 0; j < m; j++) {
                 const float4 xq = sx[j];
-                float dx = xi.x - xq.x, dy = xi.y - xq.y, dz = xi.z - xq.z;
-                dx -= S.L * rintf(dx * S.invL);
-                dy -= S.L * rintf(dy * S.invL);
-                dz -= S.L * rintf(dz * S.invL);
-                pair_term_exclusions_first<ENERGY>(S, D, xi, pi, xq, sp[j], dx, dy, dz, fx, fy, fz, en);
+                const float3 d = min_image(xi.x - xq.x, xi.y - xq.y, xi.z - xq.z, S);
+                const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+                if (r2 < S.rl2 && !excluded(pi, sp[j])) list_append<IDX>(D, p, s, S.i0, n, j0 + j);
             }
         }
     }
-#pragma unroll
-    for (int o = kFK / 2; o > 0; o >>= 1) {
-        fx += __shfl_xor_sync(0xffffffffu, fx, o);
-        fy += __shfl_xor_sync(0xffffffffu, fy, o);
-        fz += __shfl_xor_sync(0xffffffffu, fz, o);
-        if (ENERGY) {
-            en.hi += __shfl_xor_sync(0xffffffffu, en.hi, o);
-            en.lo += __shfl_xor_sync(0xffffffffu, en.lo, o);
+    if (mine) D.ncnt[p] = min(n, D.cap);
+}
+
+// Compensated FP32 accumulator (Knuth's two-sum): the running sum keeps its rounding error in `lo`.
+struct ESum {
+    float hi = 0.0f, lo = 0.0f;
+    __device__ __forceinline__ void add(float x) {
+        const float s = hi + x, bp = s - hi;
+        lo += (hi - (s - bp)) + (x - bp);
+        hi = s;
+    }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+template <bool ENERGY>
+__device__ __forceinline__ void store_force(const FFDev& D, long long* __restrict__ force, int stride, int k, int slot,
+                                            float fx, float fy, float fz, const ESum& e, int si) {
+    if (D.fcap > 0.0f) {  // relaxation: cap the magnitude
+        const float f2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
+        if (f2 > D.fcap * D.fcap) {
+            const float s = D.fcap * rsqrtf(f2);
+            fx *= s;
+            fy *= s;
+            fz *= s;
         }
     }
-    if (mine && k == 0) store_force<ENERGY>(D, force, stride, p, pi, fx, fy, fz, en);
+    // keep each component inside the 2^32 fixed-point range (|F| < 2^31 kJ/mol/nm); a non-finite
+    // force, or one beyond the range (atoms on top of each other), marks its system as failed
+    const float kMaxF = 2.0e9f;
+    if (D.fcap <= 0.0f && !(fabsf(fx) < kMaxF && fabsf(fy) < kMaxF && fabsf(fz) < kMaxF) && D.sys_status)
+        atomicOr(D.sys_status + si, 1u);
+    fx = fminf(fmaxf(fx, -kMaxF), kMaxF);
+    fy = fminf(fmaxf(fy, -kMaxF), kMaxF);
+    fz = fminf(fmaxf(fz, -kMaxF), kMaxF);
+    force[slot] = __float2ll_rn(fx * 0x1p32f);
+    force[slot + stride] = __float2ll_rn(fy * 0x1p32f);
+    force[slot + 2 * stride] = __float2ll_rn(fz * 0x1p32f);
+    if (ENERGY) D.e_atom[k] = 0.5 * e.value();
+}
+
+// 8. Forces from the lists: one thread per atom (list position p), its entries in list order; a
+// pair beyond the cutoff adds exactly nothing (its term is selected to zero, so the loop does not
+// diverge). The pair term is OpenMM's CutoffPeriodic form: reaction-field Coulomb and unshifted LJ.
+template <bool ENERGY, class IDX>
+__global__ void __launch_bounds__(128) ff_force_list(FFDev D, long long* __restrict__ force, int stride) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= D.n_int) return;
+    const int s = D.isys[p];
+    const FFSys S = D.sys[s];
+    const float4 xi = D.cpos[p];
+    const float4 pi = D.cpar[p];
+    const int n = D.ncnt[p];
+    const IDX* __restrict__ nb = (const IDX*)D.nbr + (size_t)(p >> 5) * 32 * D.cap + (p & 31);
+    const float4* __restrict__ cpos = D.cpos + S.i0;
+    const float4* __restrict__ cpar = D.cpar + S.i0;
+    const bool relax = D.fcap > 0.0f;
+    float fx = 0.f, fy = 0.f, fz = 0.f;
+    ESum en;
+    for (int e = 0; e < n; e++) {
+        const int j = (int)nb[(size_t)e * 32];
+        const float4 xq = cpos[j];
+        const float2 pq = *(const float2*)(cpar + j);
+        const float3 d = min_image(xi.x - xq.x, xi.y - xq.y, xi.z - xq.z, S);
+        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+        // relaxation: coincident atoms have no direction
+        const bool in = r2 < S.rc2 && !(relax && r2 < 1e-8f);
+        const float r2s = in ? r2 : 1.0f;
+        const float inv_r = rsqrtf(r2s), inv_r2 = inv_r * inv_r;
+        const float qq = xi.w * xq.w;
+        const float sig = pi.x + pq.x, eps = pi.y * pq.y;
+        const float s2 = sig * sig * inv_r2, s6 = s2 * s2 * s2;
+        float g = qq * (inv_r * inv_r2 - 2.0f * S.krf) + 4.0f * eps * (12.0f * s6 * s6 - 6.0f * s6) * inv_r2;
+        g = in ? g : 0.0f;
+        fx = fmaf(g, d.x, fx);
+        fy = fmaf(g, d.y, fy);
+        fz = fmaf(g, d.z, fz);
+        if (ENERGY && in) en.add(qq * (inv_r + S.krf * r2 - S.crf) + 4.0f * eps * (s6 * s6 - s6));
+    }
+    const int k = D.cell_list[p];
+    store_force<ENERGY>(D, force, stride, k, __float_as_int(pi.w), fx, fy, fz, en, s);
 }
 
 __global__ void ff_energy(FFDev D) {
@@ -400,39 +440,51 @@ int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* 
     if (D.n_int == 0) return 0;
     const int t = 256, g = (D.n_int + t - 1) / t;
     int n = 0;
+    ff_check<<<g, t, 0, st>>>(D, B, prec);
     ff_bin<<<g, t, 0, st>>>(D, B, prec);
     ff_scan<<<D.S, 256, 0, st>>>(D);
     ff_scatter<<<g, t, 0, st>>>(D);
-    n += 3;
+    n += 4;
     if (D.n_mc) {
         ff_sort<<<(D.n_mc + kSortWarps - 1) / kSortWarps, 32 * kSortWarps, 0, st>>>(D);
         n++;
     }
     ff_gather<<<g, t, 0, st>>>(D, B, prec);
     n++;
-    long long* f = const_cast<long long*>(B.force);
+    // list builds: block size of the cell kernel chosen by the autotuner (results do not depend
+    // on it: every list is built in the same order)
     if (D.n_mc) {
-        // block size: results do not depend on it (each atom's pairs are summed in the same order)
-        switch (D.cell_threads) {
-            case 64:
-                if (energy) ff_force_cells<true, 64><<<D.n_mc, 64, 0, st>>>(D, f, B.stride);
-                else ff_force_cells<false, 64><<<D.n_mc, 64, 0, st>>>(D, f, B.stride);
-                break;
-            case 256:
-                if (energy) ff_force_cells<true, 256><<<D.n_mc, 256, 0, st>>>(D, f, B.stride);
-                else ff_force_cells<false, 256><<<D.n_mc, 256, 0, st>>>(D, f, B.stride);
-                break;
-            default:
-                if (energy) ff_force_cells<true, 128><<<D.n_mc, 128, 0, st>>>(D, f, B.stride);
-                else ff_force_cells<false, 128><<<D.n_mc, 128, 0, st>>>(D, f, B.stride);
+        if (D.nbr16) {
+            switch (D.cell_threads) {
+                case 64: ff_build_cells<64, unsigned short><<<D.n_mc, 64, 0, st>>>(D); break;
+                case 256: ff_build_cells<256, unsigned short><<<D.n_mc, 256, 0, st>>>(D); break;
+                default: ff_build_cells<128, unsigned short><<<D.n_mc, 128, 0, st>>>(D);
+            }
+        } else {
+            switch (D.cell_threads) {
+                case 64: ff_build_cells<64, unsigned int><<<D.n_mc, 64, 0, st>>>(D); break;
+                case 256: ff_build_cells<256, unsigned int><<<D.n_mc, 256, 0, st>>>(D); break;
+                default: ff_build_cells<128, unsigned int><<<D.n_mc, 128, 0, st>>>(D);
+            }
         }
         n++;
     }
     if (D.n_sc) {
-        if (energy) ff_force_box<true><<<D.n_sc, kFT * kFK, 0, st>>>(D, f, B.stride);
-        else ff_force_box<false><<<D.n_sc, kFT * kFK, 0, st>>>(D, f, B.stride);
+        if (D.nbr16) ff_build_box<unsigned short><<<D.n_sc, kBT, 0, st>>>(D);
+        else ff_build_box<unsigned int><<<D.n_sc, kBT, 0, st>>>(D);
         n++;
     }
+    if (cudaMemsetAsync(D.rebuild, 0, (size_t)D.S, st) != cudaSuccess) return -1;
+    long long* f = const_cast<long long*>(B.force);
+    const int gf = (D.n_int + 127) / 128;
+    if (D.nbr16) {
+        if (energy) ff_force_list<true, unsigned short><<<gf, 128, 0, st>>>(D, f, B.stride);
+        else ff_force_list<false, unsigned short><<<gf, 128, 0, st>>>(D, f, B.stride);
+    } else {
+        if (energy) ff_force_list<true, unsigned int><<<gf, 128, 0, st>>>(D, f, B.stride);
+        else ff_force_list<false, unsigned int><<<gf, 128, 0, st>>>(D, f, B.stride);
+    }
+    n++;
     if (energy) {
         ff_energy<<<D.S, 256, 0, st>>>(D);
         n++;

@@ -79,6 +79,13 @@ struct rbx_integrator {
     std::vector<double> invm, invI;     // [nb], [nb*3]
     std::vector<uint8_t> cls;           // [nb]
     std::vector<int> dof;               // [nb]
+    // Atoms whose body index is used once: free atoms here, one-atom bodies in the reference
+    // (RigidBodySystem.cpp:37-47), which counts 5 or 6 degrees of freedom for each; single_dof is
+    // that count at the last state upload (rbx_get_num_dof_reference).
+    std::vector<int> singletons;
+    int single_dof = 0;
+    DevArray<int> d_single_loc;
+    DevArray<double> d_single_x;
     // Library order, the order of every device array: bodies by the lowest device slot of their
     // atoms, so that a tile's atoms occupy a narrow slot range. Re-planned when slots change.
     std::vector<int> lib_body;          // [nb] library position -> reference body
@@ -103,6 +110,9 @@ struct rbx_integrator {
     DevArray<int> d_dof, d_setup_counts;
     bool host_geom_valid = true;    // host copies of the geometry match the device (false after a device setup)
     DevArray<uint8_t> d_cls;
+    // failure detector of the step kernels (DevSys::status): counter and flag bytes
+    DevArray<unsigned int> d_status;
+    DevArray<uint8_t> d_body_bad, d_free_bad;
     DevArray<unsigned char> d_fixed;  // float or double SoA
     DevArray<double> d_ke_partial, d_ke_out;
     DevArray<unsigned int> d_ke_count;
@@ -139,6 +149,7 @@ struct rbx_integrator {
         s.d = d_fixed.p; s.atom_loc = d_atom_loc.p; s.free_loc = d_free_loc.p; s.tile_body0 = d_tiles.p;
         s.ref_start = refined ? (void*)d_ref_start.p : nullptr;
         s.ref_out = refined ? d_ref_out.p : nullptr;
+        s.status = d_status.p; s.body_bad = d_body_bad.p; s.free_bad = d_free_bad.p;
         return s;
     }
     ~rbx_integrator() {
@@ -154,6 +165,23 @@ struct rbx_integrator {
 };
 
 rbx::DevSys rbx::device_system(const rbx_integrator* h) { return h->sys(); }
+
+int rbx::failure_flags(rbx_integrator* h, void* stream, std::vector<uint8_t>& body_bad, std::vector<uint8_t>& free_bad,
+                       unsigned int* count) {
+    CUDA_TRY(cudaSetDevice(h->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemcpyAsync(h->h_ke + 7, h->d_status.p, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    unsigned int c = 0;
+    std::memcpy(&c, h->h_ke + 7, sizeof c);
+    *count = c;
+    body_bad.assign(h->nb, 0);
+    free_bad.assign(h->nf, 0);
+    if (!c) return RBX_OK;
+    if (h->nb) CUDA_TRY(cudaMemcpy(body_bad.data(), h->d_body_bad.p, h->nb, cudaMemcpyDeviceToHost));
+    if (h->nf) CUDA_TRY(cudaMemcpy(free_bad.data(), h->d_free_bad.p, h->nf, cudaMemcpyDeviceToHost));
+    return RBX_OK;
+}
 
 namespace {
 // Host copies of the plan after a re-plan on the device: slots and free-atom order from the device,
@@ -556,6 +584,8 @@ int replan_device(rbx_integrator* h, const int* location, int nslots) {
     if (!rc) rc = regather(h->d_dof, 1, nbp, nb, idx_body, 4);
     if (!rc) rc = regather(h->d_fixed, 3, nbap, nba, idx_atom, es);
     if (!rc) rc = regather(h->d_bmass, 1, nbap, nba, idx_atom, 8);
+    if (!rc) rc = regather(h->d_body_bad, 1, nbp, nb, idx_body, 1);
+    if (!rc) rc = regather(h->d_free_bad, 1, nfp, nf, idx_free, 1);
     if (!rc && h->d_ref_start.p) {
         // body rows then free-atom rows of one allocation each: gather both parts into a new one
         auto s2 = std::make_shared<DevArray<unsigned char>>();
@@ -596,6 +626,26 @@ int replan_device(rbx_integrator* h, const int* location, int nslots) {
 }
 
 }  // namespace
+
+// Reset the failure detector (a new state replaces the flagged one). Asynchronous on `stream`.
+static int clear_failures(rbx_integrator* h, void* stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    CUDA_TRY(cudaMemsetAsync(h->d_status.p, 0, sizeof(unsigned int), st));
+    CUDA_TRY(cudaMemsetAsync(h->d_body_bad.p, 0, h->d_body_bad.n, st));
+    CUDA_TRY(cudaMemsetAsync(h->d_free_bad.p, 0, h->d_free_bad.n, st));
+    return RBX_OK;
+}
+
+// Degrees of freedom the reference gives a one-atom body at positions x (RigidBody.cpp:65-107):
+// its centre of mass is (0 + x m) * (1/m) (Vec3 division multiplies by the reciprocal), and
+// collinear() takes the displacement x - rcm as the axis. A zero displacement gives a NaN axis,
+// the test fails and the body counts 6; a rounding residue passes it, and the body counts 5.
+static int reference_singleton_dof(const double* x, double m) {
+    const double r = 1.0 / m;
+    bool zero = true;
+    for (int k = 0; k < 3; k++) zero = zero && (x[k] - (0.0 + x[k] * m) * r == 0.0);
+    return zero ? 6 : 5;
+}
 
 extern "C" {
 
@@ -642,6 +692,7 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
         }
         if (in_body) members[compact[id]].push_back(i);
         else h->free_atoms.push_back(i);
+        if (id > 0 && count[id] == 1) h->singletons.push_back(i);
     }
     h->nb = nb;
     h->nf = (int)h->free_atoms.size();
@@ -699,6 +750,10 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
             rc = fail(RBX_ERR_CUDA, "kinetic-energy scratch initialisation failed");
     }
     if (!rc && h->d_state.p) rc = cudaMemset(h->d_state.p, 0, sizeof(double) * 14 * h->nb_pad) == cudaSuccess ? 0 : fail(RBX_ERR_CUDA, "cudaMemset");
+    if (!rc && (h->d_status.alloc(1) != cudaSuccess || h->d_body_bad.alloc(h->nb_pad) != cudaSuccess ||
+                h->d_free_bad.alloc(h->nf_pad) != cudaSuccess))
+        rc = fail(RBX_ERR_CUDA, "cudaMalloc of the failure flags");
+    if (!rc) rc = clear_failures(h, nullptr);
     if (rc) { delete h; return rc; }
     *out = h;
     return RBX_OK;
@@ -784,6 +839,9 @@ int rbx_upload_state(rbx_integrator* h, const double* positions, const double* v
         }
     }
     h->ndof = ndof;
+    if ((rc = clear_failures(h, nullptr))) return rc;
+    h->single_dof = 0;
+    for (int i : h->singletons) h->single_dof += reference_singleton_dof(positions + 3 * (size_t)i, h->masses[i]);
     CUDA_TRY(cudaSetDevice(h->device));
     if ((rc = put_state(h, state))) return rc;
     if ((rc = upload_bodies(h))) return rc;
@@ -808,6 +866,7 @@ int rbx_upload_state_device(rbx_integrator* h, void* stream, const rbx_buffers* 
                       h->d_setup_counts.alloc(2) != cudaSuccess))
         return fail(RBX_ERR_CUDA, "cudaMalloc of setup arrays failed");
     cudaStream_t st = (cudaStream_t)stream;
+    if ((rc = clear_failures(h, stream))) return rc;
     CUDA_TRY(cudaMemsetAsync(h->d_setup_counts.p, 0, 2 * sizeof(int), st));
     SetupOut o{h->d_I.p, h->d_dof.p, h->d_setup_counts.p, (unsigned int*)(h->d_setup_counts.p + 1)};
     if (launch_setup_bodies(h->prec, h->sys(), devbuf(buf), h->d_bmass.p, o, stream) < 0)
@@ -816,6 +875,23 @@ int rbx_upload_state_device(rbx_integrator* h, void* stream, const rbx_buffers* 
     CUDA_TRY(cudaMemcpyAsync(counts, h->d_setup_counts.p, sizeof counts, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     if (counts[1]) return fail(RBX_ERR_NUMERIC, "non-finite rigid-body state from the device setup");
+    int single_dof = 0;
+    if (!h->singletons.empty()) {  // the positions of the one-atom bodies of the reference
+        const int ns = (int)h->singletons.size();
+        if ((rc = ensure_host_plan(h))) return rc;
+        std::vector<int> loc(ns);
+        for (int k = 0; k < ns; k++) loc[k] = h->location[h->singletons[k]];
+        if (!h->d_single_loc.p && (h->d_single_loc.alloc(ns) != cudaSuccess || h->d_single_x.alloc((size_t)3 * ns) != cudaSuccess))
+            return fail(RBX_ERR_CUDA, "cudaMalloc of the one-atom body arrays failed");
+        CUDA_TRY(cudaMemcpyAsync(h->d_single_loc.p, loc.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+        if (launch_store_positions(h->prec, devbuf(buf), h->d_single_loc.p, ns, h->d_single_x.p, nullptr, stream) < 0)
+            return fail(RBX_ERR_CUDA, "position gather failed: %s", cudaGetErrorString(cudaGetLastError()));
+        std::vector<double> x((size_t)3 * ns);
+        CUDA_TRY(cudaMemcpyAsync(x.data(), h->d_single_x.p, x.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+        for (int k = 0; k < ns; k++) single_dof += reference_singleton_dof(&x[3 * (size_t)k], h->masses[h->singletons[k]]);
+    }
+    h->single_dof = single_dof;
     h->ndof = 3 * h->nf + counts[0];
     h->have_state = true;
     h->host_geom_valid = false;
@@ -829,6 +905,48 @@ int rbx_get_num_dof(const rbx_integrator* h, int* out) {
     if (rc) return rc;
     if (!h->have_state) return fail(RBX_ERR_STATE, "degrees of freedom are known after rbx_upload_state");
     *out = h->ndof - h->ncons;  // numDOF = free - constraints + body dof (RigidBodySystem.cpp:130)
+    return RBX_OK;
+}
+
+int rbx_check_state(rbx_integrator* h, void* stream, int* bad_bodies, int* bad_free) {
+    int rc = check(h);
+    if (rc) return rc;
+    std::vector<uint8_t> bb, fb;
+    unsigned int count = 0;
+    if ((rc = rbx::failure_flags(h, stream, bb, fb, &count))) return rc;
+    int nbad_b = 0, nbad_f = 0, first_b = -1, first_f = -1;
+    if (count) {
+        if ((rc = ensure_host_plan(h))) return rc;
+        for (int L = 0; L < h->nb; L++)
+            if (bb[L]) {
+                nbad_b++;
+                const int rb = h->lib_body[L];
+                if (first_b < 0 || rb < first_b) first_b = rb;
+            }
+        for (int j = 0; j < h->nf; j++)
+            if (fb[j]) {
+                nbad_f++;
+                const int a = h->free_atoms[j];
+                if (first_f < 0 || a < first_f) first_f = a;
+            }
+    }
+    if (bad_bodies) *bad_bodies = nbad_b;
+    if (bad_free) *bad_free = nbad_f;
+    if (!count) return RBX_OK;
+    return fail(RBX_ERR_NUMERIC, "non-finite state after a step: %d bodies (first: body %d in ascending body-index "
+                "order) and %d free atoms (first: atom %d)", nbad_b, first_b, nbad_f, first_f);
+}
+
+int rbx_get_num_dof_reference(const rbx_integrator* h, int* out) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!out) return fail(RBX_ERR_INVALID_ARGUMENT, "null output pointer");
+    if (!h->have_state) return fail(RBX_ERR_STATE, "degrees of freedom are known after rbx_upload_state");
+    // numDOF = numFree - numConstraints + sum of body dof (RigidBodySystem.cpp:130): one per free
+    // atom, and the atoms of unique indices as one-atom bodies
+    const int nsingle = (int)h->singletons.size();
+    const int body_dof = h->ndof - 3 * h->nf;
+    *out = (h->nf - nsingle) - h->ncons + body_dof + h->single_dof;
     return RBX_OK;
 }
 
@@ -1009,6 +1127,7 @@ int rbx_set_body_state(rbx_integrator* h, const double* state) {
         for (int k = 0; k < 14; k++) s[h->lib_pos[b] + (size_t)k * h->nb_pad] = state[14 * (size_t)b + k];
     CUDA_TRY(cudaSetDevice(h->device));
     h->ref_phase = 0;
+    if ((rc = clear_failures(h, nullptr))) return rc;
     return put_state(h, s);
 }
 

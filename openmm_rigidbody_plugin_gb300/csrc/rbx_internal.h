@@ -70,6 +70,11 @@ struct DevSys {
     const int* tile_body0;
     void* ref_start;  // null unless refined energies are on (then the step kernels fill it)
     float* ref_out;
+    // Failure detector of the step kernels: a body (library order) or free atom whose new state
+    // is not finite gets its flag byte set and status[0] incremented. Null: not monitored.
+    unsigned int* status;
+    uint8_t* body_bad;  // [nb_pad]
+    uint8_t* free_bad;  // [nf_pad]
 };
 
 struct DevBuf {
@@ -86,8 +91,10 @@ struct DevBuf {
 struct FFSys {
     int a0, a1;   // device slots of the system's atoms
     int i0, i1;   // its interacting atoms, as a range of the interacting-atom list
-    int c0, nc;   // first cell and cells per box edge (1: one cell, all pairs)
+    int c0, nc;   // first cell and cells per box edge of the list build (1: one cell, all pairs)
     float L, invL, rc2, krf, crf;
+    float rl2;         // (cutoff + skin)^2: pairs kept in the neighbour lists
+    float half_skin2;  // (skin/2)^2: an atom moved this far since the build invalidates the lists
 };
 struct FFDev {
     int S, n_int, n_cells;
@@ -99,12 +106,22 @@ struct FFDev {
     int* cell_count;      // [n_cells], zero between evaluations
     int* cell_start;      // [n_cells + 1] (entry c0 + nc^3 of each system ends it)
     int* cell_cursor;     // [n_cells]
-    int* cell_list;       // [n_int] interacting-atom indices in cell order
-    float4* cpos;         // [n_int] cell order: x, y, z, sqrt(K) q
+    int* cell_list;       // [n_int] interacting-atom indices in cell order (of the last list build)
+    float4* cpos;         // [n_int] cell order: x, y, z (wrapped into the box), sqrt(K) q
     float4* cpar;         // [n_int] cell order: sigma/2, sqrt(epsilon), body id, device slot (int bits)
     double* e_atom;       // [n_int] half pair-energy sums (energy evaluations)
+    // Neighbour lists (Verlet lists with a skin), rebuilt per system when one of its atoms has moved
+    // more than half the skin since the last build, and at the first evaluation of every call
+    unsigned char* rebuild;  // [S] 1: rebuild this system's lists before the next force pass
+    float4* xref;            // [n_int] cell order: positions at the last build
+    void* nbr;               // neighbour entries, u16 or u32 (nbr16), j - i0 of the system, in groups
+                             // of 32 atoms: entry e of atom p at (p/32)*32*cap + e*32 + p%32
+    int* ncnt;               // [n_int] entries per atom
+    int cap, nbr16;          // entries per atom allocated; 1: 16-bit entries
     double* energy;       // [S] potential energy per system (kJ/mol)
     float fcap;           // > 0: each atom's force is scaled down to at most this magnitude
+    unsigned int* sys_status;  // [S] set to 1 when a force of the system is non-finite or beyond the
+                               // fixed-point range (never during a capped relaxation)
     int cell_threads;     // block size of the cell kernel: 64, 128 (default) or 256
     // work lists of the force kernels (static): every cell of the multi-cell boxes with its
     // system, and every 64-atom chunk (start in the interacting-atom list) of the single-cell boxes
@@ -214,6 +231,10 @@ int launch_gather_rows(void* dst, const void* src, int rows, size_t ld, int n, c
 
 // Internal views of an integrator for the batched driver (defined in rbx_host.cpp).
 DevSys device_system(const rbx_integrator* h);
+// The failure detector's counter (synchronises `stream`) and, when it is non-zero, the flag bytes of
+// every body (library order, [nb]) and free atom (library order, [nf]); all zero otherwise.
+int failure_flags(rbx_integrator* h, void* stream, std::vector<uint8_t>& body_bad, std::vector<uint8_t>& free_bad,
+                  unsigned int* count);
 // Host copies of the body geometry, fetched from the device after a device-side setup (all of
 // it, or only the degrees of freedom per body).
 int ensure_host_geometry(rbx_integrator* h);

@@ -4,6 +4,7 @@
 // The kinetic-energy kernel reduces [KE_t, KE_r] in FP64 in a fixed order.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cstdio>
 #include <mutex>
 
@@ -475,7 +476,8 @@ __global__ void __launch_bounds__(kKEThreads) kinetic_static_kernel(DevSys S, De
     for (int j = first + (int)threadIdx.x; j < last && j < S.nf; j += kKEThreads) {
         V4 vm = vel[S.free_loc[j]];
         double vx = vm.x, vy = vm.y, vz = vm.z;
-        kt += (vx * vx + vy * vy + vz * vz) / (double)vm.w;
+        // w = 1/m; a massless slot (w = 0, as OpenMM stores virtual sites) carries no kinetic energy
+        if (vm.w != 0) kt += (vx * vx + vy * vy + vz * vz) / (double)vm.w;
     }
     s_t[threadIdx.x] = kt;
     s_r[threadIdx.x] = kr;
@@ -508,21 +510,30 @@ __global__ void __launch_bounds__(kKEThreads) kinetic_static_kernel(DevSys S, De
     }
 }
 
-// Device address of the static scratch, looked up once per device (with that device current).
-static int static_scratch_address(double** out) {
+// Device address of the static scratch on the current device. Outside stream capture it is
+// looked up on every call (a cudaDeviceReset reloads the module, which may move the array) and
+// remembered per device; a call made while `stream` is capturing uses the remembered address,
+// so the first call on a device must come before any capture.
+static int static_scratch_address(cudaStream_t stream, double** out) {
     static std::mutex mu;
     static void* addr[kMaxDevices] = {};
     int dev = -1;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return set_error(RBX_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return set_error(RBX_ERR_UNSUPPORTED, "device %d beyond %d", dev, kMaxDevices);
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    e = cudaStreamIsCapturing(stream, &capture);
+    if (e != cudaSuccess) return set_error(RBX_ERR_CUDA, "cudaStreamIsCapturing: %s", cudaGetErrorString(e));
     std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
+    if (capture == cudaStreamCaptureStatusNone) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_static_ke_scratch);
         if (e != cudaSuccess)
             return set_error(RBX_ERR_CUDA, "cudaGetSymbolAddress of the static scratch: %s", cudaGetErrorString(e));
         addr[dev] = p;
+    } else if (!addr[dev]) {
+        return set_error(RBX_ERR_STATE, "rbx_kinetic_energies_static: the first call on device %d was made "
+                         "during stream capture; make one call before capturing", dev);
     }
     *out = (double*)addr[dev];
     return RBX_OK;
@@ -543,13 +554,17 @@ extern "C" int rbx_kinetic_energies_static(const double* body_state, int num_bod
                          kStaticKEMaxItems, kStaticKEMaxItems, kStaticKEMaxBlocks, num_bodies, num_free);
     if (num_bodies > 0 && (!body_state || !inv_mass || !inv_inertia || body_stride < num_bodies))
         return set_error(RBX_ERR_INVALID_ARGUMENT, "body arrays missing or body_stride < num_bodies");
+    // the kernel indexes row r of body b as b + r * body_stride (r <= 13) in 32-bit arithmetic
+    if (num_bodies > 0 && (long long)body_stride * 14 > (long long)INT_MAX)
+        return set_error(RBX_ERR_UNSUPPORTED, "body_stride %d beyond 32-bit indexing of 14 rows (at most %d)",
+                         body_stride, INT_MAX / 14);
     if (num_free > 0 && (!velm || !free_slots)) return set_error(RBX_ERR_INVALID_ARGUMENT, "free-atom arrays missing");
     if (!out_device) return set_error(RBX_ERR_INVALID_ARGUMENT, "null output");
     if (precision < PREC_SINGLE || precision > PREC_DOUBLE) return set_error(RBX_ERR_INVALID_ARGUMENT, "unknown precision");
-    double* scratch = nullptr;
-    int rc = static_scratch_address(&scratch);
-    if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
+    double* scratch = nullptr;
+    int rc = static_scratch_address(st, &scratch);
+    if (rc) return rc;
     // The array keeps the previous call's contents: the ticket counter must start at zero.
     cudaError_t e = cudaMemsetAsync(scratch + 2 * kStaticKEMaxBlocks, 0, sizeof(unsigned int), st);
     if (e != cudaSuccess) return set_error(RBX_ERR_CUDA, "clearing the static scratch: %s", cudaGetErrorString(e));

@@ -138,6 +138,19 @@ template <> struct PosIO<PREC_DOUBLE> {
 };
 
 
+// Failure detector: the new state of a body or free atom is checked for a non-finite value (NaN
+// or infinity; the check is one sum of already loaded values); a failing unit gets its flag byte
+// and the status counter one increment. Finite values never take the branch.
+__device__ __forceinline__ bool finite_f(float v) { return (__float_as_uint(v) & 0x7f800000u) != 0x7f800000u; }
+__device__ __forceinline__ bool finite_d(double v) {
+    return ((unsigned long long)__double_as_longlong(v) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
+static __device__ __noinline__ void flag_failure(unsigned int* status, uint8_t* flags, int i) {
+    if (!status) return;
+    flags[i] = 1;
+    atomicAdd(status, 1u);
+}
+
 // Shared memory of the double-precision step kernel: sF, sT, sX 3*TA each; sQ 4*TB; sRb 3*TB
 // (double); sW 3*TB; sBody TA (uint16).
 constexpr size_t step_smem_d() {
@@ -205,7 +218,7 @@ __device__ __forceinline__ ff fixed_to_ff(long long v) {
 // float-float pair posq + posqCorrection. Returns false, having written nothing, when a velocity,
 // 1/m or the step lies outside the split's range; the caller then runs the FP64 form.
 template <int KIND>
-__device__ __forceinline__ bool free_atom_ff(const DevBuf& B, double dt_d, int loc) {
+__device__ __forceinline__ bool free_atom_ff(const DevBuf& B, double dt_d, int loc, double& vsum) {
     dq4* vel = (dq4*)B.velm;
     dq4 vm = vel[loc];
     ff v[3], w, dt;
@@ -235,6 +248,7 @@ __device__ __forceinline__ bool free_atom_ff(const DevBuf& B, double dt_d, int l
     vm.y = (double)v[1].hi + (double)v[1].lo;
     vm.z = (double)v[2].hi + (double)v[2].lo;
     vel[loc] = vm;
+    vsum = vm.x + vm.y + vm.z;
     return true;
 }
 
@@ -253,7 +267,11 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
     if (j >= S.nf) return;
     const int loc = __ldg(S.free_loc + j);
     if constexpr (P == PREC_MIXED && !REF) {
-        if (free_atom_ff<KIND>(B, dt, loc)) return;
+        double vsum = 0.0;
+        if (free_atom_ff<KIND>(B, dt, loc, vsum)) {
+            if (!finite_d(vsum)) flag_failure(S.status, S.free_bad, j);
+            return;
+        }
     }
     V4* vel = (V4*)B.velm;
     V4 vm = vel[loc];
@@ -282,6 +300,7 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
     }
     vm.x = v.x; vm.y = v.y; vm.z = v.z;
     vel[loc] = vm;
+    if (!finite_d((double)(v.x + v.y + v.z))) flag_failure(S.status, S.free_bad, j);
 }
 
 // Tile of this block: the body tile (>= 0) or -1 - the free-atom tile. Free-atom tiles are spread
@@ -496,6 +515,9 @@ __global__ void __launch_bounds__(kThreads) step_kernel_d(DevSys S, DevBuf B, do
             st[b + 6 * nbp] = q.w; st[b + 7 * nbp] = q.x; st[b + 8 * nbp] = q.y; st[b + 9 * nbp] = q.z;
         }
         st[b + 10 * nbp] = pi.w; st[b + 11 * nbp] = pi.x; st[b + 12 * nbp] = pi.y; st[b + 13 * nbp] = pi.z;
+        const double chk = ((r.x + r.y) + (r.z + v.x)) + ((v.y + v.z) + (q.w + q.x)) + ((q.y + q.z) + (pi.w + pi.x)) +
+                           (pi.y + pi.z);
+        if (!finite_d(chk)) flag_failure(S.status, S.body_bad, b);
     }
     __syncthreads();
     if (KIND == STEP_PART2) {
@@ -745,6 +767,12 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
             // positions are rebuilt from exactly the r and q stored below, so that they are a
             // function of the stored state alone (sync_positions_kernel rebuilds them identically)
             rotation_matrix(q4<float>(x[6].hi, x[7].hi, x[8].hi, x[9].hi), sM + 9 * tid);
+        }
+        {
+            float chk = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 14; c++) chk += x[c].hi;
+            if (!finite_f(chk)) flag_failure(S.status, S.body_bad, b);
         }
 #pragma unroll
         for (int c = 0; c < 14; c++) {

@@ -167,6 +167,11 @@ class IntegratorKernel:
         return self._get_int(self._lib.rbx_get_num_dof)
 
     @property
+    def num_dof_reference(self):
+        """The reference's own count (one per free atom, unique indices as one-atom bodies)."""
+        return self._get_int(self._lib.rbx_get_num_dof_reference)
+
+    @property
     def num_bodies(self):
         return self._get_int(self._lib.rbx_get_num_bodies)
 
@@ -205,6 +210,15 @@ class IntegratorKernel:
         b = buffers.struct()
         _lib.check(self._lib.rbx_integrate_part1_delta(self._h, _stream_handle(stream), ctypes.byref(b),
                                                        ctypes.c_void_p(buffers.pos_delta.data_ptr()), float(dt)))
+
+    def check_state(self, stream=None):
+        """(bad bodies, bad free atoms) flagged by the step kernels since the last state change:
+        both 0 unless a step left a non-finite state (rbx_check_state)."""
+        nb, nf = ctypes.c_int(), ctypes.c_int()
+        rc = self._lib.rbx_check_state(self._h, _stream_handle(stream), ctypes.byref(nb), ctypes.byref(nf))
+        if rc not in (0, _lib.RBX_ERR_NUMERIC):
+            _lib.check(rc)
+        return nb.value, nf.value
 
     def kinetic_energies(self, buffers, stream=None):
         out = np.zeros(2)

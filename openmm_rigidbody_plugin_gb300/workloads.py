@@ -307,11 +307,15 @@ def gaussian_forces(n_atoms, seed=5, sd=500.0):
 
 
 def near_degenerate_system(n_bodies=8192, n_waters=20000, eps_range=(1e-8, 1e-2), seed=7, temperature=300.0,
-                           arm=0.1):
+                           arm=0.1, principal_frame=False):
     """Rigid bodies with nearly degenerate inertia among waters (the precision-study case): each
     body is a planar cross of four carbon-like atoms (mass 12, LJ on all four) with arms a and
     a*sqrt(1+eps), so that two of its principal moments differ by the factor 1+eps, eps
-    log-uniform in eps_range; random orientations; all molecules on one lattice at 1 g/cm^3."""
+    log-uniform in eps_range; all molecules on one lattice at 1 g/cm^3. Orientations are random,
+    or, with principal_frame, the crosses keep their arms along the x and y axes, so that their
+    inertia tensors are diagonal in the space frame (the reference's eigen-solver is exact only
+    there for such bodies: Smith's closed-form eigenvalues lose about 1e-9 relative,
+    openmmapi/src/eigenDecomposition.cpp:72-101)."""
     rng = np.random.default_rng(seed)
     eps = np.exp(rng.uniform(np.log(eps_range[0]), np.log(eps_range[1]), size=n_bodies))
     nmol = n_bodies + n_waters
@@ -329,6 +333,12 @@ def near_degenerate_system(n_bodies=8192, n_waters=20000, eps_range=(1e-8, 1e-2)
             b = arm * np.sqrt(1.0 + eps[k])
             t = np.array([[arm, 0, 0], [-arm, 0, 0], [0, b, 0], [0, -b, 0]])
             m, sp = m_body, (TETRA_C,) * 4
+            if principal_frame:
+                pos.append(sites[k] + t)
+                mass.append(m)
+                bidx.append(np.full(len(m), k + 1, dtype=np.int32))
+                spec.append(np.array(sp, dtype=np.int8))
+                continue
         else:
             t, m, sp = wt, wm, SPECIES["water"]
         pos.append(sites[k] + t @ rot[k].T)
@@ -354,13 +364,22 @@ def cutoff_for(box):
     return min(CUTOFF, 0.49 * box)
 
 
-def batch_systems(n_systems=4096, lo=64, hi=4096, fractions=(0.7, 0.2, 0.1), seed=6, temperature=300.0):
-    """Independent mixed systems without free atoms, body counts log-uniform in [lo, hi], each in
-    its own cubic box at 1 g/cm^3 and seeded from `seed` and its index."""
+def batch_body_counts(n_systems=4096, lo=64, hi=4096, seed=6):
+    """Body counts of the batched-replicas workload: log-uniform in [lo, hi], seeded."""
     rng = np.random.default_rng(seed)
-    counts = np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_systems)).astype(np.int64)
-    out = []
-    for k, nb in enumerate(counts):
-        out.append(mixed_system(n_bodies=int(nb), n_free=0, fractions=fractions, seed=seed * 100003 + k,
-                                temperature=temperature))
-    return out
+    return np.exp(rng.uniform(np.log(lo), np.log(hi), size=n_systems)).astype(np.int64)
+
+
+def batch_system(k, n_bodies, fractions=(0.7, 0.2, 0.1), seed=6, temperature=300.0):
+    """System k of the batched-replicas workload (seeded from `seed` and k), without free atoms."""
+    return mixed_system(n_bodies=int(n_bodies), n_free=0, fractions=fractions, seed=seed * 100003 + k,
+                        temperature=temperature)
+
+
+def batch_systems(n_systems=4096, lo=64, hi=4096, fractions=(0.7, 0.2, 0.1), seed=6, temperature=300.0, only=None):
+    """Independent mixed systems without free atoms, body counts log-uniform in [lo, hi], each in
+    its own cubic box at 1 g/cm^3 and seeded from `seed` and its index; `only` (indices) builds a
+    subset of them."""
+    counts = batch_body_counts(n_systems, lo, hi, seed)
+    idx = range(n_systems) if only is None else only
+    return [batch_system(int(k), counts[k], fractions, seed, temperature) for k in idx]

@@ -769,7 +769,11 @@ static void build_geometry(orc_system* s, int b, const double* R, const double* 
         d2[j] = dot3(delta + 3 * j, delta + 3 * j);
     }
     double u[3], A[9], *I = s->I + 3 * b, *invI = s->invI + 3 * b;
-    if (N > 1 && collinear(delta, d2, N, u, s->robust)) {
+    /* The reference tests a one-atom body for collinearity too (its cleanBodyIndices keeps an index
+     * used once as a body, RigidBodySystem.cpp:37-47): the atom's displacement from its own centre
+     * of mass, R - (R*m)*(1/m), is zero or a rounding residue, and in the second case the test
+     * passes and the body counts 5 degrees of freedom, otherwise 6 (RigidBody.cpp:88-107). */
+    if ((N > 1 || !s->robust) && collinear(delta, d2, N, u, s->robust)) {
         double moi = 0.0;
         for (int j = 0; j < N; j++) moi += s->masses[atom[j]] * d2[j];
         I[0] = moi; I[1] = moi; I[2] = 0.0;

@@ -120,7 +120,48 @@ def linear_bodies(mode=10, nsteps=20, dt=0.002):
                 ke=ref.kinetic(), dof=ref.num_dof)
 
 
+def near_degenerate(mode, dt, nsteps=100, sd=50.0):
+    """48 planar 4-atom crosses whose two in-plane principal moments differ by a factor 1+eps, eps
+    log-uniform in [1e-4, 1e-2], built in their principal frame (inertia tensors diagonal in the
+    space frame, where the reference's eigen-solver is exact), 300 K velocities, fixed seeded
+    Gaussian forces of standard deviation sd (kJ/mol/nm); final positions, velocities and kinetic
+    energies after nsteps steps of dt."""
+    s = W.near_degenerate_system(48, 0, eps_range=(1e-4, 1e-2), seed=17, principal_frame=True)
+    F = quantise(W.gaussian_forces(s.num_atoms, seed=9, sd=sd))
+    r = Reference(s.masses, s.body_indices, mode)
+    r.setup(s.positions, s.velocities, F)
+    for n in range(nsteps):
+        r.part1(dt, F)
+        r.part2(dt, F)
+    return dict(masses=s.masses, body_indices=s.body_indices, R0=s.positions, V0=s.velocities, F=F, dt=dt,
+                mode=mode, nsteps=nsteps, eps=s.eps, R=r.R, V=r.V, ke=r.kinetic(), dof=r.num_dof)
+
+
+def singleton_dof(ncases=12):
+    """Degrees of freedom the reference reports for systems that hold one-atom bodies (indices used
+    once, which it keeps as bodies), linear bodies, free and massless atoms: ncases seeded systems,
+    stored as concatenated arrays with atom offsets."""
+    rng = np.random.default_rng(41)
+    M, B, R, V, off, dof = [], [], [], [], [0], []
+    for c in range(ncases):
+        s = W.mixed_system(n_bodies=6, n_free=3, fractions=(0.5, 0.3, 0.2), seed=100 + c)
+        ns = 1 + c % 4
+        m = np.concatenate([s.masses, rng.uniform(1, 20, ns), [16.0, 12.0, 16.0], [0.0]])
+        b = np.concatenate([s.body_indices, 1000 + np.arange(ns), [900, 900, 900], [0]]).astype(np.int32)
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        x = np.concatenate([s.positions, rng.uniform(-3, 3, (ns, 3)), 1.0 + np.outer([-0.116, 0, 0.116], u),
+                            rng.uniform(0, 2, (1, 3))])
+        v = rng.normal(size=x.shape)
+        r = Reference(m, b, 0)
+        r.setup(x, v, np.zeros_like(x))
+        M.append(m); B.append(b); R.append(x); V.append(v); off.append(off[-1] + len(m)); dof.append(r.num_dof)
+    return dict(masses=np.concatenate(M), body_indices=np.concatenate(B), R0=np.concatenate(R), V0=np.concatenate(V),
+                offsets=np.array(off), dof=np.array(dof))
+
+
 def main():
+    only = sys.argv[1:]  # optional case names; all cases by default
     if not reference_available():
         sys.exit("oracle/_ref/librefrb.so missing: build it with `make -C oracle ref`")
     cases = {f"water64_mode{m}": water_fixed_force(m) for m in (0, 1, 10)}
@@ -130,7 +171,13 @@ def main():
     cases["water27_tether_mode4"] = water_tether(4)
     cases["single_bond"] = single_bond()
     cases["linear10_mode10"] = linear_bodies(10)
+    cases["singleton_dof"] = singleton_dof()
+    for m in (0, 1, 4, 16):
+        for dt_fs in (1, 4):
+            cases[f"cross48_mode{m}_dt{dt_fs}fs"] = near_degenerate(m, dt_fs * 1e-3)
     for name, data in cases.items():
+        if only and name not in only:
+            continue
         path = os.path.join(HERE, name + ".npz")
         np.savez_compressed(path, **data)
         print(f"{path}: {os.path.getsize(path)} bytes")

@@ -96,11 +96,14 @@ def test_intra_body_constraints_and_interactions_are_removed():
 
 
 class _FakeIntegrator:
+    """Stands in for the bound integrator: the library's count is `dof`, the reference's count
+    (one per free atom instead of three) 20 less."""
+
     def __init__(self, dof):
         self._dof = dof
 
     def getRigidBodySystem(self):
-        return type("S", (), {"getNumDOF": lambda s: self._dof})()
+        return type("S", (), {"getNumDOF": lambda s, reference=False: self._dof - (20 if reference else 0)})()
 
     def getKineticEnergies(self):
         return [30.0, 12.0]
@@ -135,6 +138,16 @@ def test_state_data_reporter_columns_and_temperature(cmm):
     v = [float(x) for x in line.split(",")]
     dof = 60 - (3 if cmm else 0)
     np.testing.assert_allclose(v, [10, -5.0, 42.0, 37.0, 2 * 42.0 / (dof * api.KB), 30.0, 12.0])
+
+
+def test_state_data_reporter_temperature_with_the_reference_count():
+    """referenceDOF=True divides by the reference's own count (RigidBodySystem.cpp:130), as the
+    plugin's reporter does (python/statedatareporter.py:19-28)."""
+    out = io.StringIO()
+    rep = api.StateDataReporter(out, 10, step=False, potentialEnergy=False, kineticEnergy=False, totalEnergy=False,
+                                referenceDOF=True)
+    rep.report(_FakeContext(60, True), 10)
+    np.testing.assert_allclose(float(out.getvalue().splitlines()[1]), 2 * 42.0 / ((60 - 20 - 3) * api.KB))
 
 
 def test_state_data_reporter_refined_columns():

@@ -8,8 +8,10 @@ import sys
 
 from conftest import ROOT
 
-ARGS = ["--impl", "reference", "--bodies", "2000", "--free", "200", "--steps", "3", "--warmup", "3",
-        "--reference-seconds", "2"]
+ARGS = ["--impl", "reference", "--workload", "single", "--bodies", "2000", "--free", "200", "--steps", "3",
+        "--warmup", "3", "--reference-seconds", "2"]
+ARGS_BATCHED = ["--impl", "reference", "--systems", "6", "--min-bodies", "40", "--max-bodies", "80", "--steps", "3",
+                "--warmup", "3", "--reference-seconds", "2"]
 
 
 def _lines(out):
@@ -48,3 +50,20 @@ def test_reference_arm_under_two_ranks_prints_once():
     assert len(lines) == 1
     _check(lines[0])
     assert lines[0]["n_gpus"] == 2
+
+
+def test_batched_reference_arm_uses_the_gpu_arms_config():
+    """The default workload (batched replicas): the reference arm's `config` is the dict the GPU arm
+    prints (bench.batched_config), so the two lines describe the same workload."""
+    import argparse
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *ARGS_BATCHED], capture_output=True,
+                       text=True, timeout=300, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = _lines(r.stdout)
+    assert len(lines) == 1
+    d = lines[0]
+    assert d["impl"] == "reference" and d["value"] > 0 and d["cpu_baseline"]["value"] == d["value"]
+    sys.path.insert(0, ROOT)
+    import bench
+    args = argparse.Namespace(systems=6, min_bodies=40, max_bodies=80, steps=3)
+    assert d["config"] == bench.batched_config(args, 1)

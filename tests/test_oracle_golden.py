@@ -123,3 +123,48 @@ def test_free_atoms_count_three_degrees_of_freedom_in_the_robust_oracle(oracle_m
     rob.setup(g["R0"], g["V0"], g["F"])
     assert ref.num_dof == int(g["dof"])
     assert rob.num_dof == int(g["dof"]) + 2 * nfree
+
+
+CROSS_CASES = [(m, dt) for m in (0, 1, 4, 16) for dt in (1, 4)]
+
+
+@pytest.mark.parametrize("mode,dt_fs", CROSS_CASES)
+def test_oracle_matches_reference_near_degenerate_tops(oracle_mod, golden, mode, dt_fs):
+    """Near-degenerate tops (two principal moments 1+eps apart, eps in [1e-4, 1e-2], built in their
+    principal frame): the reference-mode oracle follows the reference step for step, and the robust
+    oracle, whose Jacobi eigen-solver and canonical frame differ from the reference's, agrees to
+    1e-9 (positions) and 1e-8 (velocities) after 100 steps under sd 50 kJ/mol/nm forces; in mode 0
+    the reference's closed-form rotation differences third-kind elliptic integrals, which cancel
+    at small rotations (about 1e-11 per step), so the robust comparison allows 1e-8 there."""
+    g = golden(f"cross48_mode{mode}_dt{dt_fs}fs")
+    dt = float(g["dt"])
+    for robust in (False, True):
+        o = oracle_mod.Oracle(g["masses"], g["body_indices"], mode=mode, robust=robust)
+        o.setup(g["R0"], g["V0"], g["F"])
+        assert o.num_dof == int(g["dof"]) == 6 * 48
+        for n in range(int(g["nsteps"])):
+            o.part1(dt, g["F"])
+            o.part2(dt, g["F"])
+        if robust:
+            tol = 1e-8 if mode == 0 else 1e-12
+            assert rel_err(o.R, g["R"]) < tol
+            assert rel_err(o.V, g["V"]) < 10 * tol
+            np.testing.assert_allclose(o.kinetic(), g["ke"], rtol=10 * tol)
+        else:
+            assert rel_err(o.R, g["R"]) < 1e-13
+            assert rel_err(o.V, g["V"]) < 1e-12
+            np.testing.assert_allclose(o.kinetic(), g["ke"], rtol=1e-12)
+
+
+def test_reference_mode_counts_degrees_of_freedom_as_the_reference(oracle_mod, golden):
+    """One-atom bodies (body indices used once: the reference keeps them as bodies and counts 5 or 6
+    depending on the rounding of its centre-of-mass arithmetic), linear bodies, free and massless
+    atoms: the reference-mode oracle reports the reference's own integer in every case."""
+    g = golden("singleton_dof")
+    off = g["offsets"]
+    for c in range(len(off) - 1):
+        a, b = off[c], off[c + 1]
+        o = oracle_mod.Oracle(g["masses"][a:b], g["body_indices"][a:b], mode=0, robust=False)
+        o.setup(g["R0"][a:b], g["V0"][a:b], np.zeros((b - a, 3)))
+        assert o.num_dof == int(g["dof"][c])
+    assert len(set(int(d) % 2 for d in g["dof"])) == 2  # both 5- and 6-DOF one-atom bodies occur
