@@ -101,9 +101,13 @@ def parse():
     p.add_argument("--pwaters", type=int, default=20000, help="precision: waters")
     p.add_argument("--psteps", type=int, default=1000, help="precision: steps per run")
     p.add_argument("--rate", type=float, default=200.0, help="served: request arrivals per second")
-    p.add_argument("--duration", type=float, default=2.0, help="served: seconds of arrivals")
-    p.add_argument("--max-atoms", type=int, default=20000, help="served: largest request (atoms)")
-    p.add_argument("--max-steps", type=int, default=5000, help="served: longest request (steps)")
+    p.add_argument("--duration", type=float, default=60.0, help="served: seconds of arrivals")
+    p.add_argument("--max-atoms", type=int, default=200000, help="served: largest request (atoms)")
+    p.add_argument("--min-steps", type=int, default=100, help="served: shortest request (steps)")
+    p.add_argument("--max-steps", type=int, default=2000, help="served: longest request (steps)")
+    p.add_argument("--plain-requests", type=int, default=24, help="served: requests also run one at a time")
+    p.add_argument("--admit-interval", type=float, default=0.25,
+                   help="served: seconds between group creations while others run")
     p.add_argument("--plain-steps", type=int, default=0,
                    help="batched: steps of the one-per-launch arm (0: the same as --steps)")
     return p.parse_args()
@@ -653,6 +657,7 @@ def run_batched(args, world, rank, local):
     torch.cuda.synchronize()
     barrier(world)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    builds0 = b.list_builds()
     with ClockSampler(local) as clocks:
         time.sleep(0.3)
         torch.cuda.synchronize()
@@ -662,6 +667,7 @@ def run_batched(args, world, rank, local):
         end.record(stream)
         torch.cuda.synchronize()
         launches = b.last_launch_count
+        builds = (b.list_builds() - builds0).astype(np.int64)
         e_post = b.energies()
         # the clocks are sampled over the timed steps and over repeats of them until the window
         # lasts at least 1.5 s, so that a short timed region still has its own clock record
@@ -765,6 +771,10 @@ def run_batched(args, world, rank, local):
            "setup": {"systems_on_rank0": len(systems), "bodies_on_rank0": nb, "atoms_on_rank0": na,
                      "relax_steps": args.relax_steps, "seconds": setup_s, "autotune": tuning},
            "energy_drift": drift, "plain": plain,
+           "neighbour_lists": {"builds_per_system_in_timed_steps_mean": float(builds.mean()),
+                               "force_evaluations": args.steps + 1,
+                               "atoms_rebuilt_per_evaluation": float(np.sum(builds * np.array(
+                                   [s.num_atoms for s in systems])) / (args.steps + 1) / na)},
            "speedup_vs_plain": (value / world / plain["value"]) if plain else None,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "peak_source": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": bytes_step,
@@ -783,21 +793,23 @@ def run_batched(args, world, rank, local):
 def run_served(args, world, rank, local):
     """Continuous batching of a seeded Poisson stream of simulation requests (serving.Server), with
     p50/p99 completion latency and aggregate body-steps/s, against a one-request-at-a-time server on
-    a subset of the same stream."""
+    the first requests of the same stream (their latency served and alone, and whether each result
+    is the same bit for bit)."""
     import torch
     from openmm_rigidbody_plugin_gb300 import batch, build, serving
     torch.cuda.set_device(local)
     build.build_library()
-    stream = serving.poisson_stream(args.rate, args.duration, (100, args.max_atoms), (100, args.max_steps),
-                                    seed=8 + 1000 * rank)
+    stream = serving.poisson_stream(args.rate, args.duration, (100, args.max_atoms), (args.min_steps, args.max_steps),
+                                    seed=8 + 1000 * rank, lazy=True)
     nreq = len(stream)
     # warm the library (module load, kernel attributes) outside the served clock
-    warm = batch.BatchedSystems.from_systems([stream[0].system])
+    warm = batch.BatchedSystems.from_systems([stream[0].get_system()])
     warm.set_graph_steps(25)
     warm.step(60, 0.002)
     del warm
     torch.cuda.synchronize()
-    server = serving.Server(budget_bytes=150e9, chunk_steps=100, graph_steps=25, device=local)
+    server = serving.Server(budget_bytes=150e9, chunk_steps=100, graph_steps=25, device=local, keep_states=False,
+                            min_interval=args.admit_interval)
     barrier(world)
     with ClockSampler(local) as clocks:
         clocks.mark_start()
@@ -806,55 +818,74 @@ def run_served(args, world, rank, local):
         wall = time.perf_counter() - t0
         clocks.mark_end()
     wall = max_over_ranks(wall, world)
-    lat = np.array([r.latency for r in done])
-    body_steps = sum(int(r.system.num_bodies) * r.steps for r in done)
+    ok = [r for r in done if r.failed is None]
+    lat = np.array([r.latency for r in ok])
+    body_steps = sum(r.bodies * r.steps for r in ok)
     value = world * body_steps / wall
     # one request at a time (the plain way), on the first requests of the stream: each request's
     # service time alone, then the FIFO queue replayed on the same arrival times
-    sub = sorted(done, key=lambda r: r.rid)[:min(24, nreq)]
-    service = []
+    sub = sorted(ok, key=lambda r: r.rid)[:min(args.plain_requests, len(ok))]
+    service, same = [], 0
     for r in sub:
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        serving.serve_alone(r)
+        alone = serving.serve_alone(r)
         torch.cuda.synchronize()
         service.append(time.perf_counter() - t1)
+        same += int(np.array_equal(alone["energies"], r.result["energies"]))
+        r.system = None
     fin, lat_plain = 0.0, []
     for r, t_s in zip(sub, service):
         fin = max(fin, r.arrival) + t_s
         lat_plain.append(fin - r.arrival)
     lat_plain = np.array(lat_plain)
-    plain_value = sum(int(r.system.num_bodies) * r.steps for r in sub) / sum(service)
+    plain_value = sum(r.bodies * r.steps for r in sub) / sum(service)
     lat_sub = np.array([r.latency for r in sub])
+    # the whole stream served one request at a time: service times from a least-squares fit of the
+    # measured ones (seconds = a + b x body-steps), queued first come first served
+    work = np.array([r.bodies * r.steps for r in sub], dtype=np.float64)
+    coef = np.linalg.lstsq(np.stack([np.ones_like(work), work], axis=1), np.array(service), rcond=None)[0]
+    fin, lat_fifo = 0.0, []
+    for r in sorted(ok, key=lambda r: (r.arrival, r.rid)):
+        fin = max(fin, r.arrival) + max(coef[0] + coef[1] * r.bodies * r.steps, 0.0)
+        lat_fifo.append(fin - r.arrival)
+    lat_fifo = np.array(lat_fifo)
     if rank != 0:
         return
-    bytes_in = sum(r.system.num_atoms * 48 for r in done)    # positions + velocities in
-    bytes_out = sum(r.system.num_atoms * 48 + 24 for r in done)  # positions, velocities, energies out
+    bytes_in = sum(r.num_atoms * 48 for r in done)    # positions + velocities in
+    bytes_out = sum(24 for r in done)                 # energies out
     total_steps = sum(r.steps for r in done)
+    pct = lambda a, q: float(np.percentile(a, q)) if len(a) else None
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": total_steps,
            "warmup": 60, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "f32 atoms + f64 body state", "data": "synthetic",
            "config": {"workload": f"served: Poisson arrivals at {args.rate:g} req/s for {args.duration:g} s "
                                   f"({nreq} requests), rigid-water systems of 100 to {args.max_atoms} atoms "
-                                  f"(log-uniform), 100 to {args.max_steps} steps (log-uniform), dt 2 fs, cutoff "
-                                  "LJ + reaction field, mixed precision; 150 GB budget; chunks of 100 steps, "
-                                  "25-step CUDA graphs (the 10-minute, 200,000-atom, 50,000-step stream scaled "
-                                  "down to finish in seconds)",
-                      "requests": nreq, "rebuilds": server.rebuilds, "wall_seconds": wall,
-                      "server_seconds": server.seconds,
-                      "parallelism": f"{world} independent replicas"},
-           "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                         "max": float(lat.max())},
+                                  f"(log-uniform), {args.min_steps} to {args.max_steps} steps (log-uniform), dt 2 fs, "
+                                  "cutoff LJ + reaction field, mixed precision; 150 GB budget (capped by the free "
+                                  "device memory); chunks of 100 steps, 25-step CUDA graphs, one group (batch) per "
+                                  "admission, groups on their own streams",
+                      "requests": nreq, "parallelism": f"{world} independent replicas"},
+           "serving": {"wall_seconds": wall, "completed": len(ok), "failed": len(done) - len(ok),
+                       "groups_created": server.groups_created, "compactions": server.compactions,
+                       "budget_bytes": server.budget_used, "peak_bytes": server.peak_bytes,
+                       "bytes_per_atom_measured": server.bytes_per_atom, "server_seconds": server.seconds},
+           "latency_s": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": float(lat.max()) if len(lat) else None},
            "plain": {"value": plain_value, "unit": UNIT, "requests": len(sub),
-                     "latency_s": {"p50": float(np.percentile(lat_plain, 50)), "p99": float(np.percentile(lat_plain, 99))},
-                     "served_latency_same_requests_s": {"p50": float(np.percentile(lat_sub, 50)),
-                                                        "p99": float(np.percentile(lat_sub, 99))},
-                     "how": "each request alone (its own handle, same chunks), queued first come first served"},
+                     "latency_s": {"p50": pct(lat_plain, 50), "p99": pct(lat_plain, 99)},
+                     "served_latency_same_requests_s": {"p50": pct(lat_sub, 50), "p99": pct(lat_sub, 99)},
+                     "same_energies_alone_and_served": f"{same} of {len(sub)}",
+                     "whole_stream_one_at_a_time_latency_s": {"p50": pct(lat_fifo, 50), "p99": pct(lat_fifo, 99),
+                                                              "model_seconds": [float(coef[0]), float(coef[1])],
+                                                              "how": "service time a + b x body-steps fitted to the "
+                                                                     "measured requests, first come first served"},
+                     "how": "each request alone (its own handle, same chunk lengths), queued first come first "
+                            "served on the same arrival times"},
            "speedup_vs_plain": value / world / plain_value,
            "roofline": None, "cpu_baseline": None,
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(bytes_in / max(total_steps, 1)),
                    "d2h_bytes_per_step": int(bytes_out / max(total_steps, 1)),
-                   "call": "serving.Server.run (host structures in, host results out; wall clock)"},
+                   "call": "serving.Server.run (host structures in, energies out; wall clock)"},
            "clocks": clocks.summary(), "gpu_launches": server.launches}
     print(json.dumps(out), flush=True)
 

@@ -322,7 +322,12 @@ int rbx_last_launch_count(const rbx_integrator* h);
  * rbx_batch_set_graph_steps(k > 0), runs of k (forces, fused) pairs replay one captured CUDA graph
  * (captured on first use for a given dt; invalidated by rbx_batch_set_state).
  * rbx_batch_energies returns [U, KE_t, KE_r] per system (kJ/mol) at the current state
- * (synchronous). rbx_batch_get_num_dof gives each system's degrees of freedom.
+ * (synchronous); U comes from the last force evaluation of the preceding rbx_batch_step when no
+ * other call has changed the state since. rbx_batch_get_num_dof gives each system's degrees of
+ * freedom.
+ * Forces come from neighbour lists (cutoff + a skin of up to 0.15 nm) that each system rebuilds when
+ * one of its atoms has moved half the skin, and that every call rebuilds at its first evaluation:
+ * a system's results are a function of its own state and of the lengths of the calls that step it.
  */
 typedef struct rbx_batch rbx_batch;
 /* rbx_batch_set_state builds every body from the given positions and velocities (as
@@ -364,6 +369,14 @@ int rbx_batch_get_num_dof(rbx_batch* b, int* dof /* [S] */);
  * changes nothing for the others, which keep stepping exactly as they would alone. The status is
  * cleared by rbx_batch_set_state and rbx_batch_restore. */
 int rbx_batch_status(rbx_batch* b, void* stream, int* system_status, int* num_failed);
+/* Device memory the batch holds: every allocation of the batch and of its integrator, in bytes as
+ * requested from cudaMalloc (no counterpart in the reference). A serving loop admits work against
+ * this figure and the device's free memory. Grows when a later call allocates lazily (the first
+ * rbx_batch_set_state, CUDA-graph capture aside, which the driver allocates). */
+int rbx_batch_memory(const rbx_batch* b, size_t* bytes);
+/* Neighbour-list builds of each system since the batch was created (counts [S]; synchronises
+ * `stream`): a statistic of the force path (no counterpart in the reference). */
+int rbx_batch_list_builds(rbx_batch* b, void* stream, unsigned int* counts);
 int rbx_batch_set_graph_steps(rbx_batch* b, int k);
 /* Autotuner of the batched step's schedule (no counterpart in the reference, which has no batched
  * form). It times, on the batch itself, the block size of the cell force kernel (64, 128 or 256

@@ -87,6 +87,8 @@ SIGNATURES = [
     ("rbx_batch_forces", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_batch_get_num_dof", ctypes.c_int, [_vp, _ip]),
     ("rbx_batch_status", ctypes.c_int, [_vp, _vp, _ip, _ip]),
+    ("rbx_batch_memory", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_size_t)]),
+    ("rbx_batch_list_builds", ctypes.c_int, [_vp, _vp, ctypes.POINTER(ctypes.c_uint)]),
     ("rbx_batch_set_graph_steps", ctypes.c_int, [_vp, ctypes.c_int]),
     ("rbx_batch_set_timing", ctypes.c_int, [_vp, ctypes.c_int]),
     ("rbx_batch_kernel_times", ctypes.c_int, [_vp, _dp, _dp, _ip]),

@@ -163,6 +163,20 @@ class BatchedSystems:
             _lib.check(rc)
         return out
 
+    def list_builds(self, stream=None):
+        """Neighbour-list builds of each system so far (rbx_batch_list_builds)."""
+        out = np.zeros(self.num_systems, dtype=np.uint32)
+        _lib.check(self._lib.rbx_batch_list_builds(self._h, _stream(stream),
+                                                   out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint))))
+        return out
+
+    @property
+    def memory_bytes(self):
+        """Device bytes the batch and its integrator hold (rbx_batch_memory)."""
+        n = ctypes.c_size_t()
+        _lib.check(self._lib.rbx_batch_memory(self._h, ctypes.byref(n)))
+        return int(n.value)
+
     def set_graph_steps(self, k):
         _lib.check(self._lib.rbx_batch_set_graph_steps(self._h, int(k)))
 

@@ -8,8 +8,10 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <new>
 #include <vector>
 
@@ -22,7 +24,8 @@ using namespace rbx;
 namespace {
 
 constexpr double kOne4PiEps0 = 138.935456;  // kJ nm / (mol e^2)
-constexpr double kSkin = 0.1;               // nm: neighbour-list skin
+constexpr double kSkin = 0.15;              // nm: neighbour-list skin
+constexpr int kMaxTypes = 256;              // atom types of the typed force pass (FFDev::types)
 
 #define BATCH_TRY(call)                                                                             \
     do {                                                                                            \
@@ -52,9 +55,10 @@ struct rbx_batch {
     DevArray<FFSys> d_sys;
     DevArray<int> d_iatom, d_isys, d_cell_of, d_cell_count, d_cell_start, d_cell_cursor, d_cell_list;
     DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_i0;
-    DevArray<float4> d_param, d_cpos, d_cpar, d_xref;
+    DevArray<float4> d_param, d_cpos, d_cpar, d_xref, d_types;
     DevArray<unsigned char> d_rebuild, d_nbr;  // neighbour lists (FFDev::rebuild, nbr)
-    DevArray<int> d_ncnt;
+    DevArray<int> d_ncnt, d_atype;
+    DevArray<unsigned int> d_rebuilds;  // list builds per system (FFDev::rebuilds)
     DevArray<double> d_e_atom, d_energy;
     FFDev ff{};
     // per-system reductions
@@ -65,6 +69,7 @@ struct rbx_batch {
     std::vector<int> dof;
     double* h_out = nullptr;  // pinned [3*S]
     int last_launches = 0;
+    bool u_valid = false;  // d_energy holds the potential energy of the current positions
     // captured runs of (forces, fused step)
     // optional event timing of the force and integrator launch groups (direct launches only)
     bool timing = false;
@@ -317,6 +322,26 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     if (!rc) rc = upload_vec(b->d_iatom, iatom);
     if (!rc) rc = upload_vec(b->d_isys, isys);
     if (!rc) rc = upload_vec(b->d_param, param);
+    // atom types: the distinct (scaled charge, sigma/2, sqrt(epsilon)) triples; with at most
+    // kMaxTypes of them the force pass reads one 16-byte record per neighbour (position and type)
+    std::vector<float4> types;
+    std::vector<int> type_of(param.size(), -1);
+    {
+        std::map<std::array<float, 3>, int> seen;
+        for (size_t k = 0; k < param.size() && (int)types.size() <= kMaxTypes; k++) {
+            const std::array<float, 3> key{param[k].x, param[k].y, param[k].z};
+            auto it = seen.find(key);
+            if (it == seen.end()) {
+                it = seen.emplace(key, (int)types.size()).first;
+                types.push_back(make_float4(key[0], key[1], key[2], 0.0f));
+            }
+            type_of[k] = it->second;
+        }
+        if ((int)types.size() > kMaxTypes) types.clear();
+    }
+    if (types.empty()) type_of.clear();
+    if (!rc) rc = upload_vec(b->d_types, types);
+    if (!rc) rc = upload_vec(b->d_atype, type_of);
     if (!rc && (b->d_cell_of.alloc(std::max(nint, 1)) != cudaSuccess || b->d_cell_list.alloc(std::max(nint, 1)) != cudaSuccess ||
                 b->d_cell_count.alloc(cells) != cudaSuccess || b->d_cell_start.alloc(cells + 1) != cudaSuccess ||
                 b->d_cell_cursor.alloc(cells) != cudaSuccess || b->d_cpos.alloc(std::max(nint, 1)) != cudaSuccess ||
@@ -334,6 +359,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     const int nbr16 = max_sys_atoms <= 65536 ? 1 : 0;
     const size_t groups = ((size_t)std::max(nint, 1) + 31) / 32;
     if (!rc && (b->d_rebuild.alloc(num_systems) != cudaSuccess || b->d_xref.alloc(std::max(nint, 1)) != cudaSuccess ||
+                b->d_rebuilds.alloc(num_systems) != cudaSuccess ||
                 b->d_ncnt.alloc(std::max(nint, 1)) != cudaSuccess ||
                 b->d_nbr.alloc(groups * 32 * (size_t)cap * (nbr16 ? 2 : 4)) != cudaSuccess))
         rc = set_error(RBX_ERR_CUDA, "cudaMalloc of the neighbour lists failed (%d entries per atom)", cap);
@@ -342,6 +368,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
         for (int k = 0; k < (int)iota.size(); k++) iota[k] = k;  // a valid list order before the first build
         if (cudaMemcpy(b->d_cell_list.p, iota.data(), iota.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemset(b->d_rebuild.p, 1, (size_t)num_systems) != cudaSuccess ||
+            cudaMemset(b->d_rebuilds.p, 0, sizeof(unsigned int) * (size_t)num_systems) != cudaSuccess ||
             cudaMemset(b->d_ncnt.p, 0, sizeof(int) * (size_t)std::max(nint, 1)) != cudaSuccess ||
             cudaMemset(b->d_cpos.p, 0, sizeof(float4) * (size_t)std::max(nint, 1)) != cudaSuccess)
             rc = set_error(RBX_ERR_CUDA, "initialisation of the neighbour lists failed");
@@ -369,11 +396,15 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     D.fcap = 0.0f;
     D.sys_status = b->d_sys_status.p;
     D.rebuild = b->d_rebuild.p;
+    D.rebuilds = b->d_rebuilds.p;
     D.xref = b->d_xref.p;
     D.nbr = b->d_nbr.p;
     D.ncnt = b->d_ncnt.p;
     D.cap = cap;
     D.nbr16 = nbr16;
+    D.types = b->d_types.p;
+    D.atype = b->d_atype.p;
+    D.ntypes = (int)types.size();
     D.cell_threads = 128;
     D.n_mc = (int)mc_cell.size();
     D.n_sc = (int)sc_sys.size();
@@ -412,6 +443,7 @@ int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, con
     b->body0_h = body0;
     b->free0_h = free0;
     BATCH_TRY(cudaMemsetAsync(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)b->S, (cudaStream_t)stream));
+    b->u_valid = false;
     return RBX_OK;
 }
 
@@ -444,6 +476,7 @@ int rbx_batch_restore(rbx_batch* b, void* stream, const double* body_state, cons
     if ((rc = rbx_set_body_state(b->integ, body_state))) return rc;
     if ((rc = rbx_context_sync_bodies(b->integ, stream))) return rc;
     BATCH_TRY(cudaMemsetAsync(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)b->S, (cudaStream_t)stream));
+    b->u_valid = false;
     return RBX_OK;
 }
 
@@ -471,8 +504,11 @@ int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {
     for (; remaining > 0; remaining--) {
         if ((rc = forces(b, stream, false)) || (rc = fused(b, stream, dt))) return rc;
     }
-    if ((rc = forces(b, stream, false))) return rc;
+    // the last evaluation also forms the potential energy of the state the call ends in
+    b->u_valid = false;
+    if ((rc = forces(b, stream, true))) return rc;
     if ((rc = integrate(b, stream, STEP_PART2, dt))) return rc;
+    b->u_valid = true;
     return RBX_OK;
 }
 
@@ -489,6 +525,7 @@ int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double ma
     rbx_context_buffers(b->integ, &rb);
     const DevSys sys = device_system(b->integ);
     b->ff.fcap = (float)max_force;
+    b->u_valid = false;
     if ((rc = force_rebuild(b, stream))) return rc;
     for (int n = 0; n < nsteps && !rc; n++) {
         rc = forces(b, stream, false);
@@ -510,7 +547,10 @@ int rbx_batch_energies(rbx_batch* b, void* stream, double* out) {
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
     BATCH_TRY(cudaSetDevice(b->device));
     b->last_launches = 0;
-    if ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, true))) return rc;  // plus the potential energy
+    // the potential energy of the last step call's final positions when it is still current (formed
+    // in that call's last force evaluation); otherwise a force evaluation that forms it
+    if (!b->u_valid && ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, true)))) return rc;
+    b->u_valid = true;
     if (launch_kinetic_systems(b->prec, device_system(b->integ), buffers(b), b->d_body0.p, b->d_free0.p, b->S,
                                b->d_ke.p, stream) < 0)
         return set_error(RBX_ERR_CUDA, "kinetic-energy kernel failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -551,6 +591,31 @@ int rbx_batch_get_num_dof(rbx_batch* b, int* dof) {
     if (rc) return rc;
     if (b->dof.empty()) return set_error(RBX_ERR_STATE, "degrees of freedom are known after rbx_batch_set_state");
     std::copy(b->dof.begin(), b->dof.end(), dof);
+    return RBX_OK;
+}
+
+int rbx_batch_list_builds(rbx_batch* b, void* stream, unsigned int* counts) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (!counts) return set_error(RBX_ERR_INVALID_ARGUMENT, "null output");
+    BATCH_TRY(cudaSetDevice(b->device));
+    BATCH_TRY(cudaMemcpyAsync(counts, b->d_rebuilds.p, sizeof(unsigned int) * (size_t)b->S, cudaMemcpyDeviceToHost,
+                              (cudaStream_t)stream));
+    BATCH_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+    return RBX_OK;
+}
+
+int rbx_batch_memory(const rbx_batch* b, size_t* bytes) {
+    int rc = check(b);
+    if (rc) return rc;
+    if (!bytes) return set_error(RBX_ERR_INVALID_ARGUMENT, "null output");
+    size_t n = b->d_sys.bytes() + b->d_iatom.bytes() + b->d_isys.bytes() + b->d_cell_of.bytes() +
+               b->d_cell_count.bytes() + b->d_cell_start.bytes() + b->d_cell_cursor.bytes() + b->d_cell_list.bytes() +
+               b->d_mc_cell.bytes() + b->d_mc_sys.bytes() + b->d_sc_sys.bytes() + b->d_sc_i0.bytes() +
+               b->d_param.bytes() + b->d_types.bytes() + b->d_atype.bytes() + b->d_cpos.bytes() + b->d_cpar.bytes() + b->d_xref.bytes() + b->d_rebuild.bytes() + b->d_rebuilds.bytes() +
+               b->d_nbr.bytes() + b->d_ncnt.bytes() + b->d_e_atom.bytes() + b->d_energy.bytes() + b->d_body0.bytes() +
+               b->d_free0.bytes() + b->d_sys_status.bytes() + b->d_ke.bytes() + b->d_user.bytes();
+    *bytes = n + (b->integ ? device_bytes(b->integ) : 0);
     return RBX_OK;
 }
 

@@ -25,6 +25,8 @@ template <class T> struct DevArray {
     }
     // The allocation is rounded up to a multiple of 256 bytes, so that any element range widened
     // to 16-byte boundaries stays inside it.
+    // Device bytes held (the allocation as requested from cudaMalloc).
+    size_t bytes() const { return p ? ((n * sizeof(T) + 255) / 256) * 256 : 0; }
     cudaError_t alloc(size_t count) {
         release();
         n = count;

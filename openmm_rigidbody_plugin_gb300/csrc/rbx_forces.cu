@@ -107,6 +107,7 @@ __global__ void ff_bin(FFDev D, DevBuf B, int prec) {
 __global__ void ff_scan(FFDev D) {
     __shared__ int s[256];
     if (!D.rebuild[blockIdx.x]) return;
+    if (threadIdx.x == 0) D.rebuilds[blockIdx.x]++;
     const FFSys S = D.sys[blockIdx.x];
     const int ncell = S.nc * S.nc * S.nc;
     if (S.nc == 1) {
@@ -159,6 +160,7 @@ __global__ void ff_scatter(FFDev D) {
 // permutation); a cell larger than the stage falls back to an insertion sort by one lane. The one
 // cell of a single-cell box is already in order.
 constexpr int kSortWarps = 4, kSortStage = 512;
+constexpr int kMaxTypesDev = 256;  // largest type table of the typed force pass (the host's limit)
 __global__ void __launch_bounds__(32 * kSortWarps) ff_sort(FFDev D) {
     __shared__ int stage[kSortWarps][kSortStage];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -201,7 +203,7 @@ __global__ void ff_gather(FFDev D, DevBuf B, int prec) {
     const int slot = D.iatom[k];
     const float3 x = wrap_box(atom_position(B, prec, slot), D.sys[s]);
     const float4 q = D.param[k];  // scaled charge, sigma/2, sqrt(eps), body id bits
-    const float4 c = make_float4(x.x, x.y, x.z, q.x);
+    const float4 c = make_float4(x.x, x.y, x.z, D.ntypes ? __int_as_float(D.atype[k]) : q.x);
     D.cpos[p] = c;
     D.xref[p] = c;
     D.cpar[p] = make_float4(q.y, q.z, q.w, __int_as_float(slot));
@@ -368,14 +370,20 @@ __device__ __forceinline__ void store_force(const FFDev& D, long long* __restric
 // 8. Forces from the lists: one thread per atom (list position p), its entries in list order; a
 // pair beyond the cutoff adds exactly nothing (its term is selected to zero, so the loop does not
 // diverge). The pair term is OpenMM's CutoffPeriodic form: reaction-field Coulomb and unshifted LJ.
-template <bool ENERGY, class IDX>
+template <bool ENERGY, class IDX, bool TYPED>
 __global__ void __launch_bounds__(128) ff_force_list(FFDev D, long long* __restrict__ force, int stride) {
+    __shared__ float4 stype[TYPED ? kMaxTypesDev : 1];
+    if (TYPED) {
+        for (int t = threadIdx.x; t < D.ntypes; t += blockDim.x) stype[t] = D.types[t];
+        __syncthreads();
+    }
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= D.n_int) return;
     const int s = D.isys[p];
     const FFSys S = D.sys[s];
     const float4 xi = D.cpos[p];
     const float4 pi = D.cpar[p];
+    const float qi = TYPED ? stype[__float_as_int(xi.w)].x : xi.w;
     const int n = D.ncnt[p];
     const IDX* __restrict__ nb = (const IDX*)D.nbr + (size_t)(p >> 5) * 32 * D.cap + (p & 31);
     const float4* __restrict__ cpos = D.cpos + S.i0;
@@ -383,18 +391,27 @@ __global__ void __launch_bounds__(128) ff_force_list(FFDev D, long long* __restr
     const bool relax = D.fcap > 0.0f;
     float fx = 0.f, fy = 0.f, fz = 0.f;
     ESum en;
-    for (int e = 0; e < n; e++) {
-        const int j = (int)nb[(size_t)e * 32];
-        const float4 xq = cpos[j];
-        const float2 pq = *(const float2*)(cpar + j);
+    // one neighbour's term; `valid` false adds exactly nothing (padding of the last group of loads)
+    auto pair = [&](float4 xq, float2 pq, bool valid) {
+        float qj, sj, ej;
+        if (TYPED) {  // one 16-byte record per neighbour; parameters from the type table
+            const float4 tq = stype[__float_as_int(xq.w)];
+            qj = tq.x;
+            sj = tq.y;
+            ej = tq.z;
+        } else {
+            qj = xq.w;
+            sj = pq.x;
+            ej = pq.y;
+        }
         const float3 d = min_image(xi.x - xq.x, xi.y - xq.y, xi.z - xq.z, S);
         const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
         // relaxation: coincident atoms have no direction
-        const bool in = r2 < S.rc2 && !(relax && r2 < 1e-8f);
+        const bool in = valid && r2 < S.rc2 && !(relax && r2 < 1e-8f);
         const float r2s = in ? r2 : 1.0f;
         const float inv_r = rsqrtf(r2s), inv_r2 = inv_r * inv_r;
-        const float qq = xi.w * xq.w;
-        const float sig = pi.x + pq.x, eps = pi.y * pq.y;
+        const float qq = qi * qj;
+        const float sig = pi.x + sj, eps = pi.y * ej;
         const float s2 = sig * sig * inv_r2, s6 = s2 * s2 * s2;
         float g = qq * (inv_r * inv_r2 - 2.0f * S.krf) + 4.0f * eps * (12.0f * s6 * s6 - 6.0f * s6) * inv_r2;
         g = in ? g : 0.0f;
@@ -402,6 +419,25 @@ __global__ void __launch_bounds__(128) ff_force_list(FFDev D, long long* __restr
         fy = fmaf(g, d.y, fy);
         fz = fmaf(g, d.z, fz);
         if (ENERGY && in) en.add(qq * (inv_r + S.krf * r2 - S.crf) + 4.0f * eps * (s6 * s6 - s6));
+    };
+    // groups of kU entries: all of a group's index and neighbour loads are issued before its terms
+    // are formed (in entry order), so that the dependent index -> position loads overlap
+    constexpr int kU = 4;
+    for (int e0 = 0; e0 < n; e0 += kU) {
+        int jj[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) jj[u] = e0 + u < n ? (int)nb[(size_t)(e0 + u) * 32] : 0;
+        float4 xq[kU];
+        float2 pq[kU];
+#pragma unroll
+        for (int u = 0; u < kU; u++) {
+            xq[u] = cpos[jj[u]];
+            pq[u] = TYPED ? make_float2(0.f, 0.f) : *(const float2*)(cpar + jj[u]);
+        }
+        // the group's records are all loaded before the first term (the loads are in flight together)
+        asm volatile("" ::"f"(xq[0].x), "f"(xq[1].x), "f"(xq[2].x), "f"(xq[3].x));
+#pragma unroll
+        for (int u = 0; u < kU; u++) pair(xq[u], pq[u], e0 + u < n);
     }
     const int k = D.cell_list[p];
     store_force<ENERGY>(D, force, stride, k, __float_as_int(pi.w), fx, fy, fz, en, s);
@@ -477,13 +513,16 @@ int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* 
     if (cudaMemsetAsync(D.rebuild, 0, (size_t)D.S, st) != cudaSuccess) return -1;
     long long* f = const_cast<long long*>(B.force);
     const int gf = (D.n_int + 127) / 128;
+    const bool typed = D.ntypes > 0 && D.ntypes <= kMaxTypesDev;
+#define RBX_FORCE_LIST(E, I, T) ff_force_list<E, I, T><<<gf, 128, 0, st>>>(D, f, B.stride)
     if (D.nbr16) {
-        if (energy) ff_force_list<true, unsigned short><<<gf, 128, 0, st>>>(D, f, B.stride);
-        else ff_force_list<false, unsigned short><<<gf, 128, 0, st>>>(D, f, B.stride);
+        if (typed) { if (energy) RBX_FORCE_LIST(true, unsigned short, true); else RBX_FORCE_LIST(false, unsigned short, true); }
+        else { if (energy) RBX_FORCE_LIST(true, unsigned short, false); else RBX_FORCE_LIST(false, unsigned short, false); }
     } else {
-        if (energy) ff_force_list<true, unsigned int><<<gf, 128, 0, st>>>(D, f, B.stride);
-        else ff_force_list<false, unsigned int><<<gf, 128, 0, st>>>(D, f, B.stride);
+        if (typed) { if (energy) RBX_FORCE_LIST(true, unsigned int, true); else RBX_FORCE_LIST(false, unsigned int, true); }
+        else { if (energy) RBX_FORCE_LIST(true, unsigned int, false); else RBX_FORCE_LIST(false, unsigned int, false); }
     }
+#undef RBX_FORCE_LIST
     n++;
     if (energy) {
         ff_energy<<<D.S, 256, 0, st>>>(D);

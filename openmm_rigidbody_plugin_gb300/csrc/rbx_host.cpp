@@ -166,6 +166,23 @@ struct rbx_integrator {
 
 rbx::DevSys rbx::device_system(const rbx_integrator* h) { return h->sys(); }
 
+size_t rbx::device_bytes(const rbx_integrator* h) {
+    size_t n = h->d_single_loc.bytes() + h->d_single_x.bytes() + h->d_ref_first.bytes() + h->d_ref_atoms.bytes() +
+               h->d_lib_pos.bytes() + h->d_free_atoms.bytes() + h->d_free_index.bytes() + h->r_loc.bytes() +
+               h->r_marks.bytes() + h->r_scan.bytes() + h->r_aux.bytes() + h->r_status.bytes() + h->r_lib_body.bytes() +
+               h->r_free.bytes() + h->r_idx.bytes() + h->r_seen.bytes() + h->d_state.bytes() + h->d_invm.bytes() +
+               h->d_invI.bytes() + h->d_bconst.bytes() + h->d_atom0.bytes() + h->d_atom_loc.bytes() +
+               h->d_free_loc.bytes() + h->d_tiles.bytes() + h->d_bmass.bytes() + h->d_I.bytes() + h->d_dof.bytes() +
+               h->d_setup_counts.bytes() + h->d_cls.bytes() + h->d_status.bytes() + h->d_body_bad.bytes() +
+               h->d_free_bad.bytes() + h->d_fixed.bytes() + h->d_ke_partial.bytes() + h->d_ke_out.bytes() +
+               h->d_ke_count.bytes() + h->d_ref_start.bytes() + h->d_ref_out.bytes() + h->d_ref_partial.bytes() +
+               h->d_ref_res.bytes() + h->d_ref_count.bytes() + h->c_posq.bytes() + h->c_corr.bytes() +
+               h->c_velm.bytes() + h->c_force.bytes() + h->c_x.bytes() + h->c_v.bytes() + h->c_f.bytes() +
+               h->c_m.bytes() + h->c_loc.bytes();
+    for (int s = 0; s < 2; s++) n += h->p_f[s].bytes() + h->p_x[s].bytes() + h->p_v[s].bytes();
+    return n;
+}
+
 int rbx::failure_flags(rbx_integrator* h, void* stream, std::vector<uint8_t>& body_bad, std::vector<uint8_t>& free_bad,
                        unsigned int* count) {
     CUDA_TRY(cudaSetDevice(h->device));

@@ -28,6 +28,7 @@
 
 #include <vector_types.h>
 
+#include <cstddef>
 #include <cstdint>
 #include <vector>
 
@@ -107,17 +108,24 @@ struct FFDev {
     int* cell_start;      // [n_cells + 1] (entry c0 + nc^3 of each system ends it)
     int* cell_cursor;     // [n_cells]
     int* cell_list;       // [n_int] interacting-atom indices in cell order (of the last list build)
-    float4* cpos;         // [n_int] cell order: x, y, z (wrapped into the box), sqrt(K) q
+    float4* cpos;         // [n_int] cell order: x, y, z (wrapped into the box), sqrt(K) q (or the type)
     float4* cpar;         // [n_int] cell order: sigma/2, sqrt(epsilon), body id, device slot (int bits)
     double* e_atom;       // [n_int] half pair-energy sums (energy evaluations)
     // Neighbour lists (Verlet lists with a skin), rebuilt per system when one of its atoms has moved
     // more than half the skin since the last build, and at the first evaluation of every call
     unsigned char* rebuild;  // [S] 1: rebuild this system's lists before the next force pass
+    unsigned int* rebuilds;  // [S] list builds of each system so far (a statistic)
     float4* xref;            // [n_int] cell order: positions at the last build
     void* nbr;               // neighbour entries, u16 or u32 (nbr16), j - i0 of the system, in groups
                              // of 32 atoms: entry e of atom p at (p/32)*32*cap + e*32 + p%32
     int* ncnt;               // [n_int] entries per atom
     int cap, nbr16;          // entries per atom allocated; 1: 16-bit entries
+    // Atom types (ntypes > 0): the distinct (sqrt(K) q, sigma/2, sqrt(epsilon)) of the interacting
+    // atoms; cpos .w then holds the atom's type (int bits) instead of its charge, so that the force
+    // pass reads one 16-byte record per neighbour
+    const float4* types;     // [ntypes]
+    const int* atype;        // [n_int] type of each interacting atom
+    int ntypes;
     double* energy;       // [S] potential energy per system (kJ/mol)
     float fcap;           // > 0: each atom's force is scaled down to at most this magnitude
     unsigned int* sys_status;  // [S] set to 1 when a force of the system is non-finite or beyond the
@@ -231,6 +239,8 @@ int launch_gather_rows(void* dst, const void* src, int rows, size_t ld, int n, c
 
 // Internal views of an integrator for the batched driver (defined in rbx_host.cpp).
 DevSys device_system(const rbx_integrator* h);
+// Device bytes the integrator holds (every allocation it made, as requested from cudaMalloc).
+size_t device_bytes(const rbx_integrator* h);
 // The failure detector's counter (synchronises `stream`) and, when it is non-zero, the flag bytes of
 // every body (library order, [nb]) and free atom (library order, [nf]); all zero otherwise.
 int failure_flags(rbx_integrator* h, void* stream, std::vector<uint8_t>& body_bad, std::vector<uint8_t>& free_bad,

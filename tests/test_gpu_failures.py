@@ -72,12 +72,14 @@ def test_non_finite_free_atom_is_flagged(rbx):
 
 
 def _batch_of(batch, systems, overlap=None):
+    """The systems, set up twice (the second time from the positions and velocities the first set-up
+    gives back), so that a run with and a run without a planted overlap share the same history."""
     b = batch.BatchedSystems.from_systems(systems)
     x, v = b.get_state()
     if overlap is not None:  # two atoms of different molecules put on top of each other
         a, c = overlap
         x[c] = x[a] + 1e-4
-        b.set_state(x, v)
+    b.set_state(x, v)
     return b
 
 

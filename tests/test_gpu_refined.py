@@ -49,11 +49,11 @@ def gpu_run(api, prec, rot, nsteps, dt=DT, refined=True, **kw):
     return np.array(out)
 
 
-def oracle_run(oracle_mod, rot, nsteps, dt=DT, **kw):
+def oracle_run(oracle_mod, rot, nsteps, dt=DT, weights=1, **kw):
     m, bidx, x0, v0, force = tether_system(**kw)
     o = oracle_mod.Oracle(m, bidx, mode=rot, robust=True)
     o.setup(x0, v0, force(x0)[0])
-    o.set_refined(1)
+    o.set_refined(weights)
     out = []
     for _ in range(nsteps):
         o.part1(dt, force(o.R)[0])
@@ -81,6 +81,26 @@ def test_refined_energies_match_oracle(api, oracle_mod, prec, rot):
             assert abs(dt_g - dt_o) <= 1e-4 * abs(dt_o) + 1e-7 * okt, (n, dt_g, dt_o)
             assert abs(dr_g - dr_o) <= 2e-2 * abs(dr_o) + 1e-6 * okr, (n, dr_g, dr_o)
             assert abs(ur - our) <= 1e-4 * abs(our), (n, ur, our)
+
+
+@pytest.mark.parametrize("prec", ["double", "mixed"])
+@pytest.mark.parametrize("rot", [0, 4])
+def test_body_stencils_match_the_reference_weights(api, oracle_mod, prec, rot):
+    """Rigid bodies only (no free atoms, so the free-atom stencil that this library corrects, defect
+    D9, plays no part): the refined energies against the oracle run with the reference's own
+    stencil weights (mode 2, the literal restatement of rigidbodyintegrator.cu:285-292, :318-321,
+    :380-384, :433-469), to the tolerances of test_refined_energies_match_oracle."""
+    g = gpu_run(api, prec, rot, 30, n_free=0)
+    o = oracle_run(oracle_mod, rot, 30, weights=2, n_free=0)
+    for n in (0, 9, 29):
+        _, kt, kr, rt, rr, ur = g[n]
+        _, okt, okr, ort, orr, our = o[n]
+        dt_g, dt_o = rt - kt, ort - okt
+        dr_g, dr_o = rr - kr, orr - okr
+        tk, tr, tu = (1e-6, 1e-6, 1e-6) if prec == "double" else (1e-4, 2e-2, 1e-4)
+        assert abs(dt_g - dt_o) <= tk * abs(dt_o) + (0 if prec == "double" else 1e-7 * okt), (n, dt_g, dt_o)
+        assert abs(dr_g - dr_o) <= tr * abs(dr_o) + (0 if prec == "double" else 1e-6 * okr), (n, dr_g, dr_o)
+        assert abs(ur - our) <= tu * abs(our), (n, ur, our)
 
 
 @pytest.mark.parametrize("rot", [0, 4])

@@ -41,19 +41,37 @@ def test_checkpoint_restore_is_exact(mods, precision):
 
 
 def test_served_requests_equal_requests_alone(mods):
-    _, serving, W = mods
+    batch, serving, W = mods
     reqs = []
     for rid, (nw, steps) in enumerate([(20, 130), (150, 40), (60, 95), (210, 70), (40, 60), (90, 120)]):
         reqs.append(serving.Request(rid, W.water_box(nw, seed=100 + rid), steps, arrival=0.0))
     atoms = [r.num_atoms for r in reqs]
-    server = serving.Server(budget_bytes=serving.BYTES_PER_ATOM * (max(atoms) + 2 * min(atoms) + 200),
+    # a budget that holds the largest request and two small ones at the largest bytes per atom the
+    # server can measure (a batch of all the requests: its neighbour lists are sized for the largest),
+    # so requests join as others finish
+    bpa = 0.0
+    for group in [reqs] + [[r] for r in reqs]:
+        probe = batch.BatchedSystems.from_systems([r.system for r in group])
+        bpa = max(bpa, 1.05 * probe.memory_bytes / sum(r.num_atoms for r in group))
+        del probe
+    server = serving.Server(budget_bytes=bpa * (max(atoms) + 2 * min(atoms) + 200), reserve_bytes=0,
                             chunk_steps=25, graph_steps=10)
     done = server.run(reqs, realtime=False)
     assert sorted(r.rid for r in done) == list(range(len(reqs)))
-    assert server.rebuilds >= 3  # membership changed while systems were in flight
+    assert server.groups_created >= 3  # groups formed while others were in flight
+    assert server.peak_bytes <= server.budget_used
     for r in done:
-        assert sum(r.chunks) == r.steps
+        assert r.failed is None and sum(r.chunks) == r.steps
         alone = serving.serve_alone(r)
         assert np.array_equal(alone["positions"], r.result["positions"])
         assert np.array_equal(alone["velocities"], r.result["velocities"])
         assert np.array_equal(alone["energies"], r.result["energies"])
+
+
+def test_memory_report_counts_the_neighbour_lists(mods):
+    """rbx_batch_memory: the bytes a batch holds grow with its atoms (the neighbour lists dominate)."""
+    batch, _, W = mods
+    small = batch.BatchedSystems.from_systems([W.water_box(200, seed=1)])
+    large = batch.BatchedSystems.from_systems([W.water_box(2000, seed=1)])
+    assert 0 < small.memory_bytes < large.memory_bytes
+    assert large.memory_bytes / (3 * 2000) > 200  # lists, state, cells: hundreds of bytes per atom
