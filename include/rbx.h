@@ -325,9 +325,11 @@ int rbx_last_launch_count(const rbx_integrator* h);
  * (synchronous); U comes from the last force evaluation of the preceding rbx_batch_step when no
  * other call has changed the state since. rbx_batch_get_num_dof gives each system's degrees of
  * freedom.
- * Forces come from neighbour lists (cutoff + a skin of up to 0.15 nm) that each system rebuilds when
- * one of its atoms has moved half the skin, and that every call rebuilds at its first evaluation:
- * a system's results are a function of its own state and of the lengths of the calls that step it.
+ * Forces come from neighbour lists of atom groups (each rigid body is one group, each free atom a
+ * group of its own): two groups are listed together when their centroids lie within cutoff + a
+ * skin of 0.1 nm + both groups' radii. Each system rebuilds its lists when one of its centroids has
+ * moved half the skin, and every call rebuilds them at its first evaluation: a system's results are
+ * a function of its own state and of the lengths of the calls that step it.
  */
 typedef struct rbx_batch rbx_batch;
 /* rbx_batch_set_state builds every body from the given positions and velocities (as
@@ -379,12 +381,13 @@ int rbx_batch_memory(const rbx_batch* b, size_t* bytes);
 int rbx_batch_list_builds(rbx_batch* b, void* stream, unsigned int* counts);
 int rbx_batch_set_graph_steps(rbx_batch* b, int k);
 /* Autotuner of the batched step's schedule (no counterpart in the reference, which has no batched
- * form). It times, on the batch itself, the block size of the cell force kernel (64, 128 or 256
- * threads per cell) with direct launches. Where a step takes under 1 ms, so that launch overhead
+ * form). It times, on the batch itself, the block size of the cell list-build kernel (64, 128 or
+ * 256 threads per cell) with direct launches. Where a step takes under 1 ms, so that launch overhead
  * matters, it also times the steps per captured graph (0, 10 or 50). Each trial runs trial_steps
  * steps (2k+1 for a graph of k) twice and times the second run with CUDA events. It keeps the
  * fastest, and then restores the batch's exact state (rbx_batch_restore): neither choice changes
- * any result, since each atom's force sums keep their order and graphs replay the same launches.
+ * any result, since each group's list, and so each atom's force sum, keeps its order and graphs
+ * replay the same launches.
  * chosen[2] (optional) receives the block size and the graph run length.
  * rbx_batch_set_tuning sets both by hand. */
 int rbx_batch_autotune(rbx_batch* b, void* stream, double dt, int trial_steps, int* chosen);

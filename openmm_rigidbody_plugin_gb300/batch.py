@@ -181,7 +181,7 @@ class BatchedSystems:
         _lib.check(self._lib.rbx_batch_set_graph_steps(self._h, int(k)))
 
     def autotune(self, dt=0.002, trial_steps=3, stream=None):
-        """Pick the cell force kernel's block size and the steps per captured graph by timing them on
+        """Pick the cell list-build kernel's block size and the steps per captured graph by timing them on
         this batch; the state is restored exactly afterwards. Returns the choice."""
         out = np.zeros(2, dtype=np.int32)
         _lib.check(self._lib.rbx_batch_autotune(self._h, _stream(stream), float(dt), int(trial_steps),

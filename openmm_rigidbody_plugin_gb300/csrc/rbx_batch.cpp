@@ -24,7 +24,7 @@ using namespace rbx;
 namespace {
 
 constexpr double kOne4PiEps0 = 138.935456;  // kJ nm / (mol e^2)
-constexpr double kSkin = 0.15;              // nm: neighbour-list skin
+constexpr double kSkin = 0.1;               // nm: neighbour-list skin (of group centroids)
 constexpr int kMaxTypes = 256;              // atom types of the typed force pass (FFDev::types)
 
 #define BATCH_TRY(call)                                                                             \
@@ -54,11 +54,17 @@ struct rbx_batch {
     // force field
     DevArray<FFSys> d_sys;
     DevArray<int> d_iatom, d_isys, d_cell_of, d_cell_count, d_cell_start, d_cell_cursor, d_cell_list;
-    DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_i0;
-    DevArray<float4> d_param, d_cpos, d_cpar, d_xref, d_types;
-    DevArray<unsigned char> d_rebuild, d_nbr;  // neighbour lists (FFDev::rebuild, nbr)
+    DevArray<int> d_grp_k0, d_grp_n, d_gsys, d_kgrp;
+    DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_g0;
+    DevArray<float4> d_param, d_cpos, d_gcen, d_gref, d_gq, d_types;
+    DevArray<unsigned char> d_rebuild;  // FFDev::rebuild
+    DevArray<unsigned int> d_nbr;       // neighbour lists of groups (FFDev::nbr)
     DevArray<int> d_ncnt, d_atype;
     DevArray<unsigned int> d_rebuilds;  // list builds per system (FFDev::rebuilds)
+    // host copies for the set-up with a state: systems, cells allocated per system, group layout
+    std::vector<FFSys> sys_h;
+    std::vector<int> cells_alloc, iatom_h, grp_k0_h, grp_n_h;
+    std::vector<double> box_h;
     DevArray<double> d_e_atom, d_energy;
     FFDev ff{};
     // per-system reductions
@@ -107,6 +113,79 @@ struct rbx_batch {
 namespace {
 
 int check(const rbx_batch* b) { return b ? RBX_OK : set_error(RBX_ERR_INVALID_ARGUMENT, "null batch handle"); }
+
+// Neighbour-list geometry for a state (host positions, user order): each group's radius about its
+// centroid (constant for a rigid body), and from the largest radius of each system its list cells
+// (at least cutoff + skin + two radii per edge), the build work lists and the list capacity.
+int setup_lists(rbx_batch* b, const double* x) {
+    const int S = b->S;
+    std::vector<FFSys> sys = b->sys_h;
+    std::vector<int> mc_cell, mc_sys, sc_sys, sc_g0;
+    double cap_need = 1.0;
+    for (int s = 0; s < S; s++) {
+        FFSys& f = sys[s];
+        const double L = b->box_h[s];
+        auto img = [L](double d) { return d - L * std::nearbyint(d / L); };
+        double rho_max = 0.0;
+        for (int g = f.g0; g < f.g1; g++) {
+            const int k0 = b->grp_k0_h[g], n = b->grp_n_h[g];
+            const double* x0 = x + 3 * (size_t)b->iatom_h[k0];
+            double c[3] = {0.0, 0.0, 0.0};
+            for (int a = 1; a < n; a++)
+                for (int d = 0; d < 3; d++) c[d] += img(x[3 * (size_t)b->iatom_h[k0 + a] + d] - x0[d]);
+            for (int d = 0; d < 3; d++) c[d] = x0[d] + c[d] / n;
+            for (int a = 0; a < n; a++) {
+                double r2 = 0.0;
+                for (int d = 0; d < 3; d++) {
+                    const double v = img(x[3 * (size_t)b->iatom_h[k0 + a] + d] - c[d]);
+                    r2 += v * v;
+                }
+                rho_max = std::max(rho_max, std::sqrt(r2));
+            }
+        }
+        // the device forms the radii in FP32: a margin of 1e-3 nm keeps its ones within the cells
+        const double edge = (double)f.rl + 2.0 * rho_max + 1e-3;
+        int nc = (int)std::floor(L / edge);
+        if (nc > b->cells_alloc[s]) nc = b->cells_alloc[s];
+        if (nc < 3) nc = 1;
+        f.nc = nc;
+        if (nc > 1) {
+            for (int c = 0; c < nc * nc * nc; c++) {
+                mc_cell.push_back(f.c0 + c);
+                mc_sys.push_back(s);
+            }
+        } else {
+            for (int g = f.g0; g < f.g1; g += 64) {
+                sc_sys.push_back(s);
+                sc_g0.push_back(g);
+            }
+        }
+        const int G = f.g1 - f.g0;
+        const double reach = (double)f.rl + 2.0 * rho_max;
+        const double expect = 4.18879 * reach * reach * reach * (double)G / (L * L * L);
+        cap_need = std::max(cap_need, std::min((double)std::max(G - 1, 1), 1.35 * expect + 32.0));
+    }
+    const int cap = std::max(32, ((int)std::ceil(cap_need) + 31) / 32 * 32);
+    const size_t entries = ((size_t)std::max(b->ff.n_groups, 1) + 31) / 32 * 32 * (size_t)cap;
+    if (b->d_nbr.n < entries && b->d_nbr.alloc(entries) != cudaSuccess)
+        return set_error(RBX_ERR_CUDA, "cudaMalloc of the neighbour lists failed (%d entries per group)", cap);
+    BATCH_TRY(cudaMemcpy(b->d_sys.p, sys.data(), sizeof(FFSys) * (size_t)S, cudaMemcpyHostToDevice));
+    if (!mc_cell.empty()) {
+        BATCH_TRY(cudaMemcpy(b->d_mc_cell.p, mc_cell.data(), sizeof(int) * mc_cell.size(), cudaMemcpyHostToDevice));
+        BATCH_TRY(cudaMemcpy(b->d_mc_sys.p, mc_sys.data(), sizeof(int) * mc_sys.size(), cudaMemcpyHostToDevice));
+    }
+    if (!sc_sys.empty()) {
+        BATCH_TRY(cudaMemcpy(b->d_sc_sys.p, sc_sys.data(), sizeof(int) * sc_sys.size(), cudaMemcpyHostToDevice));
+        BATCH_TRY(cudaMemcpy(b->d_sc_g0.p, sc_g0.data(), sizeof(int) * sc_g0.size(), cudaMemcpyHostToDevice));
+    }
+    BATCH_TRY(cudaMemset(b->d_rebuild.p, 1, (size_t)S));
+    FFDev& D = b->ff;
+    D.n_mc = (int)mc_cell.size();
+    D.n_sc = (int)sc_sys.size();
+    D.cap = cap;
+    D.nbr = b->d_nbr.p;
+    return RBX_OK;
+}
 
 DevBuf buffers(rbx_batch* b) {
     rbx_buffers rb;
@@ -251,40 +330,65 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     int rc = rbx_create(&b->integ, N, ids.data(), masses, rotation_mode, precision, device);
     if (rc) { delete b; return rc; }
 
-    // force field tables: interacting atoms (charge or LJ) system by system
+    // force field tables: interacting atoms (charge or LJ) system by system and, within a system,
+    // body by body (ascending id; each free atom a group of its own)
     std::vector<FFSys> sys(num_systems);
-    std::vector<int> iatom, isys;
+    std::vector<int> iatom, isys, grp_k0, grp_n, gsys, kgrp;
     std::vector<float4> param;
     int cells = 0;
-    double cap_need = 1.0;
-    int max_sys_atoms = 0;
     for (int s = 0; s < num_systems; s++) {
         FFSys& f = sys[s];
         f.a0 = atom_offsets[s];
         f.a1 = atom_offsets[s + 1];
         f.i0 = (int)iatom.size();
+        f.g0 = (int)grp_k0.size();
+        std::map<int, std::vector<int>> bodies;
+        std::vector<int> free_atoms;
         for (int i = f.a0; i < f.a1; i++) {
             if (charges[i] == 0.0 && epsilons[i] == 0.0) continue;
-            iatom.push_back(i);
-            isys.push_back(s);
-            const float qs = (float)(std::sqrt(kOne4PiEps0) * charges[i]);
-            param.push_back(make_float4(qs, (float)(0.5 * sigmas[i]), (float)std::sqrt(std::max(epsilons[i], 0.0)),
-                                        int_bits(ids[i])));
+            if (body_indices[i] > 0) bodies[body_indices[i]].push_back(i);
+            else free_atoms.push_back(i);
         }
+        auto add_group = [&](const std::vector<int>& atoms) {
+            grp_k0.push_back((int)iatom.size());
+            grp_n.push_back((int)atoms.size());
+            gsys.push_back(s);
+            for (int i : atoms) {
+                kgrp.push_back((int)grp_k0.size() - 1);
+                iatom.push_back(i);
+                isys.push_back(s);
+                const float qs = (float)(std::sqrt(kOne4PiEps0) * charges[i]);
+                param.push_back(make_float4(qs, (float)(0.5 * sigmas[i]), (float)std::sqrt(std::max(epsilons[i], 0.0)),
+                                            int_bits(ids[i])));
+            }
+        };
+        for (auto& kv : bodies) {
+            if ((int)kv.second.size() > kMaxGroupAtoms) {
+                delete b;
+                return set_error(RBX_ERR_UNSUPPORTED, "system %d: a body with %d interacting atoms (at most %d)", s,
+                                 (int)kv.second.size(), kMaxGroupAtoms);
+            }
+            add_group(kv.second);
+        }
+        for (int i : free_atoms) add_group(std::vector<int>{i});
         f.i1 = (int)iatom.size();
+        f.g1 = (int)grp_k0.size();
+        if (f.i1 - f.i0 >= kMaxSystemAtoms) {
+            delete b;
+            return set_error(RBX_ERR_UNSUPPORTED, "system %d: %d interacting atoms (at most %d)", s, f.i1 - f.i0,
+                             kMaxSystemAtoms - 1);
+        }
         const double L = box_edges[s], rc_s = cutoffs[s];
-        // neighbour-list skin: 0.1 nm, less where the box is too small for a unique minimum image
-        // of every pair within cutoff + skin (cutoff + skin <= L/2)
-        const double skin = std::max(0.0, std::min(kSkin, 0.5 * L - rc_s));
-        const double rl = rc_s + skin;
-        f.rl2 = (float)(rl * rl);
-        f.half_skin2 = (float)(0.25 * skin * skin);
-        int nc = (int)std::floor(L / rl);
+        // Pairs are tested by minimum image when the lists are built and when forces are formed, so
+        // cutoff + skin + radii may exceed half the box: an image within the cutoff (below half the
+        // box) is always the minimum image, and its group pair is always listed.
+        f.rl = (float)(rc_s + kSkin);
+        f.half_skin2 = (float)(0.25 * kSkin * kSkin);
+        // cells for the largest grid any set of radii allows (the radii, known with the positions,
+        // can only make the cells larger and fewer)
+        int nc = (int)std::floor(L / (rc_s + kSkin));
         if (nc < 3) nc = 1;
         if (nc > 256) nc = 256;
-        const double dens = (double)(f.i1 - f.i0) / (L * L * L);
-        cap_need = std::max(cap_need, std::min((double)(f.i1 - f.i0), 1.35 * 4.18879 * rl * rl * rl * dens + 32.0));
-        max_sys_atoms = std::max(max_sys_atoms, f.i1 - f.i0);
         f.c0 = cells;
         f.nc = nc;
         cells += nc * nc * nc;
@@ -295,33 +399,24 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
         f.krf = (float)krf;
         f.crf = (float)(1.0 / rc_s + krf * rc_s * rc_s);
     }
-    // force work lists: cells of multi-cell boxes; 64-atom chunks of single-cell boxes
-    std::vector<int> mc_cell, mc_sys, sc_sys, sc_i0;
-    for (int s = 0; s < num_systems; s++) {
-        const FFSys& f = sys[s];
-        if (f.nc > 1) {
-            for (int c = 0; c < f.nc * f.nc * f.nc; c++) {
-                mc_cell.push_back(f.c0 + c);
-                mc_sys.push_back(s);
-            }
-        } else {
-            for (int i = f.i0; i < f.i1; i += 64) {
-                sc_sys.push_back(s);
-                sc_i0.push_back(i);
-            }
-        }
-    }
+    b->sys_h = sys;
+    b->cells_alloc.resize(num_systems);
+    for (int s = 0; s < num_systems; s++) b->cells_alloc[s] = sys[s].nc;
+    b->iatom_h = iatom;
+    b->grp_k0_h = grp_k0;
+    b->grp_n_h = grp_n;
+    b->box_h.assign(box_edges, box_edges + num_systems);
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) { delete b; return set_error(RBX_ERR_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e)); }
-    const int nint = (int)iatom.size();
+    const int nint = (int)iatom.size(), ngrp = (int)grp_k0.size();
     rc = upload_vec(b->d_sys, sys);
-    if (!rc) rc = upload_vec(b->d_mc_cell, mc_cell);
-    if (!rc) rc = upload_vec(b->d_mc_sys, mc_sys);
-    if (!rc) rc = upload_vec(b->d_sc_sys, sc_sys);
-    if (!rc) rc = upload_vec(b->d_sc_i0, sc_i0);
     if (!rc) rc = upload_vec(b->d_iatom, iatom);
     if (!rc) rc = upload_vec(b->d_isys, isys);
     if (!rc) rc = upload_vec(b->d_param, param);
+    if (!rc) rc = upload_vec(b->d_grp_k0, grp_k0);
+    if (!rc) rc = upload_vec(b->d_grp_n, grp_n);
+    if (!rc) rc = upload_vec(b->d_gsys, gsys);
+    if (!rc) rc = upload_vec(b->d_kgrp, kgrp);
     // atom types: the distinct (scaled charge, sigma/2, sqrt(epsilon)) triples; with at most
     // kMaxTypes of them the force pass reads one 16-byte record per neighbour (position and type)
     std::vector<float4> types;
@@ -342,76 +437,74 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     if (types.empty()) type_of.clear();
     if (!rc) rc = upload_vec(b->d_types, types);
     if (!rc) rc = upload_vec(b->d_atype, type_of);
-    if (!rc && (b->d_cell_of.alloc(std::max(nint, 1)) != cudaSuccess || b->d_cell_list.alloc(std::max(nint, 1)) != cudaSuccess ||
+    // work lists (filled with the state): at most every cell, and every 64-group chunk
+    size_t sc_max = 0;
+    for (int s = 0; s < num_systems; s++) sc_max += (size_t)(sys[s].g1 - sys[s].g0 + 63) / 64;
+    const int g1 = std::max(ngrp, 1), n1 = std::max(nint, 1);
+    if (!rc && (b->d_cell_of.alloc(g1) != cudaSuccess || b->d_cell_list.alloc(g1) != cudaSuccess ||
+                b->d_gcen.alloc(g1) != cudaSuccess || b->d_gref.alloc(g1) != cudaSuccess ||
+                b->d_gq.alloc(g1) != cudaSuccess || b->d_ncnt.alloc(g1) != cudaSuccess ||
                 b->d_cell_count.alloc(cells) != cudaSuccess || b->d_cell_start.alloc(cells + 1) != cudaSuccess ||
-                b->d_cell_cursor.alloc(cells) != cudaSuccess || b->d_cpos.alloc(std::max(nint, 1)) != cudaSuccess ||
-                b->d_cpar.alloc(std::max(nint, 1)) != cudaSuccess || b->d_e_atom.alloc(std::max(nint, 1)) != cudaSuccess ||
+                b->d_cell_cursor.alloc(cells) != cudaSuccess || b->d_cpos.alloc(n1) != cudaSuccess ||
+                b->d_e_atom.alloc(n1) != cudaSuccess || b->d_mc_cell.alloc(std::max(cells, 1)) != cudaSuccess ||
+                b->d_mc_sys.alloc(std::max(cells, 1)) != cudaSuccess ||
+                b->d_sc_sys.alloc(std::max<size_t>(sc_max, 1)) != cudaSuccess ||
+                b->d_sc_g0.alloc(std::max<size_t>(sc_max, 1)) != cudaSuccess ||
                 b->d_energy.alloc(num_systems) != cudaSuccess || b->d_ke.alloc(2 * (size_t)num_systems) != cudaSuccess ||
-                b->d_user.alloc(3 * (size_t)N) != cudaSuccess || b->d_sys_status.alloc(num_systems) != cudaSuccess))
+                b->d_user.alloc(3 * (size_t)N) != cudaSuccess || b->d_sys_status.alloc(num_systems) != cudaSuccess ||
+                b->d_rebuild.alloc(num_systems) != cudaSuccess || b->d_rebuilds.alloc(num_systems) != cudaSuccess))
         rc = set_error(RBX_ERR_CUDA, "cudaMalloc of force-field arrays failed");
-    if (!rc && cudaMemset(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)num_systems) != cudaSuccess)
-        rc = set_error(RBX_ERR_CUDA, "cudaMemset of the system status failed");
-    if (!rc && cudaMemset(b->d_cell_count.p, 0, sizeof(int) * (size_t)cells) != cudaSuccess)
-        rc = set_error(RBX_ERR_CUDA, "cudaMemset of cell counts failed");
-    // neighbour lists: entries per atom from the densest system with a wide margin, in groups of 32
-    // atoms; 16-bit entries when every system has at most 65536 interacting atoms
-    const int cap = std::max(32, ((int)std::ceil(cap_need) + 31) / 32 * 32);
-    const int nbr16 = max_sys_atoms <= 65536 ? 1 : 0;
-    const size_t groups = ((size_t)std::max(nint, 1) + 31) / 32;
-    if (!rc && (b->d_rebuild.alloc(num_systems) != cudaSuccess || b->d_xref.alloc(std::max(nint, 1)) != cudaSuccess ||
-                b->d_rebuilds.alloc(num_systems) != cudaSuccess ||
-                b->d_ncnt.alloc(std::max(nint, 1)) != cudaSuccess ||
-                b->d_nbr.alloc(groups * 32 * (size_t)cap * (nbr16 ? 2 : 4)) != cudaSuccess))
-        rc = set_error(RBX_ERR_CUDA, "cudaMalloc of the neighbour lists failed (%d entries per atom)", cap);
-    if (!rc) {
-        std::vector<int> iota(std::max(nint, 1));
-        for (int k = 0; k < (int)iota.size(); k++) iota[k] = k;  // a valid list order before the first build
-        if (cudaMemcpy(b->d_cell_list.p, iota.data(), iota.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemset(b->d_rebuild.p, 1, (size_t)num_systems) != cudaSuccess ||
-            cudaMemset(b->d_rebuilds.p, 0, sizeof(unsigned int) * (size_t)num_systems) != cudaSuccess ||
-            cudaMemset(b->d_ncnt.p, 0, sizeof(int) * (size_t)std::max(nint, 1)) != cudaSuccess ||
-            cudaMemset(b->d_cpos.p, 0, sizeof(float4) * (size_t)std::max(nint, 1)) != cudaSuccess)
-            rc = set_error(RBX_ERR_CUDA, "initialisation of the neighbour lists failed");
-    }
+    if (!rc && (cudaMemset(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)num_systems) != cudaSuccess ||
+                cudaMemset(b->d_cell_count.p, 0, sizeof(int) * (size_t)cells) != cudaSuccess ||
+                cudaMemset(b->d_rebuild.p, 1, (size_t)num_systems) != cudaSuccess ||
+                cudaMemset(b->d_rebuilds.p, 0, sizeof(unsigned int) * (size_t)num_systems) != cudaSuccess ||
+                cudaMemset(b->d_ncnt.p, 0, sizeof(int) * (size_t)g1) != cudaSuccess ||
+                cudaMemset(b->d_cell_list.p, 0, sizeof(int) * (size_t)g1) != cudaSuccess))
+        rc = set_error(RBX_ERR_CUDA, "initialisation of the force-field arrays failed");
     if (!rc && cudaMallocHost((void**)&b->h_out, sizeof(double) * 3 * (size_t)num_systems) != cudaSuccess)
         rc = set_error(RBX_ERR_CUDA, "pinned allocation failed");
     if (rc) { delete b; return rc; }
     FFDev& D = b->ff;
     D.S = num_systems;
     D.n_int = nint;
+    D.n_groups = ngrp;
     D.n_cells = cells;
     D.sys = b->d_sys.p;
     D.iatom = b->d_iatom.p;
     D.isys = b->d_isys.p;
     D.param = b->d_param.p;
+    D.grp_k0 = b->d_grp_k0.p;
+    D.grp_n = b->d_grp_n.p;
+    D.gsys = b->d_gsys.p;
+    D.kgrp = b->d_kgrp.p;
+    D.gcen = b->d_gcen.p;
+    D.gref = b->d_gref.p;
+    D.gq = b->d_gq.p;
     D.cell_of = b->d_cell_of.p;
     D.cell_count = b->d_cell_count.p;
     D.cell_start = b->d_cell_start.p;
     D.cell_cursor = b->d_cell_cursor.p;
     D.cell_list = b->d_cell_list.p;
     D.cpos = b->d_cpos.p;
-    D.cpar = b->d_cpar.p;
     D.e_atom = b->d_e_atom.p;
     D.energy = b->d_energy.p;
     D.fcap = 0.0f;
     D.sys_status = b->d_sys_status.p;
     D.rebuild = b->d_rebuild.p;
     D.rebuilds = b->d_rebuilds.p;
-    D.xref = b->d_xref.p;
-    D.nbr = b->d_nbr.p;
+    D.nbr = nullptr;  // allocated with the state (its capacity follows the groups' radii)
     D.ncnt = b->d_ncnt.p;
-    D.cap = cap;
-    D.nbr16 = nbr16;
+    D.cap = 0;
     D.types = b->d_types.p;
     D.atype = b->d_atype.p;
     D.ntypes = (int)types.size();
     D.cell_threads = 128;
-    D.n_mc = (int)mc_cell.size();
-    D.n_sc = (int)sc_sys.size();
+    D.n_mc = 0;
+    D.n_sc = 0;
     D.mc_cell = b->d_mc_cell.p;
     D.mc_sys = b->d_mc_sys.p;
     D.sc_sys = b->d_sc_sys.p;
-    D.sc_i0 = b->d_sc_i0.p;
+    D.sc_g0 = b->d_sc_g0.p;
     // the owned OpenMM-layout buffers (forces of non-interacting atoms stay zero)
     rbx_buffers rb;
     if ((rc = rbx_context_buffers(b->integ, &rb))) { delete b; return rc; }
@@ -428,6 +521,10 @@ int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, con
     int rc = check(b);
     if (rc) return rc;
     b->drop_graph();
+    if (!positions || !velocities) return set_error(RBX_ERR_INVALID_ARGUMENT, "null positions or velocities");
+    BATCH_TRY(cudaSetDevice(b->device));
+    BATCH_TRY(cudaStreamSynchronize((cudaStream_t)stream));  // no force pass in flight on the old lists
+    if ((rc = setup_lists(b, positions))) return rc;
     // positions and velocities into the device buffers, bodies built there (no host round trip)
     if ((rc = rbx_context_load(b->integ, stream, positions, velocities))) return rc;
     rbx_buffers rb;
@@ -611,9 +708,11 @@ int rbx_batch_memory(const rbx_batch* b, size_t* bytes) {
     if (!bytes) return set_error(RBX_ERR_INVALID_ARGUMENT, "null output");
     size_t n = b->d_sys.bytes() + b->d_iatom.bytes() + b->d_isys.bytes() + b->d_cell_of.bytes() +
                b->d_cell_count.bytes() + b->d_cell_start.bytes() + b->d_cell_cursor.bytes() + b->d_cell_list.bytes() +
-               b->d_mc_cell.bytes() + b->d_mc_sys.bytes() + b->d_sc_sys.bytes() + b->d_sc_i0.bytes() +
-               b->d_param.bytes() + b->d_types.bytes() + b->d_atype.bytes() + b->d_cpos.bytes() + b->d_cpar.bytes() + b->d_xref.bytes() + b->d_rebuild.bytes() + b->d_rebuilds.bytes() +
-               b->d_nbr.bytes() + b->d_ncnt.bytes() + b->d_e_atom.bytes() + b->d_energy.bytes() + b->d_body0.bytes() +
+               b->d_grp_k0.bytes() + b->d_grp_n.bytes() + b->d_gsys.bytes() + b->d_kgrp.bytes() +
+               b->d_mc_cell.bytes() + b->d_mc_sys.bytes() + b->d_sc_sys.bytes() + b->d_sc_g0.bytes() +
+               b->d_param.bytes() + b->d_cpos.bytes() + b->d_gcen.bytes() + b->d_gref.bytes() + b->d_gq.bytes() +
+               b->d_types.bytes() + b->d_rebuild.bytes() + b->d_nbr.bytes() + b->d_ncnt.bytes() + b->d_atype.bytes() +
+               b->d_rebuilds.bytes() + b->d_e_atom.bytes() + b->d_energy.bytes() + b->d_body0.bytes() +
                b->d_free0.bytes() + b->d_sys_status.bytes() + b->d_ke.bytes() + b->d_user.bytes();
     *bytes = n + (b->integ ? device_bytes(b->integ) : 0);
     return RBX_OK;

@@ -87,39 +87,48 @@ struct DevBuf {
 };
 
 // Cutoff LJ + reaction-field force field over many independent cubic boxes (rbx_forces.cu).
-// Interacting atoms (non-zero charge or LJ epsilon) are listed system by system; cells of all
-// systems are numbered consecutively.
+// Interacting atoms (non-zero charge or LJ epsilon) are listed system by system and, within a
+// system, body by body: the interacting atoms of one rigid body (or one free atom) form a group,
+// a contiguous range of the list. Neighbour lists pair groups, not atoms: a rigid group's atoms stay
+// within its radius of its centroid whatever it rotates, so only centroid motion ages a list.
+// Cells (of groups, by centroid) of all systems are numbered consecutively.
 struct FFSys {
     int a0, a1;   // device slots of the system's atoms
     int i0, i1;   // its interacting atoms, as a range of the interacting-atom list
+    int g0, g1;   // its groups
     int c0, nc;   // first cell and cells per box edge of the list build (1: one cell, all pairs)
     float L, invL, rc2, krf, crf;
-    float rl2;         // (cutoff + skin)^2: pairs kept in the neighbour lists
-    float half_skin2;  // (skin/2)^2: an atom moved this far since the build invalidates the lists
+    float rl;          // cutoff + skin: groups are listed when their centroids lie within rl + both radii
+    float half_skin2;  // (skin/2)^2: a centroid moved this far since the build invalidates the lists
 };
 struct FFDev {
-    int S, n_int, n_cells;
+    int S, n_int, n_groups, n_cells;
     const FFSys* sys;     // [S]
     const int* iatom;     // [n_int] device slot of each interacting atom
     const int* isys;      // [n_int] its system
     const float4* param;  // [n_int] sqrt(K) q, sigma/2, sqrt(epsilon), body id (int bits; 0 = free)
-    int* cell_of;         // [n_int]
+    const int* grp_k0;    // [n_groups] first interacting atom of each group
+    const int* grp_n;     // [n_groups] its atoms
+    const int* gsys;      // [n_groups] its system
+    const int* kgrp;      // [n_int] group of each interacting atom
+    float4* gcen;         // [n_groups] centroid (wrapped into the box) and radius, every evaluation
+    float4* gref;         // [n_groups] centroid at the last build
+    float4* gq;           // [n_groups] cell order: centroid and radius (list builds)
+    int* cell_of;         // [n_groups]
     int* cell_count;      // [n_cells], zero between evaluations
     int* cell_start;      // [n_cells + 1] (entry c0 + nc^3 of each system ends it)
     int* cell_cursor;     // [n_cells]
-    int* cell_list;       // [n_int] interacting-atom indices in cell order (of the last list build)
-    float4* cpos;         // [n_int] cell order: x, y, z (wrapped into the box), sqrt(K) q (or the type)
-    float4* cpar;         // [n_int] cell order: sigma/2, sqrt(epsilon), body id, device slot (int bits)
+    int* cell_list;       // [n_groups] group indices in cell order (of the last list build)
+    float4* cpos;         // [n_int] x, y, z (wrapped into the box), sqrt(K) q (or the atom's type)
     double* e_atom;       // [n_int] half pair-energy sums (energy evaluations)
-    // Neighbour lists (Verlet lists with a skin), rebuilt per system when one of its atoms has moved
-    // more than half the skin since the last build, and at the first evaluation of every call
+    // Neighbour lists of groups, rebuilt per system when one of its centroids has moved more than
+    // half the skin since the last build, and at the first evaluation of every call
     unsigned char* rebuild;  // [S] 1: rebuild this system's lists before the next force pass
     unsigned int* rebuilds;  // [S] list builds of each system so far (a statistic)
-    float4* xref;            // [n_int] cell order: positions at the last build
-    void* nbr;               // neighbour entries, u16 or u32 (nbr16), j - i0 of the system, in groups
-                             // of 32 atoms: entry e of atom p at (p/32)*32*cap + e*32 + p%32
-    int* ncnt;               // [n_int] entries per atom
-    int cap, nbr16;          // entries per atom allocated; 1: 16-bit entries
+    unsigned int* nbr;       // entries (first atom - i0) << 11 | atoms, in groups of 32 groups:
+                             // entry e of group g at (g/32)*32*cap + e*32 + g%32
+    int* ncnt;               // [n_groups] entries per group
+    int cap;                 // entries per group allocated
     // Atom types (ntypes > 0): the distinct (sqrt(K) q, sigma/2, sqrt(epsilon)) of the interacting
     // atoms; cpos .w then holds the atom's type (int bits) instead of its charge, so that the force
     // pass reads one 16-byte record per neighbour
@@ -128,17 +137,22 @@ struct FFDev {
     int ntypes;
     double* energy;       // [S] potential energy per system (kJ/mol)
     float fcap;           // > 0: each atom's force is scaled down to at most this magnitude
-    unsigned int* sys_status;  // [S] set to 1 when a force of the system is non-finite or beyond the
-                               // fixed-point range (never during a capped relaxation)
-    int cell_threads;     // block size of the cell kernel: 64, 128 (default) or 256
-    // work lists of the force kernels (static): every cell of the multi-cell boxes with its
-    // system, and every 64-atom chunk (start in the interacting-atom list) of the single-cell boxes
+    unsigned int* sys_status;  // [S] bit 0: a force of the system is non-finite or beyond the
+                               // fixed-point range (never during a capped relaxation); bit 1: a list
+                               // outgrew its capacity
+    int cell_threads;     // block size of the cell list-build kernel: 64, 128 (default) or 256
+    // work lists of the list builds (set with the state): every cell of the multi-cell boxes with
+    // its system, and every 64-group chunk (first group) of the single-cell boxes
     int n_mc, n_sc;
     const int* mc_cell;
     const int* mc_sys;
     const int* sc_sys;
-    const int* sc_i0;
+    const int* sc_g0;
 };
+// Largest first-atom offset and group size a packed list entry holds.
+constexpr int kGroupAtomBits = 11;
+constexpr int kMaxGroupAtoms = (1 << kGroupAtomBits) - 1;
+constexpr int kMaxSystemAtoms = 1 << (32 - kGroupAtomBits);
 int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* stream);
 // Fixed-point forces of slots [0, natoms) -> user-order doubles out[3*natoms] (kJ/mol/nm).
 int launch_forces_to_user(const long long* force, int stride, int natoms, double* out, void* stream);
