@@ -97,6 +97,8 @@ def parse():
     p.add_argument("--no-autotune", action="store_true",
                    help="batched/water: keep --graph-steps and the default cell-kernel block size")
     p.add_argument("--plain-systems", type=int, default=32, help="batched: systems run one per launch")
+    p.add_argument("--tile-threads", default="auto", choices=["auto", "256", "128"],
+                   help="single: step-kernel tile shape (auto: the faster of both, timed before the warm-up)")
     p.add_argument("--pbodies", type=int, default=8192, help="precision: near-degenerate bodies")
     p.add_argument("--pwaters", type=int, default=20000, help="precision: waters")
     p.add_argument("--psteps", type=int, default=1000, help="precision: steps per run")
@@ -391,6 +393,38 @@ def time_replan(k, buf, s, repeats=3):
                     "OpenMM itself does (torch indexing here)"}
 
 
+def choose_tile(k, buf, dt, stream, args, launches=40):
+    """The step kernel's tile shape for the timed steps: as asked, or (auto, single/mixed) the faster
+    of 256 and 128 threads over `launches` event-timed fused steps each, after 5 untimed ones. Both
+    shapes give bit-identical results, so the trial only advances the warm-up. Returns (threads,
+    {threads: ms per step} or None)."""
+    import torch
+    from openmm_rigidbody_plugin_gb300 import _lib
+    if args.tile_threads != "auto":
+        k.tile_threads = int(args.tile_threads)
+        return k.tile_threads, None
+    if args.precision == "double":
+        return k.tile_threads, None
+    trial = {}
+    for nt in (256, 128):
+        try:
+            k.tile_threads = nt
+        except _lib.RbxError:  # a body of more than 512 atoms
+            continue
+        for _ in range(5):
+            k.fused(buf, dt, stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(launches):
+            k.fused(buf, dt, stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        trial[nt] = e0.elapsed_time(e1) / launches
+    best = min(trial, key=trial.get)
+    k.tile_threads = best
+    return best, trial
+
+
 def measure_single(args, world, rank, local, with_cpu=True, steps=None):
     """The single-large-system integrator step (the drop-in path): the fused step kernel timed over
     `steps` launches, its roofline, e2e through the host-buffer C ABI, and the CPU port beside it.
@@ -417,6 +451,7 @@ def measure_single(args, world, rank, local, with_cpu=True, steps=None):
     torch.cuda.synchronize()
 
     k.part1(buf, dt, stream)
+    tile_threads, tile_trial = choose_tile(k, buf, dt, stream, args)
     for _ in range(args.warmup):
         k.fused(buf, dt, stream)
     torch.cuda.synchronize()
@@ -468,6 +503,7 @@ def measure_single(args, world, rank, local, with_cpu=True, steps=None):
     f_h = torch.from_numpy(np.ascontiguousarray(F)).pin_memory().numpy()
     ke2 = kernel.IntegratorKernel(s.masses, s.body_indices, rotation_mode=args.mode, precision=args.precision,
                                   device=local)
+    ke2.tile_threads = tile_threads
     ke2.context_set_state(s.positions, s.velocities, stream)
     for i in range(2):
         ke2.step_host_async(1, dt, f_h, x_h[i % 2], v_h[i % 2], stream)
@@ -502,6 +538,7 @@ def measure_single(args, world, rank, local, with_cpu=True, steps=None):
            "config": {"workload": workload_name(args.bodies, args.free) + f"; rotation mode {args.mode}; {args.precision} precision"
                                   + ("; refined energies on" if args.refined else ""),
                       "bodies_per_gpu": nb, "body_atoms_per_gpu": nba, "free_atoms_per_gpu": nf,
+                      "tile_threads": tile_threads, "tile_trial_ms_per_step": tile_trial,
                       "l2": "working set > 129 MB L2 (no flush needed)", "parallelism": f"{world} independent replicas"},
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "peak_source": peak_kind, "traffic": traffic, "algorithmic_bytes_per_launch": bytes_step,

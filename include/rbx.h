@@ -123,6 +123,19 @@ int rbx_get_rotation_mode(const rbx_integrator* h, int* out);
 int rbx_get_num_dof_reference(const rbx_integrator* h, int* out);
 
 /*
+ * Tile shape of the single/mixed step kernel (no counterpart in the reference, which launches
+ * fixed 128-thread blocks, CudaRigidBodyKernels.cpp:135-139): 256 threads per tile of at most 256
+ * bodies and 1024 body atoms (the default, 3 tiles resident per SM) or 128 threads per tile of at
+ * most 128 bodies and 512 body atoms (6 per SM). Results are identical, bit for bit, under either;
+ * only the speed differs. RBX_ERR_UNSUPPORTED for 128 threads when a body has more than 32 atoms
+ * (such bodies are summed by a whole warp, in a form of the kernel built for 256 threads only), or
+ * in double precision (one shape: 256 threads, 512 body atoms). Waits for the device; call it
+ * between steps, not during a stream capture.
+ */
+int rbx_set_tile_threads(rbx_integrator* h, int threads);
+int rbx_get_tile_threads(const rbx_integrator* h, int* out);
+
+/*
  * One half of a step on OpenMM-layout device buffers, enqueued on `stream` (cudaStream_t,
  * NULL = default stream). Replaces the integrateRigidBodyPart1 / integrateRigidBodyPart2
  * kernels and freeAtomsDelta (platforms/cuda/src/kernels/rigidbodyintegrator.cu:270-396)
@@ -381,17 +394,24 @@ int rbx_batch_memory(const rbx_batch* b, size_t* bytes);
 int rbx_batch_list_builds(rbx_batch* b, void* stream, unsigned int* counts);
 int rbx_batch_set_graph_steps(rbx_batch* b, int k);
 /* Autotuner of the batched step's schedule (no counterpart in the reference, which has no batched
- * form). It times, on the batch itself, the block size of the cell list-build kernel (64, 128 or
- * 256 threads per cell) with direct launches. Where a step takes under 1 ms, so that launch overhead
- * matters, it also times the steps per captured graph (0, 10 or 50). Each trial runs trial_steps
- * steps (2k+1 for a graph of k) twice and times the second run with CUDA events. It keeps the
- * fastest, and then restores the batch's exact state (rbx_batch_restore): neither choice changes
- * any result, since each group's list, and so each atom's force sum, keeps its order and graphs
- * replay the same launches.
- * chosen[2] (optional) receives the block size and the graph run length.
- * rbx_batch_set_tuning sets both by hand. */
+ * form). It times, on the batch itself and with direct launches:
+ *   1. the step kernel's tile shape (rbx_set_tile_threads: 256 or 128 threads, single/mixed
+ *      precision with bodies of at most 32 atoms), by the integrator launches' own event times
+ *      over 2 x trial_steps steps after an untimed run of trial_steps;
+ *   2. the block size of the cell list-build kernel (64, 128 or 256 threads per cell);
+ *   3. where a step takes under 1 ms, so that launch overhead matters, the steps per captured graph
+ *      (0, 10 or 50).
+ * Trials 2 and 3 run trial_steps steps (2k+1 for a graph of k) twice and time the second run with
+ * CUDA events. It keeps the fastest of each, and then restores the batch's exact state
+ * (rbx_batch_restore): no choice changes any result, since each body is integrated alike in any
+ * tile, each group's list (and so each atom's force sum) keeps its order, and graphs replay the
+ * same launches.
+ * chosen[2] (optional) receives the block size and the graph run length; rbx_batch_get_tile_threads
+ * the tile shape. rbx_batch_set_tuning and rbx_batch_set_tile_threads set them by hand. */
 int rbx_batch_autotune(rbx_batch* b, void* stream, double dt, int trial_steps, int* chosen);
 int rbx_batch_set_tuning(rbx_batch* b, int cell_threads, int graph_steps);
+int rbx_batch_set_tile_threads(rbx_batch* b, int threads);
+int rbx_batch_get_tile_threads(rbx_batch* b, int* out);
 /* Event timing of the force and integrator launch groups of later calls (direct launches only:
  * graphs are not used while timing is on); rbx_batch_kernel_times waits for and sums them
  * (milliseconds) and starts a new tally. */

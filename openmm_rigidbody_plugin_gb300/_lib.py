@@ -40,6 +40,8 @@ SIGNATURES = [
     ("rbx_get_num_dof", ctypes.c_int, [_vp, _ip]),
     ("rbx_get_num_dof_reference", ctypes.c_int, [_vp, _ip]),
     ("rbx_check_state", ctypes.c_int, [_vp, _vp, _ip, _ip]),
+    ("rbx_set_tile_threads", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("rbx_get_tile_threads", ctypes.c_int, [_vp, _ip]),
     ("rbx_get_num_bodies", ctypes.c_int, [_vp, _ip]),
     ("rbx_get_num_free", ctypes.c_int, [_vp, _ip]),
     ("rbx_get_rotation_mode", ctypes.c_int, [_vp, _ip]),
@@ -84,6 +86,8 @@ SIGNATURES = [
     ("rbx_batch_energies", ctypes.c_int, [_vp, _vp, _dp]),
     ("rbx_batch_autotune", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_int, _ip]),
     ("rbx_batch_set_tuning", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
+    ("rbx_batch_set_tile_threads", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("rbx_batch_get_tile_threads", ctypes.c_int, [_vp, _ip]),
     ("rbx_batch_forces", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_batch_get_num_dof", ctypes.c_int, [_vp, _ip]),
     ("rbx_batch_status", ctypes.c_int, [_vp, _vp, _ip, _ip]),

@@ -181,12 +181,24 @@ class BatchedSystems:
         _lib.check(self._lib.rbx_batch_set_graph_steps(self._h, int(k)))
 
     def autotune(self, dt=0.002, trial_steps=3, stream=None):
-        """Pick the cell list-build kernel's block size and the steps per captured graph by timing them on
-        this batch; the state is restored exactly afterwards. Returns the choice."""
+        """Pick the step kernel's tile shape, the cell list-build kernel's block size and the steps per
+        captured graph by timing them on this batch; the state is restored exactly afterwards.
+        Returns the choice."""
         out = np.zeros(2, dtype=np.int32)
         _lib.check(self._lib.rbx_batch_autotune(self._h, _stream(stream), float(dt), int(trial_steps),
                                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
-        return {"cell_threads": int(out[0]), "graph_steps": int(out[1])}
+        return {"tile_threads": self.tile_threads, "cell_threads": int(out[0]), "graph_steps": int(out[1])}
+
+    @property
+    def tile_threads(self):
+        """Block size of the step kernel's tiles (results do not depend on it)."""
+        out = ctypes.c_int()
+        _lib.check(self._lib.rbx_batch_get_tile_threads(self._h, ctypes.byref(out)))
+        return out.value
+
+    @tile_threads.setter
+    def tile_threads(self, threads):
+        _lib.check(self._lib.rbx_batch_set_tile_threads(self._h, int(threads)))
 
     def set_tuning(self, cell_threads, graph_steps):
         _lib.check(self._lib.rbx_batch_set_tuning(self._h, int(cell_threads), int(graph_steps)))

@@ -25,7 +25,7 @@ namespace {
 
 constexpr double kOne4PiEps0 = 138.935456;  // kJ nm / (mol e^2)
 constexpr double kSkin = 0.1;               // nm: neighbour-list skin (of group centroids)
-constexpr int kMaxTypes = 256;              // atom types of the typed force pass (FFDev::types)
+constexpr int kMaxTypes = 32;               // atom types of the type-pair table (FFDev::types)
 
 #define BATCH_TRY(call)                                                                             \
     do {                                                                                            \
@@ -55,7 +55,7 @@ struct rbx_batch {
     DevArray<FFSys> d_sys;
     DevArray<int> d_iatom, d_isys, d_cell_of, d_cell_count, d_cell_start, d_cell_cursor, d_cell_list;
     DevArray<int> d_grp_k0, d_grp_n, d_gsys, d_kgrp;
-    DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_g0;
+    DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_g0, d_small_groups, d_large_groups;
     DevArray<float4> d_param, d_cpos, d_gcen, d_gref, d_gq, d_types;
     DevArray<unsigned char> d_rebuild;  // FFDev::rebuild
     DevArray<unsigned int> d_nbr;       // neighbour lists of groups (FFDev::nbr)
@@ -65,7 +65,7 @@ struct rbx_batch {
     std::vector<FFSys> sys_h;
     std::vector<int> cells_alloc, iatom_h, grp_k0_h, grp_n_h;
     std::vector<double> box_h;
-    DevArray<double> d_e_atom, d_energy;
+    DevArray<double> d_e_group, d_energy;
     FFDev ff{};
     // per-system reductions
     DevArray<int> d_body0, d_free0;
@@ -145,6 +145,7 @@ int setup_lists(rbx_batch* b, const double* x) {
         }
         // the device forms the radii in FP32: a margin of 1e-3 nm keeps its ones within the cells
         const double edge = (double)f.rl + 2.0 * rho_max + 1e-3;
+        f.pair_image = std::sqrt((double)f.rc2) + 2.0 * rho_max + 1e-3 >= 0.5 * L ? 1 : 0;
         int nc = (int)std::floor(L / edge);
         if (nc > b->cells_alloc[s]) nc = b->cells_alloc[s];
         if (nc < 3) nc = 1;
@@ -166,7 +167,7 @@ int setup_lists(rbx_batch* b, const double* x) {
         cap_need = std::max(cap_need, std::min((double)std::max(G - 1, 1), 1.35 * expect + 32.0));
     }
     const int cap = std::max(32, ((int)std::ceil(cap_need) + 31) / 32 * 32);
-    const size_t entries = ((size_t)std::max(b->ff.n_groups, 1) + 31) / 32 * 32 * (size_t)cap;
+    const size_t entries = (size_t)std::max(b->ff.n_groups, 1) * (size_t)cap;
     if (b->d_nbr.n < entries && b->d_nbr.alloc(entries) != cudaSuccess)
         return set_error(RBX_ERR_CUDA, "cudaMalloc of the neighbour lists failed (%d entries per group)", cap);
     BATCH_TRY(cudaMemcpy(b->d_sys.p, sys.data(), sizeof(FFSys) * (size_t)S, cudaMemcpyHostToDevice));
@@ -362,14 +363,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
                                             int_bits(ids[i])));
             }
         };
-        for (auto& kv : bodies) {
-            if ((int)kv.second.size() > kMaxGroupAtoms) {
-                delete b;
-                return set_error(RBX_ERR_UNSUPPORTED, "system %d: a body with %d interacting atoms (at most %d)", s,
-                                 (int)kv.second.size(), kMaxGroupAtoms);
-            }
-            add_group(kv.second);
-        }
+        for (auto& kv : bodies) add_group(kv.second);
         for (int i : free_atoms) add_group(std::vector<int>{i});
         f.i1 = (int)iatom.size();
         f.g1 = (int)grp_k0.size();
@@ -379,11 +373,13 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
                              kMaxSystemAtoms - 1);
         }
         const double L = box_edges[s], rc_s = cutoffs[s];
-        // Pairs are tested by minimum image when the lists are built and when forces are formed, so
-        // cutoff + skin + radii may exceed half the box: an image within the cutoff (below half the
-        // box) is always the minimum image, and its group pair is always listed.
+        // Pairs are tested by minimum image when the lists are built (and, where cutoff + two radii
+        // may reach half the box, when forces are formed), so cutoff + skin + radii may exceed half
+        // the box: an image within the cutoff (below half the box) is always the minimum image, and
+        // its group pair is always listed.
         f.rl = (float)(rc_s + kSkin);
         f.half_skin2 = (float)(0.25 * kSkin * kSkin);
+        f.pair_image = 1;  // until the radii are known (rbx_batch_set_state)
         // cells for the largest grid any set of radii allows (the radii, known with the positions,
         // can only make the cells larger and fewer)
         int nc = (int)std::floor(L / (rc_s + kSkin));
@@ -417,8 +413,13 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     if (!rc) rc = upload_vec(b->d_grp_n, grp_n);
     if (!rc) rc = upload_vec(b->d_gsys, gsys);
     if (!rc) rc = upload_vec(b->d_kgrp, kgrp);
+    std::vector<int> small_groups, large_groups;  // the two force passes
+    for (int g = 0; g < (int)grp_n.size(); g++) (grp_n[g] <= 4 ? small_groups : large_groups).push_back(g);
+    if (!rc) rc = upload_vec(b->d_small_groups, small_groups);
+    if (!rc) rc = upload_vec(b->d_large_groups, large_groups);
     // atom types: the distinct (scaled charge, sigma/2, sqrt(epsilon)) triples; with at most
     // kMaxTypes of them the force pass reads one 16-byte record per neighbour (position and type)
+    // and takes each pair's coefficients from a table of type pairs
     std::vector<float4> types;
     std::vector<int> type_of(param.size(), -1);
     {
@@ -435,7 +436,18 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
         if ((int)types.size() > kMaxTypes) types.clear();
     }
     if (types.empty()) type_of.clear();
-    if (!rc) rc = upload_vec(b->d_types, types);
+    // the type-pair table: (K q_i q_j, C12 = 4 eps sig^12, C6 = 4 eps sig^6) with Lorentz-Berthelot
+    // sig = (sig_i + sig_j)/2, eps = sqrt(eps_i eps_j), formed in FP64 from the FP32 type values
+    const int nt = (int)types.size();
+    std::vector<float4> pair_table((size_t)nt * nt);
+    for (int i = 0; i < nt; i++)
+        for (int j = 0; j < nt; j++) {
+            const double sig = (double)types[i].y + (double)types[j].y, eps = (double)types[i].z * (double)types[j].z;
+            const double s6 = sig * sig * sig * sig * sig * sig;
+            pair_table[(size_t)i * nt + j] = make_float4((float)((double)types[i].x * (double)types[j].x),
+                                                         (float)(4.0 * eps * s6 * s6), (float)(4.0 * eps * s6), 0.0f);
+        }
+    if (!rc) rc = upload_vec(b->d_types, pair_table);
     if (!rc) rc = upload_vec(b->d_atype, type_of);
     // work lists (filled with the state): at most every cell, and every 64-group chunk
     size_t sc_max = 0;
@@ -446,7 +458,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
                 b->d_gq.alloc(g1) != cudaSuccess || b->d_ncnt.alloc(g1) != cudaSuccess ||
                 b->d_cell_count.alloc(cells) != cudaSuccess || b->d_cell_start.alloc(cells + 1) != cudaSuccess ||
                 b->d_cell_cursor.alloc(cells) != cudaSuccess || b->d_cpos.alloc(n1) != cudaSuccess ||
-                b->d_e_atom.alloc(n1) != cudaSuccess || b->d_mc_cell.alloc(std::max(cells, 1)) != cudaSuccess ||
+                b->d_e_group.alloc(g1) != cudaSuccess || b->d_mc_cell.alloc(std::max(cells, 1)) != cudaSuccess ||
                 b->d_mc_sys.alloc(std::max(cells, 1)) != cudaSuccess ||
                 b->d_sc_sys.alloc(std::max<size_t>(sc_max, 1)) != cudaSuccess ||
                 b->d_sc_g0.alloc(std::max<size_t>(sc_max, 1)) != cudaSuccess ||
@@ -486,7 +498,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     D.cell_cursor = b->d_cell_cursor.p;
     D.cell_list = b->d_cell_list.p;
     D.cpos = b->d_cpos.p;
-    D.e_atom = b->d_e_atom.p;
+    D.e_group = b->d_e_group.p;
     D.energy = b->d_energy.p;
     D.fcap = 0.0f;
     D.sys_status = b->d_sys_status.p;
@@ -498,6 +510,10 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     D.types = b->d_types.p;
     D.atype = b->d_atype.p;
     D.ntypes = (int)types.size();
+    D.n_small = (int)small_groups.size();
+    D.n_large = (int)large_groups.size();
+    D.small_groups = b->d_small_groups.p;
+    D.large_groups = b->d_large_groups.p;
     D.cell_threads = 128;
     D.n_mc = 0;
     D.n_sc = 0;
@@ -710,9 +726,10 @@ int rbx_batch_memory(const rbx_batch* b, size_t* bytes) {
                b->d_cell_count.bytes() + b->d_cell_start.bytes() + b->d_cell_cursor.bytes() + b->d_cell_list.bytes() +
                b->d_grp_k0.bytes() + b->d_grp_n.bytes() + b->d_gsys.bytes() + b->d_kgrp.bytes() +
                b->d_mc_cell.bytes() + b->d_mc_sys.bytes() + b->d_sc_sys.bytes() + b->d_sc_g0.bytes() +
+               b->d_small_groups.bytes() + b->d_large_groups.bytes() +
                b->d_param.bytes() + b->d_cpos.bytes() + b->d_gcen.bytes() + b->d_gref.bytes() + b->d_gq.bytes() +
                b->d_types.bytes() + b->d_rebuild.bytes() + b->d_nbr.bytes() + b->d_ncnt.bytes() + b->d_atype.bytes() +
-               b->d_rebuilds.bytes() + b->d_e_atom.bytes() + b->d_energy.bytes() + b->d_body0.bytes() +
+               b->d_rebuilds.bytes() + b->d_e_group.bytes() + b->d_energy.bytes() + b->d_body0.bytes() +
                b->d_free0.bytes() + b->d_sys_status.bytes() + b->d_ke.bytes() + b->d_user.bytes();
     *bytes = n + (b->integ ? device_bytes(b->integ) : 0);
     return RBX_OK;
@@ -787,9 +804,35 @@ int rbx_batch_autotune(rbx_batch* b, void* stream, double dt, int trial_steps, i
     const int k0 = b->graph_k;
     int best_ct = b->ff.cell_threads, best_k = k0;
     float best = 0.0f, ms = 0.0f;
-    // 1. block size of the cell force kernel, direct launches
     b->graph_k = 0;
     b->drop_graph();
+    // 1. tile shape of the step kernel (single/mixed; 128 threads only for bodies of at most 32
+    // atoms): the integrator launches alone, event-timed over 2 x trial_steps steps after one
+    // untimed run, since they are a small share of a step
+    int best_nt = 0;
+    if (!rc && (rc = rbx_get_tile_threads(b->integ, &best_nt)) == RBX_OK) {
+        const int nts[2] = {kThreadsF, kThreadsFNarrow};
+        double best_i = 0.0;
+        bool any = false;
+        for (int nt : nts) {
+            if (rbx_set_tile_threads(b->integ, nt) != RBX_OK) continue;  // shape not supported here
+            b->timing = true;
+            if ((rc = rbx_batch_step(b, stream, trial_steps, dt)) || (rc = rbx_batch_set_timing(b, 1)) ||
+                (rc = rbx_batch_step(b, stream, 2 * trial_steps, dt)))
+                break;
+            double mf = 0.0, mi = 0.0;
+            if ((rc = rbx_batch_kernel_times(b, &mf, &mi, nullptr))) break;
+            if (!any || mi < best_i) {
+                best_i = mi;
+                best_nt = nt;
+                any = true;
+            }
+        }
+        b->timing = false;
+        const int rc1 = rbx_set_tile_threads(b->integ, best_nt);
+        if (!rc) rc = rc1;
+    }
+    // 2. block size of the cell list-build kernel, direct launches
     const int cts[3] = {64, 128, 256};
     for (int i = 0; i < 3 && !rc; i++) {
         if (!b->ff.n_mc && cts[i] != best_ct) continue;
@@ -801,7 +844,7 @@ int rbx_batch_autotune(rbx_batch* b, void* stream, double dt, int trial_steps, i
         }
     }
     b->ff.cell_threads = best_ct;
-    // 2. steps per captured graph, where launch overhead matters (steps under 1 ms)
+    // 3. steps per captured graph, where launch overhead matters (steps under 1 ms)
     if (!rc && best < 1.0f) {
         const int ks[3] = {0, 10, 50};
         float best_g = 0.0f;
@@ -822,6 +865,9 @@ int rbx_batch_autotune(rbx_batch* b, void* stream, double dt, int trial_steps, i
     b->graph_k = best_k;
     b->drop_graph();
     b->timing = timing;
+    b->ev_marks.clear();
+    b->ev_kind.clear();
+    b->ev_used = 0;
     const int rc2 = rbx_batch_restore(b, stream, body.data(), x.data(), v.data());
     if (rc) return rc;
     if (rc2) return rc2;
@@ -830,6 +876,22 @@ int rbx_batch_autotune(rbx_batch* b, void* stream, double dt, int trial_steps, i
         chosen[1] = best_k;
     }
     return RBX_OK;
+}
+
+int rbx_batch_set_tile_threads(rbx_batch* b, int threads) {
+    int rc = check(b);
+    if (rc) return rc;
+    int cur = 0;
+    if ((rc = rbx_get_tile_threads(b->integ, &cur))) return rc;
+    if (cur == threads) return RBX_OK;
+    b->drop_graph();
+    return rbx_set_tile_threads(b->integ, threads);
+}
+
+int rbx_batch_get_tile_threads(rbx_batch* b, int* out) {
+    int rc = check(b);
+    if (rc) return rc;
+    return rbx_get_tile_threads(b->integ, out);
 }
 
 int rbx_batch_set_tuning(rbx_batch* b, int cell_threads, int graph_steps) {

@@ -26,10 +26,12 @@
 //   7. ff_build_cells / ff_build_box  one block per cell (27 neighbour cells staged in shared
 //                  memory) or per 64 groups of a single-cell box (all groups, minimum image): every
 //                  other group in range, in a fixed order, into the group's list
-//   8. ff_force_groups  one thread per atom (all systems): the atoms of the groups in its group's
-//                  list, pairs within the cutoff (minimum image per pair), no atomics; forces
-//                  written as OpenMM fixed point (2^32) to the slot, pair terms summed in list order
-//   9. ff_energy   (energy evaluations only) one block per system: fixed-order FP64 sum.
+//   8. ff_force_groups  one warp per group (all systems): the group's atoms in shared memory, the
+//                  lanes streaming the atoms of the listed groups, pairs within the cutoff; per-lane
+//                  partial sums joined by a fixed butterfly, no atomics; forces written as OpenMM
+//                  fixed point (2^32) to the slots
+//   9. ff_energy   (energy evaluations only) one block per system: fixed-order FP64 sum of its
+//                  groups' pair energies.
 // The atoms of one group never meet in a list: pairs of one rigid body are excluded, as the
 // plugin's ForceField helper removes them (python/forcefield.py:131-138).
 #include <cuda_runtime.h>
@@ -73,8 +75,9 @@ __device__ __forceinline__ float3 min_image(float dx, float dy, float dz, const 
     return make_float3(dx - S.L * rintf(dx * S.invL), dy - S.L * rintf(dy * S.invL), dz - S.L * rintf(dz * S.invL));
 }
 
-// 1. Per group: positions and types of its atoms, its centroid (the mean of the atoms' minimum-image
-// displacements from its first atom) and radius, and the rebuild test.
+// 1. Per group: its centroid (the mean of the atoms' minimum-image displacements from its first
+// atom, wrapped into the box) and radius, its atoms at their images nearest the centroid (so that
+// one periodic shift moves a whole group) with their types, and the rebuild test.
 __global__ void ff_gcheck(FFDev D, DevBuf B, int prec) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= D.n_groups) return;
@@ -95,10 +98,10 @@ __global__ void ff_gcheck(FFDev D, DevBuf B, int prec) {
     float rho2 = 0.f;
     for (int a = 0; a < n; a++) {
         const int k = k0 + a;
-        const float3 x = wrap_box(atom_position(B, prec, D.iatom[k]), S);
+        const float3 x = atom_position(B, prec, D.iatom[k]);
         const float3 d = min_image(x.x - c.x, x.y - c.y, x.z - c.z, S);
         rho2 = fmaxf(rho2, fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z)));
-        D.cpos[k] = make_float4(x.x, x.y, x.z, D.ntypes ? __int_as_float(D.atype[k]) : D.param[k].x);
+        D.cpos[k] = make_float4(c.x + d.x, c.y + d.y, c.z + d.z, D.ntypes ? __int_as_float(D.atype[k]) : D.param[k].x);
     }
     D.gcen[g] = make_float4(c.x, c.y, c.z, sqrtf(rho2));
     if (D.rebuild[s]) return;
@@ -180,7 +183,7 @@ __global__ void ff_scatter(FFDev D) {
 // entries against all of them (the entries are distinct, so the ranks are a permutation); a cell
 // larger than the stage falls back to an insertion sort by one lane.
 constexpr int kSortWarps = 4, kSortStage = 512;
-constexpr int kMaxTypesDev = 256;  // largest type table of the typed force pass (the host's limit)
+constexpr int kMaxTypesDev = 32;  // most atom types of the type-pair table (the host's limit)
 __global__ void __launch_bounds__(32 * kSortWarps) ff_sort(FFDev D) {
     __shared__ int stage[kSortWarps][kSortStage];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -228,16 +231,16 @@ __global__ void ff_gather(FFDev D) {
 // liquid).
 __device__ __forceinline__ void list_append(const FFDev& D, int g, int s, int& n, unsigned int entry) {
     if (n < D.cap) {
-        D.nbr[(size_t)(g >> 5) * 32 * D.cap + (size_t)n * 32 + (g & 31)] = entry;
+        D.nbr[(size_t)g * D.cap + n] = entry;
     } else if (n == D.cap && D.sys_status) {
         atomicOr(D.sys_status + s, 2u);
     }
     n++;
 }
 
-// Group j as a list entry: its first atom relative to the system's, and its atom count.
-__device__ __forceinline__ unsigned int pack_group(const FFDev& D, const FFSys& S, int j) {
-    return ((unsigned int)(D.grp_k0[j] - S.i0) << kGroupAtomBits) | (unsigned int)D.grp_n[j];
+// Group j as a list entry: its index relative to the system's first group.
+__device__ __forceinline__ unsigned int pack_group(const FFDev&, const FFSys& S, int j) {
+    return (unsigned int)(j - S.g0);
 }
 
 // 7a. Lists of multi-cell boxes: one block per cell; its groups kFC at a time, each of the 27
@@ -348,9 +351,9 @@ struct ESum {
     __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
 
-template <bool ENERGY>
-__device__ __forceinline__ void store_force(const FFDev& D, long long* __restrict__ force, int stride, int k, int slot,
-                                            float fx, float fy, float fz, const ESum& e, int si) {
+// A group atom's force as OpenMM fixed point (2^32) in its device slot.
+__device__ __forceinline__ void store_force(const FFDev& D, long long* __restrict__ force, int stride, int slot, float fx,
+                                            float fy, float fz, int si) {
     if (D.fcap > 0.0f) {  // relaxation: cap the magnitude
         const float f2 = fmaf(fx, fx, fmaf(fy, fy, fz * fz));
         if (f2 > D.fcap * D.fcap) {
@@ -371,77 +374,219 @@ __device__ __forceinline__ void store_force(const FFDev& D, long long* __restric
     force[slot] = __float2ll_rn(fx * 0x1p32f);
     force[slot + stride] = __float2ll_rn(fy * 0x1p32f);
     force[slot + 2 * stride] = __float2ll_rn(fz * 0x1p32f);
-    if (ENERGY) D.e_atom[k] = 0.5 * e.value();
 }
 
-// 8. Forces from the group lists: one thread per atom k, the atoms of every group in its group's
-// list, in list order; a pair beyond the cutoff adds exactly nothing (its term is selected to zero).
+// 8. Forces from the group lists: one warp per group. The group's atoms (KIC at a time) sit in
+// shared memory. The lanes take the group's list entries 32 at a time: each finds its listed
+// group's periodic shift (the minimum image of its centroid relative to this group's) and drops
+// the entry when the centroids lie farther apart than cutoff + both radii (no pair of the two is
+// then within the cutoff). The surviving groups' atoms are expanded in list order into a queue of
+// (atom, entry) words and streamed, 32 at a time, one per lane (the next 32 are loaded while this
+// 32 are paired): each streamed atom is shifted and paired with every group atom. Each lane keeps
+// partial sums per group atom; a fixed butterfly of shuffles joins the lanes, so every force is a
+// sum in a fixed order, with no atomics. A pair beyond the cutoff adds exactly nothing (its term is
+// selected to zero, never multiplied).
+// Atoms sit at their images nearest their own group's centroid, so the group shift gives the
+// minimum image of every pair within the cutoff when cutoff + two radii < L/2; systems of smaller
+// boxes (FFSys::pair_image) take the minimum image per pair as well.
+// Groups of at most 4 atoms (waters, free atoms) run in a launch with KIC = 4, the others with
+// KIC = 12 (fewer registers for the common case). With at most 32 atom types (PT) each pair's
+// (K q_i q_j, C12, C6) comes from a type-pair table in shared memory, else from the atoms' own
+// parameters by Lorentz-Berthelot.
 // The pair term is OpenMM's CutoffPeriodic form: reaction-field Coulomb and unshifted LJ.
-template <bool ENERGY, bool TYPED>
-__global__ void __launch_bounds__(128) ff_force_groups(FFDev D, long long* __restrict__ force, int stride) {
-    __shared__ float4 stype[TYPED ? kMaxTypesDev : 1];
-    if (TYPED) {
-        for (int t = threadIdx.x; t < D.ntypes; t += blockDim.x) stype[t] = D.types[t];
+constexpr int kFW = 4;     // warps (groups) per block
+constexpr int kQ = 256;    // streamed-atom queue per warp
+constexpr int kSmallGroup = 4;
+constexpr int kLargeChunk = 12;
+
+// One neighbour (position xj after its shift; w: type bits, or its parameters pj) against the ni
+// group atoms in shared memory. RELAX: coincident atoms have no direction and add nothing. PI: the
+// minimum image per pair.
+template <int KIC, bool ENERGY, bool PT, bool RELAX, bool PI>
+__device__ __forceinline__ void pair_terms(const float4* xs, const float4* ps, int ni, const FFSys& S,
+                                           const float4* ptab, int ntypes, float4 xj, float4 pj, bool valid,
+                                           float (&f)[KIC][3], ESum& en) {
+    const float4* prow = PT ? ptab + __float_as_int(xj.w) : nullptr;  // column of the neighbour's type
+#pragma unroll
+    for (int a = 0; a < KIC; a++) {
+        if (a >= ni) break;
+        const float4 xi = xs[a];
+        float3 d = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+        if (PI) d = min_image(d.x, d.y, d.z, S);
+        const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
+        const bool in = valid && r2 < S.rc2 && !(RELAX && r2 < 1e-8f);
+        const float inv_r = rsqrtf(r2), inv_r2 = inv_r * inv_r, inv_r6 = inv_r2 * inv_r2 * inv_r2;
+        float qq, c12, c6;
+        if (PT) {
+            const float4 t = prow[__float_as_int(xi.w) * ntypes];
+            qq = t.x;
+            c12 = t.y;
+            c6 = t.z;
+        } else {
+            const float4 pi = ps[a];
+            qq = pi.x * pj.x;
+            const float sig = pi.y + pj.y, sig2 = sig * sig, sig6 = sig2 * sig2 * sig2;
+            c6 = 4.0f * (pi.z * pj.z) * sig6;
+            c12 = c6 * sig6;
+        }
+        const float t6 = c6 * inv_r6, t12 = c12 * inv_r6 * inv_r6;
+        float gf = qq * (inv_r * inv_r2 - 2.0f * S.krf) + fmaf(12.0f, t12, -6.0f * t6) * inv_r2;
+        gf = in ? gf : 0.0f;
+        f[a][0] = fmaf(gf, d.x, f[a][0]);
+        f[a][1] = fmaf(gf, d.y, f[a][1]);
+        f[a][2] = fmaf(gf, d.z, f[a][2]);
+        if (ENERGY && in) en.add(qq * (inv_r + S.krf * r2 - S.crf) + (t12 - t6));
+    }
+}
+
+template <int KIC, bool ENERGY, bool PT, bool RELAX>
+__global__ void __launch_bounds__(32 * kFW, KIC == kSmallGroup ? 8 : 5)
+    ff_force_groups(FFDev D, const int* __restrict__ work, int n_work, long long* __restrict__ force, int stride) {
+    __shared__ float4 stab[PT ? kMaxTypesDev * kMaxTypesDev : 1];
+    __shared__ float4 sxi[kFW][KIC];           // group atoms: position, type or charge
+    __shared__ float4 spi[kFW][PT ? 1 : KIC];  // their sqrt(K) q, sigma/2, sqrt(epsilon)
+    __shared__ float4 ssh[kFW][32];            // periodic shift of each lane's listed group
+    __shared__ int squeue[kFW][kQ];            // streamed atoms: (atom - i0) << 5 | lane of its entry
+    const int nt = D.ntypes;
+    if (PT) {
+        for (int t = threadIdx.x; t < nt * nt; t += blockDim.x) stab[t] = D.types[t];
         __syncthreads();
     }
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= D.n_int) return;
-    const int s = D.isys[k];
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    const int w = blockIdx.x * kFW + warp;
+    if (w >= n_work) return;
+    constexpr unsigned int kAll = 0xffffffffu;
+    const int g = work[w];
+    const int s = D.gsys[g];
     const FFSys S = D.sys[s];
-    const int g = D.kgrp[k];
-    const float4 xi = D.cpos[k];
-    const float4 par = D.param[k];  // sqrt(K) q, sigma/2, sqrt(epsilon)
-    const int n = D.ncnt[g];
-    const unsigned int* __restrict__ nb = D.nbr + (size_t)(g >> 5) * 32 * D.cap + (g & 31);
+    const float4 c = D.gcen[g];
+    const int k0 = D.grp_k0[g], ng = D.grp_n[g], n = D.ncnt[g];
+    const unsigned int* __restrict__ nb = D.nbr + (size_t)g * D.cap;
     const float4* __restrict__ cpos = D.cpos + S.i0;
     const float4* __restrict__ cpar = D.param + S.i0;
-    const bool relax = D.fcap > 0.0f;
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    ESum en;
-    unsigned int next = n > 0 ? nb[0] : 0u;
-    for (int e = 0; e < n; e++) {
-        const unsigned int w = next;
-        if (e + 1 < n) next = nb[(size_t)(e + 1) * 32];  // the next entry's load overlaps this group
-        const int j0 = (int)(w >> kGroupAtomBits), nj = (int)(w & (unsigned int)kMaxGroupAtoms);
-        for (int a = 0; a < nj; a++) {
-            const float4 xq = cpos[j0 + a];
-            float qj, sj, ej;
-            if (TYPED) {  // one 16-byte record per neighbour; parameters from the type table
-                const float4 tq = stype[__float_as_int(xq.w)];
-                qj = tq.x;
-                sj = tq.y;
-                ej = tq.z;
-            } else {
-                const float4 pq = cpar[j0 + a];
-                qj = pq.x;
-                sj = pq.y;
-                ej = pq.z;
+    const float reach = sqrtf(S.rc2) + c.w;
+    const bool pim = S.pair_image != 0;
+    float4* xs = sxi[warp];
+    float4* ps = spi[warp];
+    float4* sh = ssh[warp];
+    int* queue = squeue[warp];
+    double e_sum = 0.0;
+    for (int a0 = 0; a0 < ng; a0 += KIC) {
+        const int ni = min(KIC, ng - a0);
+        __syncwarp();
+        if (lane < ni) {
+            const int k = k0 + a0 + lane;
+            xs[lane] = D.cpos[k];
+            if (!PT) ps[lane] = D.param[k];
+        }
+        __syncwarp();
+        float f[KIC][3];
+#pragma unroll
+        for (int a = 0; a < KIC; a++) f[a][0] = f[a][1] = f[a][2] = 0.0f;
+        ESum en;
+        for (int e0 = 0; e0 < n; e0 += 32) {
+            int nj = 0, j0 = 0;
+            float4 shift = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (e0 + lane < n) {
+                const int gj = S.g0 + (int)nb[e0 + lane];
+                const float4 cj = D.gcen[gj];
+                const int njg = D.grp_n[gj], j0g = D.grp_k0[gj];
+                const float dx = cj.x - c.x, dy = cj.y - c.y, dz = cj.z - c.z;
+                shift = make_float4(-S.L * rintf(dx * S.invL), -S.L * rintf(dy * S.invL), -S.L * rintf(dz * S.invL), 0.f);
+                const float ex = dx + shift.x, ey = dy + shift.y, ez = dz + shift.z;
+                const float lim = reach + cj.w;
+                if (fmaf(ex, ex, fmaf(ey, ey, ez * ez)) < lim * lim) {
+                    nj = njg;
+                    j0 = j0g - S.i0;
+                }
             }
-            const float3 d = min_image(xi.x - xq.x, xi.y - xq.y, xi.z - xq.z, S);
-            const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
-            // relaxation: coincident atoms have no direction
-            const bool in = r2 < S.rc2 && !(relax && r2 < 1e-8f);
-            const float r2s = in ? r2 : 1.0f;
-            const float inv_r = rsqrtf(r2s), inv_r2 = inv_r * inv_r;
-            const float qq = par.x * qj;
-            const float sig = par.y + sj, eps = par.z * ej;
-            const float s2 = sig * sig * inv_r2, s6 = s2 * s2 * s2;
-            float gf = qq * (inv_r * inv_r2 - 2.0f * S.krf) + 4.0f * eps * (12.0f * s6 * s6 - 6.0f * s6) * inv_r2;
-            gf = in ? gf : 0.0f;
-            fx = fmaf(gf, d.x, fx);
-            fy = fmaf(gf, d.y, fy);
-            fz = fmaf(gf, d.z, fz);
-            if (ENERGY && in) en.add(qq * (inv_r + S.krf * r2 - S.crf) + 4.0f * eps * (s6 * s6 - s6));
+            __syncwarp();  // the previous batch's readers of sh and queue are done
+            sh[lane] = shift;
+            int incl = nj;  // inclusive prefix sum of the atom counts over the lanes
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(kAll, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int total = __shfl_sync(kAll, incl, 31), excl = incl - nj;
+            for (int base = 0; base < total; base += kQ) {
+                __syncwarp();
+                const int hi = min(incl, base + kQ);
+                for (int t = max(excl, base); t < hi; t++) queue[t - base] = ((j0 + t - excl) << 5) | lane;
+                __syncwarp();
+                const int cnt = min(kQ, total - base);
+                bool valid = lane < cnt;
+                int qv = queue[valid ? lane : 0];
+                float4 xq = cpos[qv >> 5];
+                for (int q0 = 0; q0 < cnt; q0 += 32) {
+                    const int qn = q0 + 32;
+                    const bool vn = qn + lane < cnt;
+                    int qvn = qv;
+                    float4 xqn = xq;
+                    if (qn < cnt) {
+                        qvn = queue[vn ? qn + lane : qn];
+                        xqn = cpos[qvn >> 5];
+                    }
+                    const float4 sv = sh[qv & 31];
+                    const float4 xj = make_float4(xq.x + sv.x, xq.y + sv.y, xq.z + sv.z, xq.w);
+                    const float4 pj = PT ? xj : cpar[qv >> 5];
+                    if (pim)
+                        pair_terms<KIC, ENERGY, PT, RELAX, true>(xs, ps, ni, S, stab, nt, xj, pj, valid, f, en);
+                    else
+                        pair_terms<KIC, ENERGY, PT, RELAX, false>(xs, ps, ni, S, stab, nt, xj, pj, valid, f, en);
+                    valid = vn;
+                    qv = qvn;
+                    xq = xqn;
+                }
+            }
+        }
+        // join the lanes (every lane ends with the same sums) and store the pass's atoms
+#pragma unroll
+        for (int a = 0; a < KIC; a++) {
+            if (a >= ni) break;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                f[a][0] += __shfl_xor_sync(kAll, f[a][0], o);
+                f[a][1] += __shfl_xor_sync(kAll, f[a][1], o);
+                f[a][2] += __shfl_xor_sync(kAll, f[a][2], o);
+            }
+            if (lane == a) store_force(D, force, stride, D.iatom[k0 + a0 + a], f[a][0], f[a][1], f[a][2], s);
+        }
+        if (ENERGY) {
+            double e = en.value();
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(kAll, e, o);
+            e_sum += e;
         }
     }
-    store_force<ENERGY>(D, force, stride, k, D.iatom[k], fx, fy, fz, en, s);
+    if (ENERGY && lane == 0) D.e_group[g] = 0.5 * e_sum;
+}
+
+template <int KIC, bool RELAX>
+void launch_force_pass(const FFDev& D, const int* work, int n_work, bool energy, bool typed, long long* f, int stride,
+                       cudaStream_t st) {
+    const int grid = (n_work + kFW - 1) / kFW;
+    if (typed) {
+        if (energy) ff_force_groups<KIC, true, true, RELAX><<<grid, 32 * kFW, 0, st>>>(D, work, n_work, f, stride);
+        else ff_force_groups<KIC, false, true, RELAX><<<grid, 32 * kFW, 0, st>>>(D, work, n_work, f, stride);
+    } else {
+        if (energy) ff_force_groups<KIC, true, false, RELAX><<<grid, 32 * kFW, 0, st>>>(D, work, n_work, f, stride);
+        else ff_force_groups<KIC, false, false, RELAX><<<grid, 32 * kFW, 0, st>>>(D, work, n_work, f, stride);
+    }
+}
+
+template <int KIC>
+void launch_force_pass(const FFDev& D, const int* work, int n_work, bool energy, bool typed, long long* f, int stride,
+                       cudaStream_t st) {
+    if (D.fcap > 0.0f) launch_force_pass<KIC, true>(D, work, n_work, energy, typed, f, stride, st);
+    else launch_force_pass<KIC, false>(D, work, n_work, energy, typed, f, stride, st);
 }
 
 __global__ void ff_energy(FFDev D) {
     __shared__ double s[256];
     const FFSys S = D.sys[blockIdx.x];
     double e = 0.0;
-    for (int p = S.i0 + threadIdx.x; p < S.i1; p += blockDim.x) e += D.e_atom[p];
+    for (int p = S.g0 + threadIdx.x; p < S.g1; p += blockDim.x) e += D.e_group[p];
     s[threadIdx.x] = e;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -497,16 +642,15 @@ int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* 
     }
     if (cudaMemsetAsync(D.rebuild, 0, (size_t)D.S, st) != cudaSuccess) return -1;
     long long* f = const_cast<long long*>(B.force);
-    const int gf = (D.n_int + 127) / 128;
     const bool typed = D.ntypes > 0 && D.ntypes <= kMaxTypesDev;
-    if (typed) {
-        if (energy) ff_force_groups<true, true><<<gf, 128, 0, st>>>(D, f, B.stride);
-        else ff_force_groups<false, true><<<gf, 128, 0, st>>>(D, f, B.stride);
-    } else {
-        if (energy) ff_force_groups<true, false><<<gf, 128, 0, st>>>(D, f, B.stride);
-        else ff_force_groups<false, false><<<gf, 128, 0, st>>>(D, f, B.stride);
+    if (D.n_small) {
+        launch_force_pass<kSmallGroup>(D, D.small_groups, D.n_small, energy, typed, f, B.stride, st);
+        n++;
     }
-    n++;
+    if (D.n_large) {
+        launch_force_pass<kLargeChunk>(D, D.large_groups, D.n_large, energy, typed, f, B.stride, st);
+        n++;
+    }
     if (energy) {
         ff_energy<<<D.S, 256, 0, st>>>(D);
         n++;

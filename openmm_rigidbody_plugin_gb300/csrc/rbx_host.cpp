@@ -65,6 +65,8 @@ struct rbx_integrator {
     int max_location = 0;  // largest device slot in use; every buffer stride must exceed it
     int ncons = 0;         // constraints between free atoms (each removes one degree of freedom)
     int nb_pad = 0, nba_pad = 0, nf_pad = 0, n_body_tiles = 0, n_free_tiles = 0;
+    int tile_threads = kThreadsF;  // single/mixed step-kernel block size (rbx_set_tile_threads)
+    int max_body_atoms = 0;
     bool have_state = false;
     int last_launches = 0;
     std::vector<double> masses;
@@ -144,6 +146,8 @@ struct rbx_integrator {
         DevSys s;
         s.nb = nb; s.nf = nf; s.nba = nba; s.nb_pad = nb_pad; s.nba_pad = nba_pad; s.nf_pad = nf_pad;
         s.n_body_tiles = n_body_tiles; s.n_free_tiles = n_free_tiles; s.rot_n = mode;
+        s.tile_threads = tile_threads;
+        s.large = max_body_atoms > kWarpBody ? 1 : 0;
         s.state = d_state.p; s.invm = d_invm.p; s.invI = d_invI.p; s.bconst = d_bconst.p;
         s.atom0 = d_atom0.p; s.cls = d_cls.p;
         s.d = d_fixed.p; s.atom_loc = d_atom_loc.p; s.free_loc = d_free_loc.p; s.tile_body0 = d_tiles.p;
@@ -342,7 +346,7 @@ template <class T> int upload(DevArray<T>& a, const std::vector<T>& h) {
 // larger than one tile).
 // Greedy packing of the library order into tiles of at most TB bodies and TA body atoms.
 void pack_tiles(rbx_integrator* h) {
-    const int TA = tile_atoms(h->prec), TB = tile_bodies(h->prec), nb = h->nb;
+    const int TA = tile_atoms(h->prec, h->tile_threads), TB = tile_bodies(h->prec, h->tile_threads), nb = h->nb;
     h->tile_body0.assign(1, 0);
     for (int L = 0; L < nb;) {
         int atoms = 0, cnt = 0;
@@ -357,7 +361,8 @@ void pack_tiles(rbx_integrator* h) {
         h->tile_body0.push_back(L);
     }
     h->n_body_tiles = (int)h->tile_body0.size() - 1;
-    h->n_free_tiles = (h->nf + free_per_tile(h->prec) - 1) / free_per_tile(h->prec);
+    const int fpt = free_per_tile(h->prec, h->tile_threads);
+    h->n_free_tiles = (h->nf + fpt - 1) / fpt;
 }
 
 void plan_order(rbx_integrator* h) {
@@ -722,6 +727,7 @@ int rbx_create(rbx_integrator** out, int num_atoms, const int* body_indices, con
         }
         for (int i : members[b]) h->ref_atoms.push_back(i);
         h->ref_first.push_back((int)h->ref_atoms.size());
+        h->max_body_atoms = std::max(h->max_body_atoms, (int)members[b].size());
     }
     h->nba = (int)h->ref_atoms.size();
     plan_order(h);
@@ -922,6 +928,37 @@ int rbx_get_num_dof(const rbx_integrator* h, int* out) {
     if (rc) return rc;
     if (!h->have_state) return fail(RBX_ERR_STATE, "degrees of freedom are known after rbx_upload_state");
     *out = h->ndof - h->ncons;  // numDOF = free - constraints + body dof (RigidBodySystem.cpp:130)
+    return RBX_OK;
+}
+
+int rbx_set_tile_threads(rbx_integrator* h, int threads) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (threads != kThreadsF && threads != kThreadsFNarrow)
+        return fail(RBX_ERR_INVALID_ARGUMENT, "tile threads must be %d or %d, not %d", kThreadsF, kThreadsFNarrow, threads);
+    if (h->prec == PREC_DOUBLE && threads != kThreadsF)
+        return fail(RBX_ERR_UNSUPPORTED, "double precision has one tile shape (%d threads)", kThreadsF);
+    if (threads == kThreadsFNarrow && h->max_body_atoms > kWarpBody)
+        return fail(RBX_ERR_UNSUPPORTED, "the %d-thread tile takes bodies of at most %d atoms, not %d", threads,
+                    kWarpBody, h->max_body_atoms);
+    if (threads == h->tile_threads) return RBX_OK;
+    CUDA_TRY(cudaSetDevice(h->device));
+    CUDA_TRY(cudaDeviceSynchronize());  // no step in flight reads the old tiles
+    const int old = h->tile_threads;
+    h->tile_threads = threads;
+    pack_tiles(h);
+    if ((rc = upload(h->d_tiles, h->tile_body0))) {
+        h->tile_threads = old;
+        pack_tiles(h);
+        return rc;
+    }
+    return RBX_OK;
+}
+
+int rbx_get_tile_threads(const rbx_integrator* h, int* out) {
+    int rc = check(h);
+    if (rc) return rc;
+    *out = h->prec == PREC_DOUBLE ? kThreads : h->tile_threads;
     return RBX_OK;
 }
 

@@ -43,21 +43,27 @@ enum StepKind : int { STEP_PART1 = 0, STEP_PART2 = 1, STEP_FUSED = 2 };
 constexpr int kThreads = 256;
 constexpr int kTileBodies = 256;
 constexpr int kTileAtomsD = 512;
-// Single/mixed precision: one 256-thread CTA per tile of at most 256 bodies / 1024 body atoms.
+// Single/mixed precision: one CTA of NT threads per tile of at most NT bodies / 4 NT body atoms,
+// 768 threads per SM: NT = 256 (3 CTAs per SM, the default) or 128 (6 per SM, bodies of at most
+// kWarpBody atoms), chosen per integrator (rbx_set_tile_threads). Results do not depend on it.
 constexpr int kThreadsF = 256;
-constexpr int kTileBodiesF = 256;
-constexpr int kTileAtomsF = 1024;
+constexpr int kThreadsFNarrow = 128;
+constexpr int kTileAtomsF = 4 * kThreadsF;
+constexpr int kWarpBody = 32;       // bodies of more atoms are summed by a whole warp
 constexpr int kBconstRows = 11;     // rows of the FP32 body-constant table (single/mixed)
 constexpr int kRefBodyRows = 10;    // rows of ref_start per body
 
-inline int tile_atoms(int prec) { return prec == PREC_DOUBLE ? kTileAtomsD : kTileAtomsF; }
-inline int tile_bodies(int prec) { return prec == PREC_DOUBLE ? kTileBodies : kTileBodiesF; }
-// Free atoms per free-atom tile: one per thread of the precision's step kernel.
-inline int free_per_tile(int prec) { return prec == PREC_DOUBLE ? kThreads : kThreadsF; }
+// Tile limits of a precision at a step-kernel block size (nt: single/mixed only).
+inline int tile_atoms(int prec, int nt = kThreadsF) { return prec == PREC_DOUBLE ? kTileAtomsD : 4 * nt; }
+inline int tile_bodies(int prec, int nt = kThreadsF) { return prec == PREC_DOUBLE ? kTileBodies : nt; }
+// Free atoms per free-atom tile: one per thread of the step kernel.
+inline int free_per_tile(int prec, int nt = kThreadsF) { return prec == PREC_DOUBLE ? kThreads : nt; }
 
 struct DevSys {
     int nb, nf, nba, nb_pad, nba_pad, nf_pad;
     int n_body_tiles, n_free_tiles;
+    int tile_threads;  // single/mixed: the step kernel's block size (kThreadsF or kThreadsFNarrow)
+    int large;         // 1: a body has more than kWarpBody atoms (the step kernels' LARGE form)
     int rot_n;  // NO-SQUISH substeps; 0 = exact rotation
     void* state;           // double* (double precision) or float* (float-float, single/mixed)
     const double* invm;    // double precision only
@@ -100,6 +106,8 @@ struct FFSys {
     float L, invL, rc2, krf, crf;
     float rl;          // cutoff + skin: groups are listed when their centroids lie within rl + both radii
     float half_skin2;  // (skin/2)^2: a centroid moved this far since the build invalidates the lists
+    int pair_image;    // 1: cutoff + two radii may reach half the box; the force pass takes the
+                       // minimum image per pair (else one shift per listed group)
 };
 struct FFDev {
     int S, n_int, n_groups, n_cells;
@@ -120,19 +128,20 @@ struct FFDev {
     int* cell_cursor;     // [n_cells]
     int* cell_list;       // [n_groups] group indices in cell order (of the last list build)
     float4* cpos;         // [n_int] x, y, z (wrapped into the box), sqrt(K) q (or the atom's type)
-    double* e_atom;       // [n_int] half pair-energy sums (energy evaluations)
+    double* e_group;      // [n_groups] half pair-energy sums of each group (energy evaluations)
     // Neighbour lists of groups, rebuilt per system when one of its centroids has moved more than
     // half the skin since the last build, and at the first evaluation of every call
     unsigned char* rebuild;  // [S] 1: rebuild this system's lists before the next force pass
     unsigned int* rebuilds;  // [S] list builds of each system so far (a statistic)
-    unsigned int* nbr;       // entries (first atom - i0) << 11 | atoms, in groups of 32 groups:
-                             // entry e of group g at (g/32)*32*cap + e*32 + g%32
+    unsigned int* nbr;       // entries: listed group - g0 of the system; entry e of group g at
+                             // g*cap + e
     int* ncnt;               // [n_groups] entries per group
     int cap;                 // entries per group allocated
     // Atom types (ntypes > 0): the distinct (sqrt(K) q, sigma/2, sqrt(epsilon)) of the interacting
     // atoms; cpos .w then holds the atom's type (int bits) instead of its charge, so that the force
-    // pass reads one 16-byte record per neighbour
-    const float4* types;     // [ntypes]
+    // pass reads one 16-byte record per neighbour, and takes each pair's (K q_i q_j, C12, C6) from
+    // a table of type pairs
+    const float4* types;     // [ntypes * ntypes] the type-pair table
     const int* atype;        // [n_int] type of each interacting atom
     int ntypes;
     double* energy;       // [S] potential energy per system (kJ/mol)
@@ -148,11 +157,13 @@ struct FFDev {
     const int* mc_sys;
     const int* sc_sys;
     const int* sc_g0;
+    // groups of the force pass (set at creation): at most 4 interacting atoms, and the others
+    int n_small, n_large;
+    const int* small_groups;
+    const int* large_groups;
 };
-// Largest first-atom offset and group size a packed list entry holds.
-constexpr int kGroupAtomBits = 11;
-constexpr int kMaxGroupAtoms = (1 << kGroupAtomBits) - 1;
-constexpr int kMaxSystemAtoms = 1 << (32 - kGroupAtomBits);
+// Interacting atoms of one system: the force pass streams (atom << 5 | lane) words.
+constexpr int kMaxSystemAtoms = 1 << 26;
 int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* stream);
 // Fixed-point forces of slots [0, natoms) -> user-order doubles out[3*natoms] (kJ/mol/nm).
 int launch_forces_to_user(const long long* force, int stride, int natoms, double* out, void* stream);
@@ -188,7 +199,6 @@ int launch_load_positions(int prec, const double* x_dev_user, const double* v_de
 int launch_store_positions(int prec, const DevBuf& b, const int* location, int natoms, double* x_dev_user,
                            double* v_dev_user, void* stream);
 int kinetic_blocks(const DevSys& s);
-size_t step_smem_bytes(int prec);
 
 // Record an error message for rbx_last_error() and return `code` (defined in rbx_host.cpp).
 int set_error(int code, const char* fmt, ...);

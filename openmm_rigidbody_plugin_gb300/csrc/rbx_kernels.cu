@@ -309,7 +309,6 @@ __global__ void store_positions_kernel(DevBuf B, const int* __restrict__ loc, in
 // ------------------------------------------------------------------------------------------
 // Launchers
 // ------------------------------------------------------------------------------------------
-size_t step_smem_bytes(int prec) { return prec == PREC_DOUBLE ? step_smem_d() : step_smem_f(); }
 
 int launch_sync_positions(int prec, const DevSys& s, const DevBuf& b, void* stream) {
     if (s.nb == 0) return 0;

@@ -14,7 +14,8 @@
 //      (single/mixed: phase 1's loads are issued before phase 0, so that the slot -> force
 //      dependency overlaps it: 4 % faster)
 //   2. one thread per body sums its atoms' F and tau in a fixed order (deterministic, no
-//      atomics), applies the half kick(s), drift and free rotation, and writes its state;
+//      atomics; a whole warp per body for bodies of more than 32 atoms), applies the half
+//      kick(s), drift and free rotation, and writes its state;
 //   3. one thread per atom writes the new position r + At(q) d (or, for part2, the velocity
 //      v + omega x delta) to its device slot.
 // Free atoms live in separate tiles of the same launch (velocity Verlet), interleaved with the
@@ -152,11 +153,11 @@ static __device__ __noinline__ void flag_failure(unsigned int* status, uint8_t* 
 }
 
 // Shared memory of the double-precision step kernel: sF, sT, sX 3*TA each; sQ 4*TB; sRb 3*TB
-// (double); sW 3*TB; sBody TA (uint16).
+// (double); sW 3*TB; sBody TA (uint16); sBig one word per warp.
 constexpr size_t step_smem_d() {
     constexpr int TA = kTileAtomsD, TB = kTileBodies;
     return (size_t)3 * 3 * TA * sizeof(double) + 4 * TB * sizeof(double) + 3 * TB * sizeof(double) +
-           3 * TB * sizeof(double) + TA * sizeof(unsigned short) + 64;
+           3 * TB * sizeof(double) + TA * sizeof(unsigned short) + (kThreads / 32) * sizeof(unsigned) + 64;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -324,6 +325,7 @@ template <class A> struct StepSmem {
     A *sF, *sT, *sX, *sQ, *sW;
     double* sRb;
     unsigned short* sBody;
+    unsigned* sBig;  // large-body ballots, one word per warp
     template <int TA, int TB> __device__ __forceinline__ void carve(unsigned char* smem) {
         sF = (A*)smem;
         sT = sF + 3 * TA;
@@ -332,6 +334,7 @@ template <class A> struct StepSmem {
         sRb = (double*)(sQ + 4 * TB);
         sW = (A*)(sRb + 3 * TB);
         sBody = (unsigned short*)(sW + 3 * TB);
+        sBig = (unsigned*)(sBody + TA);
     }
 };
 
@@ -385,6 +388,61 @@ __device__ __forceinline__ void body_sums(const StepSmem<A>& sm, int s, int e, V
     }
 }
 
+// Bodies of more than a warp's atoms are summed by a whole warp instead of one thread: lane l adds
+// the atoms s+l, s+l+32, ... in order and a fixed butterfly of shuffles joins the lanes, so a
+// 1024-atom body costs 32 dependent additions instead of 1024 (the plugin sums serially,
+// rigidbodyintegrator.cu:367-373). Phase 0 records the tile's large bodies as one ballot per warp
+// (masks[w], bit l: tile body 32w + l); they are dealt round-robin to the warps in that order.
+// The sums are a function of the body's atoms alone, not of the tile or the warp that forms them.
+// This path is compiled into separate kernels (LARGE), launched only for integrators that have such
+// bodies (DevSys::large), so that the common case carries none of it.
+
+// The sums of tile body t go to outF[os t + c] and outT[os t + c], c = 0, 1, 2 (out of line: the
+// branch is rare and stays out of the callers' register allocation).
+template <int NW, class A>
+__device__ __noinline__ void warp_body_sums(const unsigned* masks, const int* __restrict__ atom0, int b0, int a0,
+                                            const A* sF, const A* sT, A* outF, A* outT, int os) {
+    const int warp = (int)threadIdx.x >> 5, lane = (int)threadIdx.x & 31;
+    int k = 0;
+    for (int m = 0; m < NW; m++) {
+        unsigned bits = masks[m];
+        while (bits) {
+            const int t = 32 * m + __ffs(bits) - 1;
+            bits &= bits - 1;
+            if (k++ % NW != warp) continue;
+            const int s = __ldg(atom0 + b0 + t) - a0, e = __ldg(atom0 + b0 + t + 1) - a0;
+            A f[6] = {A(0), A(0), A(0), A(0), A(0), A(0)};
+            for (int j = s + lane; j < e; j += 32) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    f[c] += sF[3 * j + c];
+                    f[3 + c] += sT[3 * j + c];
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+                for (int c = 0; c < 6; c++) f[c] += __shfl_xor_sync(0xffffffffu, f[c], o);
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    outF[os * t + c] = f[c];
+                    outT[os * t + c] = f[3 + c];
+                }
+            }
+        }
+    }
+}
+
+// Number of large bodies in the tile (block-uniform).
+template <int NW> __device__ __forceinline__ int count_large(const unsigned* masks) {
+    int n = 0;
+#pragma unroll
+    for (int m = 0; m < NW; m++) n += __popc(masks[m]);
+    return n;
+}
+
 // Phase 3, part2: atom velocities v + omega_space x delta.
 template <int P, class A>
 __device__ __forceinline__ void atom_velocities(const DevSys& S, const DevBuf& B, const StepSmem<A>& sm, int a0, int nat) {
@@ -420,8 +478,10 @@ __device__ __forceinline__ void rotate_d(const DevSys& S, int b, V3<double> invI
     }
 }
 
-template <int KIND, bool EXACT, bool REF>
-__global__ void __launch_bounds__(kThreads) step_kernel_d(DevSys S, DevBuf B, double dt) {
+// Residency per SM: 3 CTAs for NO-SQUISH (80 registers; shared memory allows 3), 2 for the exact
+// rotation (128), 1 with the refined-energy stencils.
+template <int KIND, bool EXACT, bool REF, bool LARGE>
+__global__ void __launch_bounds__(kThreads, REF ? 1 : EXACT ? 2 : 3) step_kernel_d(DevSys S, DevBuf B, double dt) {
     constexpr int P = PREC_DOUBLE;
     constexpr int TA = kTileAtomsD, TB = kTileBodies;
     const int tile = block_tile(S);
@@ -439,19 +499,36 @@ __global__ void __launch_bounds__(kThreads) step_kernel_d(DevSys S, DevBuf B, do
     const int nbp = S.nb_pad;
     double* __restrict__ st = (double*)S.state;
 
+    bool big = false;
     if (tid < nbt) {
         const int b = b0 + tid;
         for (int c = 0; c < 4; c++) sm.sQ[4 * tid + c] = st[b + (6 + c) * nbp];
         const int s = __ldg(S.atom0 + b) - a0, e = __ldg(S.atom0 + b + 1) - a0;
         for (int j = s; j < e; j++) sm.sBody[j] = (unsigned short)tid;
+        big = e - s > kWarpBody;
+    }
+    if (LARGE) {
+        const unsigned m = __ballot_sync(0xffffffffu, big);
+        if ((tid & 31) == 0) sm.sBig[tid >> 5] = m;
     }
     __syncthreads();
     atom_forces<P, KIND, double, double>(S, B, sm, a0, nat);
     __syncthreads();
+    if (LARGE && count_large<kThreads / 32>(sm.sBig)) {
+        // large bodies' sums parked in sRb (force) and sW (torque) of their tile body
+        warp_body_sums<kThreads / 32>(sm.sBig, S.atom0, b0, a0, sm.sF, sm.sT, sm.sRb, sm.sW, 3);
+        __syncthreads();
+    }
     if (tid < nbt) {
         const int b = b0 + tid;
         V3<double> Fa, Ta;
-        body_sums(sm, __ldg(S.atom0 + b) - a0, __ldg(S.atom0 + b + 1) - a0, Fa, Ta);
+        const int s = __ldg(S.atom0 + b) - a0, e = __ldg(S.atom0 + b + 1) - a0;
+        if (LARGE && e - s > kWarpBody) {
+            Fa = v3<double>(sm.sRb[3 * tid], sm.sRb[3 * tid + 1], sm.sRb[3 * tid + 2]);
+            Ta = v3<double>(sm.sW[3 * tid], sm.sW[3 * tid + 1], sm.sW[3 * tid + 2]);
+        } else {
+            body_sums(sm, s, e, Fa, Ta);
+        }
         V3<double> r = v3<double>(st[b], st[b + nbp], st[b + 2 * nbp]);
         V3<double> v = v3<double>(st[b + 3 * nbp], st[b + 4 * nbp], st[b + 5 * nbp]);
         Q4<double> q = q4<double>(st[b + 6 * nbp], st[b + 7 * nbp], st[b + 8 * nbp], st[b + 9 * nbp]);
@@ -535,19 +612,20 @@ __global__ void __launch_bounds__(kThreads) step_kernel_d(DevSys S, DevBuf B, do
 
 // ------------------------------------------------------------------------------------------
 // Single and mixed precision: FP32 arithmetic, float-float body state, rotation increments.
-// One 256-thread CTA per tile (<= 256 bodies, <= 1024 body atoms), 3 CTAs per SM. Each body's
-// rotation matrix is formed once per phase and kept in shared memory, so the per-atom rebuild
-// delta = At(q) d costs 9 FMAs.
+// One CTA of NT threads per tile (<= NT bodies, <= 4 NT body atoms), 768 threads per SM. Each
+// body's rotation matrix is formed once per phase and kept in shared memory, so the per-atom
+// rebuild delta = At(q) d costs 9 FMAs.
 // ------------------------------------------------------------------------------------------
-struct FSmem {
-    static constexpr int TA = kTileAtomsF, TB = kTileBodiesF;
+template <int NT> struct FSmem {
+    static constexpr int TA = 4 * NT, TB = NT;
     static constexpr int SF = 0;              // 3 x TA: F
     static constexpr int ST = SF + 3 * TA;    // 3 x TA: torque
     static constexpr int SM = ST + 3 * TA;    // 9 x TB: rotation matrix At(q), row-major per body
     static constexpr int SR = SM + 9 * TB;    // 6 x TB: COM (hi, lo) or COM velocity (double)
     static constexpr int SW = SR + 6 * TB;    // 3 x TB: space-frame omega (part2)
     static constexpr int SB = SW + 3 * TB;    // TA ushort: atom -> tile body
-    static constexpr int WORDS = SB + TA / 2;
+    static constexpr int SG = SB + TA / 2;    // one word per warp: large-body ballots
+    static constexpr int WORDS = SG + NT / 32;
 };
 
 // At(q) as a row-major 3x3 matrix (homogeneous quadratic form, equal to Ct(q, B(q, .))).
@@ -570,10 +648,10 @@ __device__ __forceinline__ Q4<float> rotation_increment(const DevSys& S, int b, 
     return nosquish_increment(L, R, R.invI.z != 0.0f, dt, S.rot_n);
 }
 
-template <int P, int KIND, bool EXACT, bool REF>
-__global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B, double dt_d) {
-    constexpr int TA = kTileAtomsF;
-    constexpr int APT = TA / kThreadsF;
+template <int P, int KIND, bool EXACT, bool REF, int NT, bool LARGE>
+__global__ void __launch_bounds__(NT, 768 / NT) step_kernel_f(DevSys S, DevBuf B, double dt_d) {
+    using FSmem = rbx::FSmem<NT>;
+    constexpr int APT = 4;  // body atoms per thread in phase 1
     const int tile = block_tile(S);
     if (tile < 0) {
         free_atom_tile<P, KIND, REF>(S, B, dt_d, -1 - tile);
@@ -586,6 +664,7 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
     float* sR = fsm + FSmem::SR;
     float* sW = fsm + FSmem::SW;
     unsigned short* sBody = (unsigned short*)(fsm + FSmem::SB);
+    unsigned* sBig = (unsigned*)(fsm + FSmem::SG);
     const int tid = threadIdx.x;
     const int b0 = __ldg(S.tile_body0 + tile), b1 = __ldg(S.tile_body0 + tile + 1);
     const int nbt = b1 - b0;
@@ -603,12 +682,12 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
         V3<float> F[APT], d[APT];
 #pragma unroll
         for (int i = 0; i < APT; i++) {
-            const int a = tid + i * kThreadsF;
+            const int a = tid + i * NT;
             loc[i] = a < nat ? __ldg(S.atom_loc + a0 + a) : 0;
         }
 #pragma unroll
         for (int i = 0; i < APT; i++) {
-            const int a = tid + i * kThreadsF;
+            const int a = tid + i * NT;
             if (a < nat) {
                 const int k = a0 + a;
                 d[i] = v3<float>(__ldg(dg + k), __ldg(dg + k + S.nba_pad), __ldg(dg + k + 2 * S.nba_pad));
@@ -624,18 +703,23 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
         }
 #pragma unroll
         for (int i = 0; i < APT; i++) {
-            const int a = tid + i * kThreadsF;
+            const int a = tid + i * NT;
             if (a < nat) F[i] = load_force<float>(B.force, loc[i], B.stride);
         }
-        // Phase 0: rotation matrix of the current orientation; atoms -> tile-local body
+        // Phase 0: rotation matrix of the current orientation; atoms -> tile-local body; the
+        // tile's large bodies
         if (tid < nbt) {
             rotation_matrix(q0, sM + 9 * tid);
             for (int j = s0; j < e0; j++) sBody[j] = (unsigned short)tid;
         }
+        if (LARGE) {
+            const unsigned m = __ballot_sync(0xffffffffu, e0 - s0 > kWarpBody);
+            if ((tid & 31) == 0) sBig[tid >> 5] = m;
+        }
         __syncthreads();
 #pragma unroll
         for (int i = 0; i < APT; i++) {
-            const int a = tid + i * kThreadsF;
+            const int a = tid + i * NT;
             if (a < nat) {
                 const V3<float> delta = mat_vec(sM + 9 * sBody[a], d[i]);
                 const V3<float> tau = cross(delta, F[i]);
@@ -645,6 +729,11 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
         }
     }
     __syncthreads();
+    if (LARGE && count_large<NT / 32>(sBig)) {
+        // large bodies' sums parked in sR (6 words of their tile body; phase 2 reads, then reuses them)
+        warp_body_sums<NT / 32>(sBig, S.atom0, b0, a0, sF, sT, sR, sR + 3, 6);
+        __syncthreads();
+    }
 
     // Phase 2: kicks, drift and rotation on the float-float state
     if (tid < nbt) {
@@ -663,9 +752,14 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
         V3<float> Fa = v3<float>(0.f, 0.f, 0.f), Ta = Fa;
         {
             const int s0 = __ldg(S.atom0 + b) - a0, e0 = __ldg(S.atom0 + b + 1) - a0;
-            for (int j = s0; j < e0; j++) {
-                Fa = Fa + v3<float>(sF[3 * j], sF[3 * j + 1], sF[3 * j + 2]);
-                Ta = Ta + v3<float>(sT[3 * j], sT[3 * j + 1], sT[3 * j + 2]);
+            if (LARGE && e0 - s0 > kWarpBody) {
+                Fa = v3<float>(sR[6 * tid], sR[6 * tid + 1], sR[6 * tid + 2]);
+                Ta = v3<float>(sR[6 * tid + 3], sR[6 * tid + 4], sR[6 * tid + 5]);
+            } else {
+                for (int j = s0; j < e0; j++) {
+                    Fa = Fa + v3<float>(sF[3 * j], sF[3 * j + 1], sF[3 * j + 2]);
+                    Ta = Ta + v3<float>(sT[3 * j], sT[3 * j + 1], sT[3 * j + 2]);
+                }
             }
         }
         const Q4<float> qh = q4<float>(x[6].hi, x[7].hi, x[8].hi, x[9].hi);
@@ -787,7 +881,7 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
     // Phase 3: positions (part1, fused) or velocities (part2); d is read again (an L2 hit after
     // phase 1) and, for part2, delta rebuilt from the unchanged orientation
     const float* __restrict__ dg3 = (const float*)S.d;
-    for (int a = tid; a < nat; a += kThreadsF) {
+    for (int a = tid; a < nat; a += NT) {
         const int t = sBody[a];
         const int loc = __ldg(S.atom_loc + a0 + a);
         const int k = a0 + a;
@@ -825,20 +919,25 @@ __global__ void __launch_bounds__(kThreadsF, 3) step_kernel_f(DevSys S, DevBuf B
 // ------------------------------------------------------------------------------------------
 // Launch: one CTA per tile (body tiles, then free-atom tiles).
 // ------------------------------------------------------------------------------------------
-constexpr size_t step_smem_f() { return (size_t)FSmem::WORDS * 4; }
+template <int NT> constexpr size_t step_smem_f() { return (size_t)FSmem<NT>::WORDS * 4; }
 
-template <int P, int KIND, bool EXACT, bool REF> struct StepKernel {
-    static constexpr auto fn() { return step_kernel_f<P, KIND, EXACT, REF>; }
+template <int P, int KIND, bool EXACT, bool REF, int NT, bool LARGE> struct StepKernel {
+    static constexpr auto fn() { return step_kernel_f<P, KIND, EXACT, REF, NT, LARGE>; }
+    static constexpr size_t smem() { return step_smem_f<NT>(); }
+    static constexpr int threads() { return NT; }
 };
-template <int KIND, bool EXACT, bool REF> struct StepKernel<PREC_DOUBLE, KIND, EXACT, REF> {
-    static constexpr auto fn() { return step_kernel_d<KIND, EXACT, REF>; }
+template <int KIND, bool EXACT, bool REF, int NT, bool LARGE> struct StepKernel<PREC_DOUBLE, KIND, EXACT, REF, NT, LARGE> {
+    static constexpr auto fn() { return step_kernel_d<KIND, EXACT, REF, LARGE>; }
+    static constexpr size_t smem() { return step_smem_d(); }
+    static constexpr int threads() { return kThreads; }
 };
 
-template <int P, int KIND, bool EXACT, bool REF>
-int launch_step_t(const DevSys& s, const DevBuf& b, double dt, cudaStream_t stream) {
-    const size_t smem = P == PREC_DOUBLE ? step_smem_d() : step_smem_f();
-    const int threads = P == PREC_DOUBLE ? kThreads : kThreadsF;
-    auto kernel = StepKernel<P, KIND, EXACT, REF>::fn();
+template <int P, int KIND, bool EXACT, bool REF, int NT, bool LARGE>
+int launch_step_nt(const DevSys& s, const DevBuf& b, double dt, cudaStream_t stream) {
+    using K = StepKernel<P, KIND, EXACT, REF, NT, LARGE>;
+    const size_t smem = K::smem();
+    const int threads = K::threads();
+    auto kernel = K::fn();
     if (smem > 48 * 1024) {
         // The opt-in above 48 KB of dynamic shared memory is a per-device attribute: remember the
         // devices that have it (one bit each; devices past 63 set it on every launch).
@@ -856,6 +955,17 @@ int launch_step_t(const DevSys& s, const DevBuf& b, double dt, cudaStream_t stre
     if (tiles == 0) return 0;
     kernel<<<tiles, threads, smem, stream>>>(s, b, dt);
     return cudaPeekAtLastError() == cudaSuccess ? 1 : -1;
+}
+
+// The kernel for the integrator's bodies (any of more than kWarpBody atoms: the LARGE form) and,
+// in single/mixed precision, the block size its tiles were packed for (narrow tiles only without
+// large bodies).
+template <int P, int KIND, bool EXACT, bool REF>
+int launch_step_t(const DevSys& s, const DevBuf& b, double dt, cudaStream_t stream) {
+    if (s.large) return launch_step_nt<P, KIND, EXACT, REF, kThreadsF, true>(s, b, dt, stream);
+    if (P != PREC_DOUBLE && s.tile_threads == kThreadsFNarrow)
+        return launch_step_nt<P, KIND, EXACT, REF, kThreadsFNarrow, false>(s, b, dt, stream);
+    return launch_step_nt<P, KIND, EXACT, REF, kThreadsF, false>(s, b, dt, stream);
 }
 
 // part2 rotates nothing unless it closes the refined-energy stencils (a virtual rotation).

@@ -183,6 +183,16 @@ class IntegratorKernel:
     def rotation_mode(self):
         return self._get_int(self._lib.rbx_get_rotation_mode)
 
+    @property
+    def tile_threads(self):
+        """Block size of the step kernel's tiles (256, or 128 in single/mixed precision when every
+        body has at most 32 atoms); results do not depend on it (rbx_set_tile_threads)."""
+        return self._get_int(self._lib.rbx_get_tile_threads)
+
+    @tile_threads.setter
+    def tile_threads(self, threads):
+        _lib.check(self._lib.rbx_set_tile_threads(self._h, int(threads)))
+
     # device steps -------------------------------------------------------------------------
     def part1(self, buffers, dt, stream=None):
         b = buffers.struct()

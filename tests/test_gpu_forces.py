@@ -146,12 +146,13 @@ def test_water_full_steps_track_the_fp64_oracle(B, oracle_mod):
 
 
 def test_autotune_changes_no_result(B):
-    """The autotuner times schedules on the batch and restores its state exactly; every block size
-    of the cell kernel and every graph run length gives the same trajectory bit for bit."""
+    """The autotuner times schedules on the batch and restores its state exactly; every tile shape of
+    the step kernel, block size of the cell kernel and graph run length gives the same trajectory
+    bit for bit."""
     from openmm_rigidbody_plugin_gb300 import workloads as W
     systems = W.batch_systems(6, lo=300, hi=2500, seed=14)
     runs = []
-    for how in ("plain", "autotuned", 64, 256):
+    for how in ("plain", "autotuned", 64, 256, "narrow tiles"):
         b = B.BatchedSystems.from_systems(systems, relax_steps=50)
         x0, v0 = b.get_state()
         b.set_state(x0, v0)
@@ -159,6 +160,11 @@ def test_autotune_changes_no_result(B):
         if how == "autotuned":
             choice = b.autotune(0.002, trial_steps=2)
             assert choice["cell_threads"] in (64, 128, 256) and choice["graph_steps"] in (0, 10, 50)
+            assert choice["tile_threads"] in (128, 256)
+        elif how == "narrow tiles":
+            assert b.tile_threads == 256
+            b.tile_threads = 128
+            assert b.tile_threads == 128
         elif how != "plain":
             b.set_tuning(how, 10)
         b.step(25, 0.002)

@@ -220,6 +220,53 @@ def test_largest_body_vs_robust_oracle(rbx, oracle_mod, prec, size):
     assert rel_err(buf.get_velocities(), o.V) < 10 * tol
 
 
+def _blobs(sizes, seed):
+    """Rigid bodies of the given atom counts (random clouds, 0.3 nm spread), one per id from 1."""
+    rng = np.random.default_rng(seed)
+    R = np.concatenate([rng.normal(0, 0.3, (n, 3)) + rng.uniform(0, 6, 3) for n in sizes])
+    bidx = np.concatenate([np.full(n, i + 1) for i, n in enumerate(sizes)])
+    return R, bidx, rng.uniform(1, 16, len(bidx)), rng.normal(0, 0.3, R.shape)
+
+
+@pytest.mark.parametrize("prec", ["double", "mixed"])
+@pytest.mark.parametrize("mode", [0, 10])
+def test_many_large_bodies_per_tile(rbx, oracle_mod, prec, mode):
+    """Bodies of more than 32 atoms are summed by a warp each. Twelve of 33-40 atoms share one tile
+    (more large bodies than warps, so a warp takes several), among 27 waters: 20 steps against the
+    robust oracle under sd 50 forces; then the same bodies without the waters (other tiles, other
+    warps): their trajectories are bit-identical."""
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    sizes = [33, 40, 34, 39, 35, 38, 36, 37, 33, 40, 34, 39]
+    Rb, bb, mb, Vb = _blobs(sizes, seed=41)
+    w = W.water_box(27, seed=5)
+    R = np.concatenate([w.positions, Rb])
+    bidx = np.concatenate([w.body_indices, bb + w.body_indices.max()])
+    masses = np.concatenate([w.masses, mb])
+    V = np.concatenate([w.velocities, Vb])
+    F = np.round(W.gaussian_forces(len(masses), seed=9, sd=50.0) * 2.0 ** 32) / 2.0 ** 32
+    k, buf = make(rbx, masses, bidx, R, V, mode, prec)
+    buf.set_forces(F)
+    o = oracle_mod.Oracle(masses, bidx, mode=mode, robust=True)
+    o.setup(R, V, F)
+    for _ in range(20):
+        k.part1(buf, 0.002)
+        k.part2(buf, 0.002)
+        o.part1(0.002, F)
+        o.part2(0.002, F)
+    tol = {"double": 1e-9, "mixed": 1e-6}[prec]
+    x, v = buf.get_positions(), buf.get_velocities()
+    assert rel_err(x, o.R) < tol
+    assert rel_err(v, o.V) < 10 * tol
+    n = len(w.masses)
+    k2, buf2 = make(rbx, mb, bb, Rb, Vb, mode, prec)
+    buf2.set_forces(F[n:])
+    for _ in range(20):
+        k2.part1(buf2, 0.002)
+        k2.part2(buf2, 0.002)
+    assert np.array_equal(buf2.get_positions(), x[n:])
+    assert np.array_equal(buf2.get_velocities(), v[n:])
+
+
 @pytest.mark.parametrize("prec", ["double", "mixed"])
 @pytest.mark.parametrize("mode", [0, 10])
 def test_mixed_body_types_vs_robust_oracle(rbx, oracle_mod, mode, prec):
@@ -354,6 +401,50 @@ def test_host_buffer_step(rbx, golden, prec):
     assert rel_err(R, g["R"][-1]) < tol
     assert rel_err(V, g["V"][-1]) < tol * 10
     np.testing.assert_allclose(k.context_kinetic_energies(), g["ke"][-1], rtol=tol * 10)
+
+
+@pytest.mark.parametrize("prec", ["single", "mixed"])
+@pytest.mark.parametrize("mode", [0, 10])
+def test_tile_shapes_give_identical_results(rbx, prec, mode):
+    """The step kernel's two tile shapes (256 threads / 1024 body atoms and 128 / 512) integrate
+    every body alike: 600 bodies of three kinds, a 32-atom body and 40 free atoms, 20 split and 10
+    fused steps, with the shape switched mid-run in one of the runs. Bodies of more than 32 atoms
+    (summed by a warp), and double precision, have the wide shape only."""
+    from openmm_rigidbody_plugin_gb300 import _lib, workloads as W
+    s = W.mixed_system(n_bodies=600, n_free=40, fractions=(0.5, 0.3, 0.2), seed=8)
+    Rb, bb, mb, Vb = _blobs([32], seed=2)
+    R = np.concatenate([s.positions, Rb])
+    bidx = np.concatenate([s.body_indices, bb + s.body_indices.max()])
+    masses = np.concatenate([s.masses, mb])
+    V = np.concatenate([s.velocities, Vb])
+    F = np.round(W.gaussian_forces(len(masses), seed=4, sd=50.0) * 2.0 ** 32) / 2.0 ** 32
+    outs = []
+    for shape in ((256, 256), (128, 128), (256, 128)):
+        k, buf = make(rbx, masses, bidx, R, V, mode, prec)
+        assert k.tile_threads == 256
+        k.tile_threads = shape[0]
+        buf.set_forces(F)
+        for n in range(20):
+            if n == 10:
+                k.tile_threads = shape[1]
+            k.part1(buf, 0.002)
+            k.part2(buf, 0.002)
+        k.part1(buf, 0.002)
+        for _ in range(10):
+            k.fused(buf, 0.002)
+        k.part2(buf, 0.002)
+        assert k.tile_threads == shape[1]
+        outs.append((buf.get_positions(), buf.get_velocities(), k.kinetic_energies(buf)))
+    for out in outs[1:]:
+        for a, b in zip(outs[0], out):
+            assert np.array_equal(a, b)
+    big = np.concatenate([bidx, np.full(33, bidx.max() + 1)])
+    k = rbx.IntegratorKernel(np.concatenate([masses, np.ones(33)]), big, rotation_mode=mode, precision=prec)
+    with pytest.raises(_lib.RbxError, match="bodies of at most 32 atoms"):
+        k.tile_threads = 128
+    k = rbx.IntegratorKernel(masses, bidx, rotation_mode=mode, precision="double")
+    with pytest.raises(_lib.RbxError, match="one tile shape"):
+        k.tile_threads = 128
 
 
 def test_determinism(rbx, golden):
