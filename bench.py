@@ -706,6 +706,8 @@ def run_batched(args, world, rank, local):
         launches = b.last_launch_count
         builds = (b.list_builds() - builds0).astype(np.int64)
         e_post = b.energies()
+        plain_idx = np.unique(np.linspace(0, len(systems) - 1, min(args.plain_systems, len(systems))).astype(int))
+        final_b = [b.get_system_state(int(k)) for k in plain_idx] if args.plain_systems > 0 else []
         # the clocks are sampled over the timed steps and over repeats of them until the window
         # lasts at least 1.5 s, so that a short timed region still has its own clock record
         repeats = 0
@@ -756,7 +758,7 @@ def run_batched(args, world, rank, local):
     # the same systems, one system per launch (the plain drop-in way: one context per system)
     plain = None
     if args.workload == "batched" and args.plain_systems > 0:
-        idx = np.unique(np.linspace(0, len(systems) - 1, min(args.plain_systems, len(systems))).astype(int))
+        idx = plain_idx
         off = b.offsets
         handles = []
         plain_steps = args.plain_steps or args.steps
@@ -785,6 +787,12 @@ def run_batched(args, world, rank, local):
         if plain_steps == args.steps:  # the same systems inside the batch, over the same steps
             plain["batched_energy_drift_same_systems"] = _drift(e_pre[idx], e_post[idx], args.steps, dt, dof[idx])
             plain["same_final_energies_as_batched"] = bool(np.array_equal(e_post_p, e_post[idx]))
+            plain["final_energies_max_abs_diff"] = [float(v) for v in np.abs(e_post_p - e_post[idx]).max(axis=0)]
+            same_state = [bool(np.array_equal(h.get_state()[0], xb) and np.array_equal(h.get_state()[1], vb))
+                          for h, (xb, vb) in zip(handles, final_b)]
+            plain["same_final_state_as_batched"] = f"{sum(same_state)} of {len(same_state)} systems"
+            plain["status_nonzero"] = {"batched": int(np.count_nonzero(b.status())),
+                                       "plain": int(sum(int(np.count_nonzero(h.status())) for h in handles))}
         del handles
     single = None
     if args.workload == "batched" and not args.no_single:

@@ -235,6 +235,13 @@ int rbx_potential_energy_refinement(rbx_integrator* h, void* stream, const rbx_b
  */
 int rbx_get_body_state(rbx_integrator* h, double* state);
 int rbx_set_body_state(rbx_integrator* h, const double* state);
+/* The body state's exact device words, for checkpoints: 112 bytes per body in every precision, in
+ * the same body order: 14 doubles (double precision), or the 14 high then the 14 low floats of the
+ * float-float state (single, mixed). A float-float pair summed into one double loses the low word's
+ * last bits when it is below 2^-29 of the high word, so the double rows of rbx_get_body_state do
+ * not restore such a state bit for bit; these rows do. */
+int rbx_get_body_state_raw(rbx_integrator* h, void* rows);
+int rbx_set_body_state_raw(rbx_integrator* h, const void* rows);
 int rbx_get_body_geometry(rbx_integrator* h, double* moments, double* body_fixed /* [nba*3] */);
 int rbx_get_body_atoms(rbx_integrator* h, int* first_atom /* [nb+1] */, int* atoms /* [nba] */);
 
@@ -256,8 +263,8 @@ int rbx_context_get_state(rbx_integrator* h, void* stream, double* positions, do
  * the Context's positions on every state change, RigidBodyIntegrator.cpp:63-74):
  * rbx_context_load writes host positions and velocities into the owned buffers as they are, without
  * rebuilding the body state; rbx_context_sync_bodies rewrites the body atoms' positions from the
- * current body state with the step kernels' own arithmetic. With rbx_set_body_state in between,
- * a state saved by rbx_get_body_state + rbx_context_get_state is restored bit for bit. */
+ * current body state with the step kernels' own arithmetic. With rbx_set_body_state_raw in
+ * between, a state saved by rbx_get_body_state_raw + rbx_context_get_state is restored bit for bit. */
 int rbx_context_load(rbx_integrator* h, void* stream, const double* positions, const double* velocities);
 /* rbx_context_get_state for the user atoms [first_atom, first_atom + count) only. */
 int rbx_context_get_range(rbx_integrator* h, void* stream, int first_atom, int count, double* positions,
@@ -356,13 +363,13 @@ int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, con
 int rbx_batch_get_state(rbx_batch* b, void* stream, double* positions, double* velocities);
 /* Positions and velocities of system s only ([n_s*3] each). */
 int rbx_batch_get_system_state(rbx_batch* b, void* stream, int s, double* positions, double* velocities);
-/* Checkpoint and exact restore. rbx_batch_get_body_state gives every body's state (rows of 14, the
- * layout of rbx_get_body_state; bodies system by system in ascending body index). After
- * rbx_batch_set_state with the positions the saved batch was last set up from (they fix each
- * body's principal frame and body-frame coordinates), rbx_batch_restore puts back a saved body
- * state, positions and velocities bit for bit. */
-int rbx_batch_get_body_state(rbx_batch* b, double* body_state);
-int rbx_batch_restore(rbx_batch* b, void* stream, const double* body_state, const double* positions,
+/* Checkpoint and exact restore. rbx_batch_get_body_state gives every body's state as the exact
+ * rows of rbx_get_body_state_raw (112 bytes per body; bodies system by system in ascending body
+ * index). After rbx_batch_set_state with the positions the saved batch was last set up from (they
+ * fix each body's principal frame and body-frame coordinates), rbx_batch_restore puts back saved
+ * body rows, positions and velocities bit for bit. */
+int rbx_batch_get_body_state(rbx_batch* b, void* body_rows);
+int rbx_batch_restore(rbx_batch* b, void* stream, const void* body_rows, const double* positions,
                       const double* velocities);
 int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt);
 /* Relaxation by damped dynamics: nsteps times (forces capped at max_force kJ/mol/nm per atom,

@@ -58,6 +58,8 @@ SIGNATURES = [
     ("rbx_potential_energy_refinement", ctypes.c_int, [_vp, _vp, _bp, _dp]),
     ("rbx_get_body_state", ctypes.c_int, [_vp, _dp]),
     ("rbx_set_body_state", ctypes.c_int, [_vp, _dp]),
+    ("rbx_get_body_state_raw", ctypes.c_int, [_vp, _vp]),
+    ("rbx_set_body_state_raw", ctypes.c_int, [_vp, _vp]),
     ("rbx_get_body_geometry", ctypes.c_int, [_vp, _dp, _dp]),
     ("rbx_get_body_atoms", ctypes.c_int, [_vp, _ip, _ip]),
     ("rbx_context_set_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
@@ -78,9 +80,9 @@ SIGNATURES = [
     ("rbx_batch_destroy", ctypes.c_int, [_vp]),
     ("rbx_batch_set_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
     ("rbx_batch_get_state", ctypes.c_int, [_vp, _vp, _dp, _dp]),
-    ("rbx_batch_get_body_state", ctypes.c_int, [_vp, _dp]),
+    ("rbx_batch_get_body_state", ctypes.c_int, [_vp, _vp]),
     ("rbx_batch_get_system_state", ctypes.c_int, [_vp, _vp, ctypes.c_int, _dp, _dp]),
-    ("rbx_batch_restore", ctypes.c_int, [_vp, _vp, _dp, _dp, _dp]),
+    ("rbx_batch_restore", ctypes.c_int, [_vp, _vp, _vp, _dp, _dp]),
     ("rbx_batch_step", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double]),
     ("rbx_batch_relax", ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("rbx_batch_energies", ctypes.c_int, [_vp, _vp, _dp]),

@@ -12,6 +12,7 @@ import numpy as np
 from . import _lib
 
 EPS_SOLVENT = 78.3
+BODY_ROW_BYTES = 112  # exact body-state row of a checkpoint (rbx_get_body_state_raw)
 
 
 def _d(a):
@@ -115,9 +116,11 @@ class BatchedSystems:
         return x, v
 
     def checkpoint(self, stream=None):
-        """Exact state of every system: a list of (body_state [nb_s, 14], positions, velocities)."""
-        bs = np.zeros((int(self.bodies_per_system.sum()), 14))
-        _lib.check(self._lib.rbx_batch_get_body_state(self._h, _d(bs)))
+        """Exact state of every system: a list of (body rows [nb_s, 112] bytes, positions, velocities).
+        The body rows are the state's device words (rbx_get_body_state_raw): 14 doubles, or the 14
+        high then 14 low floats of the float-float state."""
+        bs = np.zeros((int(self.bodies_per_system.sum()), BODY_ROW_BYTES), dtype=np.uint8)
+        _lib.check(self._lib.rbx_batch_get_body_state(self._h, bs.ctypes.data_as(ctypes.c_void_p)))
         x, v = self.get_state(stream)
         b_off = np.concatenate([[0], np.cumsum(self.bodies_per_system)])
         return [(bs[b_off[k]:b_off[k + 1]].copy(), x[self.offsets[k]:self.offsets[k + 1]].copy(),
@@ -126,10 +129,12 @@ class BatchedSystems:
     def restore(self, states, stream=None):
         """Put back per-system states from ``checkpoint`` (bit for bit). The batch must hold the same
         systems, set up from the positions the checkpointed batch was last set up from."""
-        bs = np.ascontiguousarray(np.concatenate([s[0] for s in states]) if states else np.zeros((0, 14)))
+        bs = np.ascontiguousarray(np.concatenate([s[0] for s in states]) if states else
+                                  np.zeros((0, BODY_ROW_BYTES), dtype=np.uint8), dtype=np.uint8)
         x = np.ascontiguousarray(np.concatenate([s[1] for s in states]))
         v = np.ascontiguousarray(np.concatenate([s[2] for s in states]))
-        _lib.check(self._lib.rbx_batch_restore(self._h, _stream(stream), _d(bs), _d(x), _d(v)))
+        _lib.check(self._lib.rbx_batch_restore(self._h, _stream(stream), bs.ctypes.data_as(ctypes.c_void_p), _d(x),
+                                               _d(v)))
 
     def step(self, nsteps, dt, stream=None):
         _lib.check(self._lib.rbx_batch_step(self._h, _stream(stream), int(nsteps), float(dt)))

@@ -574,19 +574,19 @@ int rbx_batch_get_system_state(rbx_batch* b, void* stream, int s, double* positi
                                  velocities);
 }
 
-int rbx_batch_get_body_state(rbx_batch* b, double* body_state) {
+int rbx_batch_get_body_state(rbx_batch* b, void* body_rows) {
     int rc = check(b);
     if (rc) return rc;
-    return rbx_get_body_state(b->integ, body_state);
+    return rbx_get_body_state_raw(b->integ, body_rows);
 }
 
-int rbx_batch_restore(rbx_batch* b, void* stream, const double* body_state, const double* positions,
+int rbx_batch_restore(rbx_batch* b, void* stream, const void* body_rows, const double* positions,
                       const double* velocities) {
     int rc = check(b);
     if (rc) return rc;
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no geometry: call rbx_batch_set_state with the systems first");
     if ((rc = rbx_context_load(b->integ, stream, positions, velocities))) return rc;
-    if ((rc = rbx_set_body_state(b->integ, body_state))) return rc;
+    if ((rc = rbx_set_body_state_raw(b->integ, body_rows))) return rc;
     if ((rc = rbx_context_sync_bodies(b->integ, stream))) return rc;
     BATCH_TRY(cudaMemsetAsync(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)b->S, (cudaStream_t)stream));
     b->u_valid = false;

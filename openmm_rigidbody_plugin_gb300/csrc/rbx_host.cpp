@@ -1185,6 +1185,57 @@ int rbx_set_body_state(rbx_integrator* h, const double* state) {
     return put_state(h, s);
 }
 
+// Raw rows: the body state's device words, 112 bytes per body in every precision (14 doubles, or
+// 14 high then 14 low floats of the float-float state), bodies in ascending body index.
+int rbx_get_body_state_raw(rbx_integrator* h, void* rows) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body state");
+    if (!rows && h->nb) return fail(RBX_ERR_INVALID_ARGUMENT, "null output");
+    if ((rc = ensure_host_plan(h))) return rc;
+    CUDA_TRY(cudaSetDevice(h->device));
+    const size_t nbp = (size_t)h->nb_pad;
+    if (h->prec == PREC_DOUBLE) {
+        std::vector<double> d(14 * nbp);
+        CUDA_TRY(cudaMemcpy(d.data(), h->d_state.p, d.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        double* out = (double*)rows;
+        for (int b = 0; b < h->nb; b++)
+            for (int k = 0; k < 14; k++) out[14 * (size_t)b + k] = d[h->lib_pos[b] + k * nbp];
+    } else {
+        std::vector<float> f(28 * nbp);
+        CUDA_TRY(cudaMemcpy(f.data(), h->d_state.p, f.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        float* out = (float*)rows;
+        for (int b = 0; b < h->nb; b++)
+            for (int k = 0; k < 28; k++) out[28 * (size_t)b + k] = f[h->lib_pos[b] + k * nbp];
+    }
+    return RBX_OK;
+}
+
+int rbx_set_body_state_raw(rbx_integrator* h, const void* rows) {
+    int rc = check(h);
+    if (rc) return rc;
+    if (!h->have_state) return fail(RBX_ERR_STATE, "no rigid-body geometry: call rbx_upload_state first");
+    if (!rows && h->nb) return fail(RBX_ERR_INVALID_ARGUMENT, "null state");
+    if ((rc = ensure_host_plan(h))) return rc;
+    CUDA_TRY(cudaSetDevice(h->device));
+    const size_t nbp = (size_t)h->nb_pad;
+    if (h->prec == PREC_DOUBLE) {
+        std::vector<double> d(14 * nbp, 0.0);
+        const double* in = (const double*)rows;
+        for (int b = 0; b < h->nb; b++)
+            for (int k = 0; k < 14; k++) d[h->lib_pos[b] + k * nbp] = in[14 * (size_t)b + k];
+        CUDA_TRY(cudaMemcpy(h->d_state.p, d.data(), d.size() * sizeof(double), cudaMemcpyHostToDevice));
+    } else {
+        std::vector<float> f(28 * nbp, 0.0f);
+        const float* in = (const float*)rows;
+        for (int b = 0; b < h->nb; b++)
+            for (int k = 0; k < 28; k++) f[h->lib_pos[b] + k * nbp] = in[28 * (size_t)b + k];
+        CUDA_TRY(cudaMemcpy(h->d_state.p, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    h->ref_phase = 0;
+    return clear_failures(h, nullptr);
+}
+
 int rbx_get_body_geometry(rbx_integrator* h, double* moments, double* body_fixed) {
     int rc = check(h);
     if (rc) return rc;

@@ -288,6 +288,16 @@ class IntegratorKernel:
         s = np.ascontiguousarray(state, dtype=np.float64)
         _lib.check(self._lib.rbx_set_body_state(self._h, _dptr(s)))
 
+    def body_state_raw(self):
+        """The body state's exact device words, 112 bytes per body (rbx_get_body_state_raw)."""
+        out = np.zeros((self.num_bodies, 112), dtype=np.uint8)
+        _lib.check(self._lib.rbx_get_body_state_raw(self._h, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
+
+    def set_body_state_raw(self, rows):
+        r = np.ascontiguousarray(rows, dtype=np.uint8)
+        _lib.check(self._lib.rbx_set_body_state_raw(self._h, r.ctypes.data_as(ctypes.c_void_p)))
+
     def geometry(self):
         first, _ = self.body_atoms()
         I = np.zeros((self.num_bodies, 3))

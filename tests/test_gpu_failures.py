@@ -115,7 +115,7 @@ def test_non_finite_restored_state_fails_only_its_system(rbx):
     states = b.checkpoint()
     body, x, v = states[3]
     body = body.copy()
-    body[5, 11] = np.nan
+    body.view(np.float32)[5, 11] = np.nan  # pi.x of body 5, high word (mixed precision)
     states[3] = (body, x, v)
     b.restore(states)
     assert not b.status().any()

@@ -33,6 +33,9 @@ def test_checkpoint_restore_is_exact(mods, precision):
     ckpt = a.checkpoint()
     b = batch.BatchedSystems.from_systems(systems, precision=precision)
     b.restore(ckpt)
+    # the body rows are the device words: every float-float low word comes back as it was
+    for (ra, _, _), (rb, _, _) in zip(ckpt, b.checkpoint()):
+        assert ra.shape[1] == 112 and np.array_equal(ra, rb)
     for h in (a, b):
         h.step(20, 0.002)
     for u, w in zip(a.get_state(), b.get_state()):
