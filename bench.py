@@ -3,7 +3,7 @@
 Default workload (the batched-replicas configuration): 4096 independent systems per GPU, body
 counts log-uniform in [64, 4096] (70 % 3-site waters, 20 % 5-atom tetrahedra, 10 % 12-atom planar
 rings), each in its own periodic box at 1 g/cm^3, cutoff LJ + reaction-field forces from the
-library's cell-list kernel, 300 K, dt 2 fs, rotation mode 0, mixed precision. One step is one full
+library's neighbour-list kernel, 300 K, dt 2 fs, rotation mode 0, mixed precision. One step is one full
 velocity-Verlet step of every system (forces, then the integrator), all systems in one launch per
 kernel, runs of steps replayed from captured CUDA graphs. The working set (about 1 GB) exceeds the
 129 MB L2, so no flush is needed between steps.
@@ -12,7 +12,7 @@ kernel, runs of steps replayed from captured CUDA graphs. The working set (about
           launching stream, max over ranks), inputs resident in HBM
   plain / speedup_vs_plain  the same systems stepped one system per launch (one handle each, the
           plain drop-in way), from the same exact state, and the ratio; both energy drifts, and
-          whether the final energies of the two arms are bit-equal
+          whether the final states and energies of the two arms are bit-equal
   e2e     the same metric through the public API with host buffers: positions and velocities in
           (set_state), the steps in chunks of 10 with the energies read back after each, positions
           and velocities out
