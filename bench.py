@@ -197,6 +197,19 @@ def host_link(h2d, d2h, device, reps=10):
     return {"h2d_gbs": h2d / ms["in"] / 1e6, "d2h_gbs": d2h / ms["out"] / 1e6, "copies_both_ms": ms["both"]}
 
 
+def ncu_traffic_batched(bodies):
+    """DRAM bytes of one fused step launch of the batched workload (mode 0, mixed) from the
+    committed ncu summary, captured on 1024 systems and scaled to `bodies`; None without it."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    if "fused_batched_mode0_mixed_bytes_per_launch" not in d:
+        return None
+    return d["fused_batched_mode0_mixed_bytes_per_launch"] * bodies / d["batched_bodies"]
+
+
 def ncu_traffic(mode, precision, bodies):
     """DRAM bytes of one fused step launch from the committed ncu summary (profiles/traffic.json),
     captured on a smaller case of the same mix and scaled to `bodies` (traffic is proportional to
@@ -822,7 +835,8 @@ def run_batched(args, world, rank, local):
                                    [s.num_atoms for s in systems])) / (args.steps + 1) / na)},
            "speedup_vs_plain": (value / world / plain["value"]) if plain else None,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                        "peak_source": peak_kind, "traffic": None, "algorithmic_bytes_per_launch": bytes_step,
+                        "peak_source": peak_kind, "traffic": ncu_traffic_batched(nb) if args.workload == "batched" else None,
+                        "algorithmic_bytes_per_launch": bytes_step,
                         "kernel": "rbx::step_kernel_f (the integrator launches of the batched step: part1, fused, "
                                   "part2; bytes per fused launch)",
                         "integrator_ms_per_step": ms_i / 21, "force_ms_per_step": ms_f / 21,
