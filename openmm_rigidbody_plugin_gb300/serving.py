@@ -74,6 +74,9 @@ class _Group:
         self.bytes = nbytes
         self.stream = stream
         self.k = 0
+        self.event = None       # recorded after the chunk in flight
+        self.in_flight = False
+        self.t_launch = 0.0
 
     def live(self):
         return [r for r in self.members if r.completed is None]
@@ -97,11 +100,17 @@ class Server:
                    in between are admitted together)
     dead_fraction  a group whose finished or failed systems hold more than this fraction of its
                    atoms is compacted
+
+    Groups advance independently: each has at most one chunk in flight on its stream, marked by an
+    event; the loop waits for the oldest chunk, takes every chunk that has finished, and launches the
+    next chunk of each of those groups at once, so a small group never waits for a large one and
+    the host's admissions, group creations and result reads overlap the device's work.
     """
 
     def __init__(self, budget_bytes=150e9, chunk_steps=100, dt=0.002, precision="mixed", rotation_mode=0,
                  graph_steps=25, device=0, min_interval=0.05, dead_fraction=0.5, reserve_bytes=2e9,
-                 batch_factory=None, sync=None, free_memory=None, stream_factory=None, keep_states=True):
+                 batch_factory=None, sync=None, free_memory=None, stream_factory=None, keep_states=True,
+                 event_factory=None):
         self.budget = float(budget_bytes)
         self.chunk = int(chunk_steps)
         self.dt = float(dt)
@@ -127,6 +136,7 @@ class Server:
         self._sync = sync
         self._free_memory = free_memory
         self._stream_factory = stream_factory
+        self._event_factory = event_factory
 
     # ---------------------------------------------------------------------------------------
     def _torch_defaults(self):
@@ -137,6 +147,8 @@ class Server:
             self._free_memory = lambda: torch.cuda.mem_get_info(self.device)[0]
         if self._stream_factory is None:
             self._stream_factory = lambda: torch.cuda.Stream(self.device)
+        if self._event_factory is None:
+            self._event_factory = torch.cuda.Event
 
     def _make(self, systems):
         return self._factory(systems, rotation_mode=self.mode, precision=self.precision, device=self.device)
@@ -230,16 +242,25 @@ class Server:
                 if pending:
                     time.sleep(max(0.0, min(pending[0].arrival - now(), 0.01)))
                 continue
-            # one chunk of every running group, each on its own stream
+            # the next chunk of every running group without one in flight, each on its own stream
             ts = time.perf_counter()
             for g in running:
+                if g.in_flight:
+                    continue
                 g.k = min(self.chunk, min(r.steps - r.done_steps for r in g.live()))
                 g.batch.step(g.k, self.dt, stream=g.stream)
-            self._sync()
+                self.launches += g.batch.last_launch_count
+                g.event = self._event_factory()
+                g.event.record(g.stream)
+                g.in_flight = True
+                g.t_launch = time.perf_counter()
+            # wait for the oldest chunk in flight; take every chunk that has finished
+            min(running, key=lambda g: g.t_launch).event.synchronize()
+            finished_chunks = [g for g in running if g.event.query()]
             self.seconds["step"] += time.perf_counter() - ts
             tf = time.perf_counter()
-            for g in running:
-                self.launches += g.batch.last_launch_count
+            for g in finished_chunks:
+                g.in_flight = False
                 live = g.live()
                 self.body_steps += g.k * sum(r.bodies for r in live)
                 for r in live:
@@ -265,9 +286,12 @@ class Server:
                             r.system = None  # made again on demand (seeded)
                         done.append(r)
             self.seconds["results"] += time.perf_counter() - tf
-            # release finished groups; compact mostly-finished ones
+            # release finished groups; compact mostly-finished ones (not while a chunk is in flight)
             kept = []
             for g in groups:
+                if g.in_flight:
+                    kept.append(g)
+                    continue
                 live = g.live()
                 if not live:
                     in_use -= g.bytes

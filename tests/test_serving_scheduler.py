@@ -62,10 +62,23 @@ class FakeBatch:
         return np.stack([self.counter] * 3, axis=1).astype(float)
 
 
+class FakeEvent:
+    """A stand-in stream event: the stand-in batches finish their chunks at once."""
+
+    def record(self, stream):
+        pass
+
+    def synchronize(self):
+        pass
+
+    def query(self):
+        return True
+
+
 def _server(**kw):
     kw.setdefault("batch_factory", FakeBatch)
     return serving.Server(sync=lambda: None, free_memory=lambda: 1e15, stream_factory=lambda: None, reserve_bytes=0,
-                          **kw)
+                          event_factory=FakeEvent, **kw)
 
 
 def _requests(rng, n):
@@ -130,3 +143,41 @@ def test_mostly_finished_group_is_compacted_exactly():
     done = server.run(reqs, realtime=False)
     assert server.compactions >= 1
     assert {r.rid: r.result["energies"][0] for r in done} == {0: 10, 1: 200}
+
+
+@pytest.mark.timeout(60)
+@pytest.mark.parametrize("seed", [3, 4])
+def test_groups_advance_independently(seed):
+    """Chunks finish in any order (a stand-in event completes at random unless waited on): each
+    group launches its next chunk as soon as its own finishes, every request still completes with
+    exactly its steps, and groups run several chunks while another's is in flight."""
+    rng = np.random.default_rng(seed)
+    launched = []
+
+    class RandomEvent(FakeEvent):
+        def __init__(self):
+            self.done = False
+
+        def synchronize(self):
+            self.done = True
+
+        def query(self):
+            self.done = self.done or bool(rng.random() < 0.3)
+            return self.done
+
+    class Logged(FakeBatch):
+        def step(self, k, dt, stream=None):
+            launched.append(id(self))
+            super().step(k, dt, stream)
+
+    reqs = _requests(rng, 20)
+    server = serving.Server(sync=lambda: None, free_memory=lambda: 1e15, stream_factory=lambda: None, reserve_bytes=0,
+                            event_factory=RandomEvent, batch_factory=Logged, budget_bytes=BYTES_PER_ATOM * 2000,
+                            chunk_steps=20)
+    done = server.run(reqs, realtime=False)
+    assert sorted(r.rid for r in done) == list(range(20))
+    for r in done:
+        assert r.done_steps == r.steps == sum(r.chunks)
+        assert r.result["energies"][0] == r.steps
+    # some group launched two chunks in a row while others were in flight
+    assert any(a == b for a, b in zip(launched, launched[1:]))
