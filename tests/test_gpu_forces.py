@@ -39,13 +39,34 @@ def oracle_forces(oracle_mod, systems, pos):
                             body)
 
 
-@pytest.mark.parametrize("case", ["water512_one_cell", "mixed_cells", "batch_of_8"])
+def merged_waters(W, seed):
+    """A mixed box in which the 15 waters nearest one point form one rigid 45-atom body and the 40
+    nearest another point one 120-atom body: groups larger than a warp pass and than the step
+    kernel's per-thread sums, whose radii make the list cells large."""
+    s = W.mixed_system(n_bodies=3000, n_free=300, seed=seed)
+    bidx = s.body_indices.copy()
+    ids, counts = np.unique(bidx[bidx > 0], return_counts=True)
+    waters = ids[counts == 3]
+    centre = {i: s.positions[bidx == i].mean(axis=0) for i in waters}
+    free_id = bidx.max() + 1
+    for n, point in ((15, 0.25 * s.box), (40, 0.75 * s.box)):
+        near = sorted((i for i in waters if (bidx == i).any()), key=lambda i: np.sum((centre[i] - point) ** 2))[:n]
+        for i in near:
+            bidx[bidx == i] = free_id
+        free_id += 1
+    s.body_indices = bidx
+    return s
+
+
+@pytest.mark.parametrize("case", ["water512_one_cell", "mixed_cells", "batch_of_8", "large_groups"])
 def test_forces_and_energies_match_oracle(B, oracle_mod, case):
     from openmm_rigidbody_plugin_gb300 import workloads as W
     if case == "water512_one_cell":
         systems = [W.water_box(512, seed=1)]          # 2.48 nm box: fewer than 3 cells per edge
     elif case == "mixed_cells":
         systems = [W.mixed_system(n_bodies=3000, n_free=300, seed=12)]  # 5 cells per edge
+    elif case == "large_groups":
+        systems = [merged_waters(W, 13), W.mixed_system(n_bodies=400, n_free=40, seed=14)]
     else:
         systems = W.batch_systems(8, lo=64, hi=1500, seed=9)
     # generated mixed structures overlap (lattice sites 0.34 nm apart): relax them first
@@ -59,9 +80,15 @@ def test_forces_and_energies_match_oracle(B, oracle_mod, case):
     assert np.all(np.abs(e - eo) <= 1e-6 * np.abs(eo) + 1e-5 * natoms), (e, eo)
 
 
-def test_system_alone_equals_system_in_batch(B):
+@pytest.mark.parametrize("large", [False, True])
+def test_system_alone_equals_system_in_batch(B, large):
+    """With `large`, one system holds rigid bodies of 45 and 120 atoms: the batch then runs the step
+    kernel form that sums such bodies by a warp, while the other systems alone run the ordinary
+    form; their trajectories are the same bit for bit."""
     from openmm_rigidbody_plugin_gb300 import workloads as W
     systems = W.batch_systems(5, lo=64, hi=1200, seed=10)
+    if large:
+        systems = systems[:3] + [merged_waters(W, 15)]
     together = B.BatchedSystems.from_systems(systems, relax_steps=100)
     x0, v0 = together.get_state()
     together.set_state(x0, v0)  # both runs set up from the same positions (they fix the body frames)
