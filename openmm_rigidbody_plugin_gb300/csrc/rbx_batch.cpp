@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <new>
@@ -121,6 +122,7 @@ int setup_lists(rbx_batch* b, const double* x) {
     const int S = b->S;
     std::vector<FFSys> sys = b->sys_h;
     std::vector<int> mc_cell, mc_sys, sc_sys, sc_g0;
+    std::vector<uint64_t> zkey(b->grp_n_h.size());  // spatial order of the groups (see below)
     double cap_need = 1.0;
     for (int s = 0; s < S; s++) {
         FFSys& f = sys[s];
@@ -134,6 +136,15 @@ int setup_lists(rbx_batch* b, const double* x) {
             for (int a = 1; a < n; a++)
                 for (int d = 0; d < 3; d++) c[d] += img(x[3 * (size_t)b->iatom_h[k0 + a] + d] - x0[d]);
             for (int d = 0; d < 3; d++) c[d] = x0[d] + c[d] / n;
+            // Z-order (Morton) code of the centroid on a 1024^3 grid of the box
+            uint64_t z = 0;
+            for (int d = 0; d < 3; d++) {
+                double u = c[d] / L;
+                u -= std::floor(u);
+                const uint64_t q = std::min<uint64_t>(1023, (uint64_t)(u * 1024.0));
+                for (int bit = 0; bit < 10; bit++) z |= ((q >> bit) & 1ull) << (3 * bit + d);
+            }
+            zkey[g] = ((uint64_t)s << 30) | z;
             for (int a = 0; a < n; a++) {
                 double r2 = 0.0;
                 for (int d = 0; d < 3; d++) {
@@ -170,6 +181,21 @@ int setup_lists(rbx_batch* b, const double* x) {
     const size_t entries = (size_t)std::max(b->ff.n_groups, 1) * (size_t)cap;
     if (b->d_nbr.n < entries && b->d_nbr.alloc(entries) != cudaSuccess)
         return set_error(RBX_ERR_CUDA, "cudaMalloc of the neighbour lists failed (%d entries per group)", cap);
+    // The force pass takes its groups in this order: a system's groups in Z-order of their
+    // centroids, so that the warps resident on an SM at once work on neighbouring groups and find
+    // much of each other's neighbours in L1. The order schedules work only: every group's forces
+    // are formed alike whichever warp forms them.
+    {
+        std::vector<int> small, large;
+        for (int g = 0; g < (int)zkey.size(); g++) (b->grp_n_h[g] <= kSmallGroupAtoms ? small : large).push_back(g);
+        auto by_key = [&](int u, int v) { return zkey[u] < zkey[v] || (zkey[u] == zkey[v] && u < v); };
+        std::sort(small.begin(), small.end(), by_key);
+        std::sort(large.begin(), large.end(), by_key);
+        if (!small.empty())
+            BATCH_TRY(cudaMemcpy(b->d_small_groups.p, small.data(), sizeof(int) * small.size(), cudaMemcpyHostToDevice));
+        if (!large.empty())
+            BATCH_TRY(cudaMemcpy(b->d_large_groups.p, large.data(), sizeof(int) * large.size(), cudaMemcpyHostToDevice));
+    }
     BATCH_TRY(cudaMemcpy(b->d_sys.p, sys.data(), sizeof(FFSys) * (size_t)S, cudaMemcpyHostToDevice));
     if (!mc_cell.empty()) {
         BATCH_TRY(cudaMemcpy(b->d_mc_cell.p, mc_cell.data(), sizeof(int) * mc_cell.size(), cudaMemcpyHostToDevice));
@@ -414,7 +440,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     if (!rc) rc = upload_vec(b->d_gsys, gsys);
     if (!rc) rc = upload_vec(b->d_kgrp, kgrp);
     std::vector<int> small_groups, large_groups;  // the two force passes
-    for (int g = 0; g < (int)grp_n.size(); g++) (grp_n[g] <= 4 ? small_groups : large_groups).push_back(g);
+    for (int g = 0; g < (int)grp_n.size(); g++) (grp_n[g] <= kSmallGroupAtoms ? small_groups : large_groups).push_back(g);
     if (!rc) rc = upload_vec(b->d_small_groups, small_groups);
     if (!rc) rc = upload_vec(b->d_large_groups, large_groups);
     // atom types: the distinct (scaled charge, sigma/2, sqrt(epsilon)) triples; with at most

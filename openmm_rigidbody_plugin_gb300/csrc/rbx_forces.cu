@@ -396,7 +396,7 @@ __device__ __forceinline__ void store_force(const FFDev& D, long long* __restric
 // The pair term is OpenMM's CutoffPeriodic form: reaction-field Coulomb and unshifted LJ.
 constexpr int kFW = 4;     // warps (groups) per block
 constexpr int kQ = 256;    // streamed-atom queue per warp
-constexpr int kSmallGroup = 4;
+constexpr int kSmallGroup = kSmallGroupAtoms;
 constexpr int kLargeChunk = 12;
 
 // One neighbour (position xj after its shift; w: type bits, or its parameters pj) against the ni

@@ -162,6 +162,8 @@ struct FFDev {
     const int* small_groups;
     const int* large_groups;
 };
+// Groups of at most this many interacting atoms run in the force pass's small-group launch.
+constexpr int kSmallGroupAtoms = 4;
 // Interacting atoms of one system: the force pass streams (atom << 5 | lane) words.
 constexpr int kMaxSystemAtoms = 1 << 26;
 int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* stream);
