@@ -462,8 +462,9 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
         if ((int)types.size() > kMaxTypes) types.clear();
     }
     if (types.empty()) type_of.clear();
-    // the type-pair table: (K q_i q_j, C12 = 4 eps sig^12, C6 = 4 eps sig^6) with Lorentz-Berthelot
-    // sig = (sig_i + sig_j)/2, eps = sqrt(eps_i eps_j), formed in FP64 from the FP32 type values
+    // the type-pair table: (K q_i q_j, 12 C12, 6 C6) with C12 = 4 eps sig^12, C6 = 4 eps sig^6 and
+    // Lorentz-Berthelot sig = (sig_i + sig_j)/2, eps = sqrt(eps_i eps_j), formed in FP64 from the
+    // FP32 type values (the force is (12 C12 r^-6 - 6 C6) r^-8 r)
     const int nt = (int)types.size();
     std::vector<float4> pair_table((size_t)nt * nt);
     for (int i = 0; i < nt; i++)
@@ -471,7 +472,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
             const double sig = (double)types[i].y + (double)types[j].y, eps = (double)types[i].z * (double)types[j].z;
             const double s6 = sig * sig * sig * sig * sig * sig;
             pair_table[(size_t)i * nt + j] = make_float4((float)((double)types[i].x * (double)types[j].x),
-                                                         (float)(4.0 * eps * s6 * s6), (float)(4.0 * eps * s6), 0.0f);
+                                                         (float)(48.0 * eps * s6 * s6), (float)(24.0 * eps * s6), 0.0f);
         }
     if (!rc) rc = upload_vec(b->d_types, pair_table);
     if (!rc) rc = upload_vec(b->d_atype, type_of);

@@ -400,43 +400,60 @@ constexpr int kSmallGroup = kSmallGroupAtoms;
 constexpr int kLargeChunk = 12;
 
 // One neighbour (position xj after its shift; w: type bits, or its parameters pj) against the ni
-// group atoms in shared memory. RELAX: coincident atoms have no direction and add nothing. PI: the
-// minimum image per pair.
-template <int KIC, bool ENERGY, bool PT, bool RELAX, bool PI>
+// group atoms in shared memory (NI > 0: exactly NI of them, the loop unrolled without exits).
+// RELAX: coincident atoms have no direction and add nothing. PI: the minimum image per pair.
+// With PT the group atom's .w holds its row of the type-pair table (type x types) and the table
+// gives (K q_i q_j, 12 C12, 6 C6); the LJ force is (12 C12 r^-6 - 6 C6) r^-6 r^-2.
+template <int KIC, int NI, bool ENERGY, bool PT, bool RELAX, bool PI>
 __device__ __forceinline__ void pair_terms(const float4* xs, const float4* ps, int ni, const FFSys& S,
-                                           const float4* ptab, int ntypes, float4 xj, float4 pj, bool valid,
+                                           const float4* ptab, float4 xj, float4 pj, bool valid,
                                            float (&f)[KIC][3], ESum& en) {
-    const float4* prow = PT ? ptab + __float_as_int(xj.w) : nullptr;  // column of the neighbour's type
+    const float4* pcol = PT ? ptab + __float_as_int(xj.w) : nullptr;  // column of the neighbour's type
+    const float two_krf = 2.0f * S.krf;
 #pragma unroll
-    for (int a = 0; a < KIC; a++) {
-        if (a >= ni) break;
+    for (int a = 0; a < (NI > 0 ? NI : KIC); a++) {
+        if (NI == 0 && a >= ni) break;
         const float4 xi = xs[a];
         float3 d = make_float3(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
         if (PI) d = min_image(d.x, d.y, d.z, S);
         const float r2 = fmaf(d.x, d.x, fmaf(d.y, d.y, d.z * d.z));
         const bool in = valid && r2 < S.rc2 && !(RELAX && r2 < 1e-8f);
         const float inv_r = rsqrtf(r2), inv_r2 = inv_r * inv_r, inv_r6 = inv_r2 * inv_r2 * inv_r2;
-        float qq, c12, c6;
+        float4 t;  // K q_i q_j, 12 C12, 6 C6
         if (PT) {
-            const float4 t = prow[__float_as_int(xi.w) * ntypes];
-            qq = t.x;
-            c12 = t.y;
-            c6 = t.z;
+            t = pcol[__float_as_int(xi.w)];
         } else {
             const float4 pi = ps[a];
-            qq = pi.x * pj.x;
             const float sig = pi.y + pj.y, sig2 = sig * sig, sig6 = sig2 * sig2 * sig2;
-            c6 = 4.0f * (pi.z * pj.z) * sig6;
-            c12 = c6 * sig6;
+            const float c6 = 4.0f * (pi.z * pj.z) * sig6;
+            t = make_float4(pi.x * pj.x, 12.0f * c6 * sig6, 6.0f * c6, 0.0f);
         }
-        const float t6 = c6 * inv_r6, t12 = c12 * inv_r6 * inv_r6;
-        float gf = qq * (inv_r * inv_r2 - 2.0f * S.krf) + fmaf(12.0f, t12, -6.0f * t6) * inv_r2;
+        const float lj = inv_r6 * fmaf(t.y, inv_r6, -t.z);  // 12 C12 r^-12 - 6 C6 r^-6
+        float gf = fmaf(t.x, inv_r * inv_r2 - two_krf, lj * inv_r2);
         gf = in ? gf : 0.0f;
         f[a][0] = fmaf(gf, d.x, f[a][0]);
         f[a][1] = fmaf(gf, d.y, f[a][1]);
         f[a][2] = fmaf(gf, d.z, f[a][2]);
-        if (ENERGY && in) en.add(qq * (inv_r + S.krf * r2 - S.crf) + (t12 - t6));
+        if (ENERGY && in)
+            en.add(t.x * (inv_r + S.krf * r2 - S.crf) + inv_r6 * (t.y * (1.0f / 12.0f) * inv_r6 - t.z * (1.0f / 6.0f)));
     }
+}
+
+// The pair terms of one streamed neighbour, with the group size and image form chosen (the same
+// choice for every lane): exact-size forms for the common sizes (1: a free atom; 3: a water; 5:
+// a tetrahedral body; 12: a ring), the general one otherwise.
+template <int KIC, bool ENERGY, bool PT, bool RELAX, bool PI>
+__device__ __forceinline__ void pair_dispatch(const float4* xs, const float4* ps, int ni, const FFSys& S,
+                                              const float4* ptab, float4 xj, float4 pj, bool valid,
+                                              float (&f)[KIC][3], ESum& en) {
+    if (KIC == kSmallGroupAtoms) {
+        if (ni == 3) return pair_terms<KIC, (KIC >= 3 ? 3 : 0), ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
+        if (ni == 1) return pair_terms<KIC, 1, ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
+    } else {
+        if (ni == 5) return pair_terms<KIC, (KIC >= 5 ? 5 : 0), ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
+        if (ni == KIC) return pair_terms<KIC, KIC, ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
+    }
+    pair_terms<KIC, 0, ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
 }
 
 template <int KIC, bool ENERGY, bool PT, bool RELAX>
@@ -476,7 +493,9 @@ __global__ void __launch_bounds__(32 * kFW, KIC == kSmallGroup ? 8 : 5)
         __syncwarp();
         if (lane < ni) {
             const int k = k0 + a0 + lane;
-            xs[lane] = D.cpos[k];
+            const float4 x = D.cpos[k];
+            // with the type-pair table, .w becomes the atom's row offset in it (type x types)
+            xs[lane] = PT ? make_float4(x.x, x.y, x.z, __int_as_float(__float_as_int(x.w) * nt)) : x;
             if (!PT) ps[lane] = D.param[k];
         }
         __syncwarp();
@@ -531,9 +550,9 @@ __global__ void __launch_bounds__(32 * kFW, KIC == kSmallGroup ? 8 : 5)
                     const float4 xj = make_float4(xq.x + sv.x, xq.y + sv.y, xq.z + sv.z, xq.w);
                     const float4 pj = PT ? xj : cpar[qv >> 5];
                     if (pim)
-                        pair_terms<KIC, ENERGY, PT, RELAX, true>(xs, ps, ni, S, stab, nt, xj, pj, valid, f, en);
+                        pair_dispatch<KIC, ENERGY, PT, RELAX, true>(xs, ps, ni, S, stab, xj, pj, valid, f, en);
                     else
-                        pair_terms<KIC, ENERGY, PT, RELAX, false>(xs, ps, ni, S, stab, nt, xj, pj, valid, f, en);
+                        pair_dispatch<KIC, ENERGY, PT, RELAX, false>(xs, ps, ni, S, stab, xj, pj, valid, f, en);
                     valid = vn;
                     qv = qvn;
                     xq = xqn;
