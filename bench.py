@@ -84,7 +84,7 @@ def parse():
                    help="bound on the timed CPU work of --impl reference")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--workload", default="batched", choices=["single", "batched", "water", "served", "precision"],
-                   help="batched (default): many independent systems, full steps with the cell-list force field, "
+                   help="batched (default): many independent systems, full steps with the library's force field, "
                         "against one system per launch, with the single-system figures as an extra key; single: "
                         "the 1e6-body integrator step; water: 512 rigid waters, full steps")
     p.add_argument("--systems", type=int, default=4096, help="batched: number of systems per GPU")
@@ -668,7 +668,7 @@ def batched_config(args, world):
 
 
 def run_batched(args, world, rank, local):
-    """Many independent systems stepped together (full steps: cell-list forces + integrator, one
+    """Many independent systems stepped together (full steps: neighbour-list forces + integrator, one
     launch per kernel per step, runs of steps replayed from captured CUDA graphs), against the same
     systems stepped one system per launch (the plain drop-in way), at equal energy drift."""
     import torch
@@ -951,7 +951,7 @@ def run_served(args, world, rank, local):
 
 def run_precision(args, world, rank, local):
     """Precision study: near-degenerate bodies (two principal moments 1+eps apart, eps log-uniform in
-    [1e-8, 1e-2]) among waters, full steps with the cell-list force field; every precision and
+    [1e-8, 1e-2]) among waters, full steps with the library's force field; every precision and
     rotation mode from the same relaxed state; energy drift and trajectory error after --psteps
     steps against the double-precision run of the same mode and step size."""
     import torch
@@ -1017,7 +1017,7 @@ def run_precision(args, world, rank, local):
                                   "value = mixed, mode 0, 1 fs (the stated 100,000-step runs shortened to "
                                   f"{args.psteps})",
                       "bodies": int(s.num_bodies), "atoms": int(s.num_atoms), "dof": dof,
-                      "forces": "FP32 cell-list kernel in every precision (the study varies the integrator)"},
+                      "forces": "FP32 neighbour-list force pass in every precision (the study varies the integrator)"},
            "precision_study": rows, "roofline": None, "cpu_baseline": None,
            "e2e": None, "clocks": clocks.summary(), "gpu_launches": None}
     print(json.dumps(out), flush=True)

@@ -1,6 +1,6 @@
 """Batched systems: many independent periodic systems stepped together (rbx_batch_* C ABI).
 
-Each system is a rigid-body system in its own cubic box; forces come from the library's cell-list
+Each system is a rigid-body system in its own cubic box; forces come from the library's neighbour-list
 cutoff Lennard-Jones + reaction-field kernels (the CutoffPeriodic form of OpenMM's
 NonbondedForce), and the whole set advances with one integrator launch per step. Runs of steps
 can replay a captured CUDA graph (``graph_steps``).
