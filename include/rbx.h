@@ -347,7 +347,7 @@ int rbx_last_launch_count(const rbx_integrator* h);
  * freedom.
  * Forces come from neighbour lists of atom groups (each rigid body is one group, each free atom a
  * group of its own): two groups are listed together when their centroids lie within cutoff + a
- * skin of 0.1 nm + both groups' radii. Each system rebuilds its lists when one of its centroids has
+ * skin of 0.06 nm + both groups' radii. Each system rebuilds its lists when one of its centroids has
  * moved half the skin, and every call rebuilds them at its first evaluation: a system's results are
  * a function of its own state and of the lengths of the calls that step it.
  */

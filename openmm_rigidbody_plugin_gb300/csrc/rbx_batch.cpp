@@ -25,7 +25,7 @@ using namespace rbx;
 namespace {
 
 constexpr double kOne4PiEps0 = 138.935456;  // kJ nm / (mol e^2)
-constexpr double kSkin = 0.1;               // nm: neighbour-list skin (of group centroids)
+constexpr double kSkin = 0.06;              // nm: neighbour-list skin (of group centroids)
 constexpr int kMaxTypes = 32;               // atom types of the type-pair table (FFDev::types)
 
 #define BATCH_TRY(call)                                                                             \
@@ -56,7 +56,8 @@ struct rbx_batch {
     DevArray<FFSys> d_sys;
     DevArray<int> d_iatom, d_isys, d_cell_of, d_cell_count, d_cell_start, d_cell_cursor, d_cell_list;
     DevArray<int> d_grp_k0, d_grp_n, d_gsys, d_kgrp;
-    DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_g0, d_small_groups, d_large_groups;
+    DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_g0;
+    DevArray<int> d_pass_groups[kForcePasses];  // FFDev::pass_groups
     DevArray<float4> d_param, d_cpos, d_gcen, d_gref, d_gq, d_types;
     DevArray<unsigned char> d_rebuild;  // FFDev::rebuild
     DevArray<unsigned int> d_nbr;       // neighbour lists of groups (FFDev::nbr)
@@ -186,15 +187,15 @@ int setup_lists(rbx_batch* b, const double* x) {
     // much of each other's neighbours in L1. The order schedules work only: every group's forces
     // are formed alike whichever warp forms them.
     {
-        std::vector<int> small, large;
-        for (int g = 0; g < (int)zkey.size(); g++) (b->grp_n_h[g] <= kSmallGroupAtoms ? small : large).push_back(g);
+        std::vector<int> pass[kForcePasses];
+        for (int g = 0; g < (int)zkey.size(); g++) pass[force_pass_of(b->grp_n_h[g])].push_back(g);
         auto by_key = [&](int u, int v) { return zkey[u] < zkey[v] || (zkey[u] == zkey[v] && u < v); };
-        std::sort(small.begin(), small.end(), by_key);
-        std::sort(large.begin(), large.end(), by_key);
-        if (!small.empty())
-            BATCH_TRY(cudaMemcpy(b->d_small_groups.p, small.data(), sizeof(int) * small.size(), cudaMemcpyHostToDevice));
-        if (!large.empty())
-            BATCH_TRY(cudaMemcpy(b->d_large_groups.p, large.data(), sizeof(int) * large.size(), cudaMemcpyHostToDevice));
+        for (int k = 0; k < kForcePasses; k++) {
+            std::sort(pass[k].begin(), pass[k].end(), by_key);
+            if (!pass[k].empty())
+                BATCH_TRY(cudaMemcpy(b->d_pass_groups[k].p, pass[k].data(), sizeof(int) * pass[k].size(),
+                                     cudaMemcpyHostToDevice));
+        }
     }
     BATCH_TRY(cudaMemcpy(b->d_sys.p, sys.data(), sizeof(FFSys) * (size_t)S, cudaMemcpyHostToDevice));
     if (!mc_cell.empty()) {
@@ -439,10 +440,9 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     if (!rc) rc = upload_vec(b->d_grp_n, grp_n);
     if (!rc) rc = upload_vec(b->d_gsys, gsys);
     if (!rc) rc = upload_vec(b->d_kgrp, kgrp);
-    std::vector<int> small_groups, large_groups;  // the two force passes
-    for (int g = 0; g < (int)grp_n.size(); g++) (grp_n[g] <= kSmallGroupAtoms ? small_groups : large_groups).push_back(g);
-    if (!rc) rc = upload_vec(b->d_small_groups, small_groups);
-    if (!rc) rc = upload_vec(b->d_large_groups, large_groups);
+    std::vector<int> pass_groups[kForcePasses];  // the force passes' groups, by size
+    for (int g = 0; g < (int)grp_n.size(); g++) pass_groups[force_pass_of(grp_n[g])].push_back(g);
+    for (int k = 0; k < kForcePasses && !rc; k++) rc = upload_vec(b->d_pass_groups[k], pass_groups[k]);
     // atom types: the distinct (scaled charge, sigma/2, sqrt(epsilon)) triples; with at most
     // kMaxTypes of them the force pass reads one 16-byte record per neighbour (position and type)
     // and takes each pair's coefficients from a table of type pairs
@@ -537,10 +537,10 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     D.types = b->d_types.p;
     D.atype = b->d_atype.p;
     D.ntypes = (int)types.size();
-    D.n_small = (int)small_groups.size();
-    D.n_large = (int)large_groups.size();
-    D.small_groups = b->d_small_groups.p;
-    D.large_groups = b->d_large_groups.p;
+    for (int k = 0; k < kForcePasses; k++) {
+        D.n_pass[k] = (int)pass_groups[k].size();
+        D.pass_groups[k] = b->d_pass_groups[k].p;
+    }
     D.cell_threads = 128;
     D.n_mc = 0;
     D.n_sc = 0;
@@ -753,7 +753,7 @@ int rbx_batch_memory(const rbx_batch* b, size_t* bytes) {
                b->d_cell_count.bytes() + b->d_cell_start.bytes() + b->d_cell_cursor.bytes() + b->d_cell_list.bytes() +
                b->d_grp_k0.bytes() + b->d_grp_n.bytes() + b->d_gsys.bytes() + b->d_kgrp.bytes() +
                b->d_mc_cell.bytes() + b->d_mc_sys.bytes() + b->d_sc_sys.bytes() + b->d_sc_g0.bytes() +
-               b->d_small_groups.bytes() + b->d_large_groups.bytes() +
+               b->d_pass_groups[0].bytes() + b->d_pass_groups[1].bytes() + b->d_pass_groups[2].bytes() +
                b->d_param.bytes() + b->d_cpos.bytes() + b->d_gcen.bytes() + b->d_gref.bytes() + b->d_gq.bytes() +
                b->d_types.bytes() + b->d_rebuild.bytes() + b->d_nbr.bytes() + b->d_ncnt.bytes() + b->d_atype.bytes() +
                b->d_rebuilds.bytes() + b->d_e_group.bytes() + b->d_energy.bytes() + b->d_body0.bytes() +

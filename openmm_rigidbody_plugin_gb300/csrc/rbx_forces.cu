@@ -8,7 +8,7 @@
 //
 // Forces come from neighbour lists of groups: the interacting atoms of one rigid body (or one free
 // atom) form a group, and a group's list holds every group whose centroid lies within cutoff +
-// skin (0.1 nm) + both groups' radii. A rigid group's atoms stay within its radius of its centroid
+// skin (0.06 nm) + both groups' radii. A rigid group's atoms stay within its radius of its centroid
 // however the body turns, so a list ages only as the centroids move: each system rebuilds its
 // lists when one of its centroids has moved half the skin since its last build, and at the first
 // evaluation of every call (so a call's results depend only on the positions it starts from, never
@@ -389,15 +389,15 @@ __device__ __forceinline__ void store_force(const FFDev& D, long long* __restric
 // Atoms sit at their images nearest their own group's centroid, so the group shift gives the
 // minimum image of every pair within the cutoff when cutoff + two radii < L/2; systems of smaller
 // boxes (FFSys::pair_image) take the minimum image per pair as well.
-// Groups of at most 4 atoms (waters, free atoms) run in a launch with KIC = 4, the others with
-// KIC = 12 (fewer registers for the common case). With at most 32 atom types (PT) each pair's
-// (K q_i q_j, C12, C6) comes from a type-pair table in shared memory, else from the atoms' own
-// parameters by Lorentz-Berthelot.
+// Groups run in three launches by size (force_pass_of): at most 4 atoms (waters, free atoms) with
+// KIC = 4, at most 8 with KIC = 8, the others 12 at a time (fewer registers, and so more warps, for
+// the small groups). With at most 32 atom types (PT) each pair's (K q_i q_j, 12 C12, 6 C6) comes
+// from a type-pair table in shared memory, else from the atoms' own parameters by
+// Lorentz-Berthelot.
 // The pair term is OpenMM's CutoffPeriodic form: reaction-field Coulomb and unshifted LJ.
 constexpr int kFW = 4;     // warps (groups) per block
 constexpr int kQ = 256;    // streamed-atom queue per warp
-constexpr int kSmallGroup = kSmallGroupAtoms;
-constexpr int kLargeChunk = 12;
+constexpr int kPassKIC[kForcePasses] = {4, 8, 12};  // group atoms per pass over the list, by launch
 
 // One neighbour (position xj after its shift; w: type bits, or its parameters pj) against the ni
 // group atoms in shared memory (NI > 0: exactly NI of them, the loop unrolled without exits).
@@ -441,23 +441,24 @@ __device__ __forceinline__ void pair_terms(const float4* xs, const float4* ps, i
 
 // The pair terms of one streamed neighbour, with the group size and image form chosen (the same
 // choice for every lane): exact-size forms for the common sizes (1: a free atom; 3: a water; 5:
-// a tetrahedral body; 12: a ring), the general one otherwise.
+// a tetrahedral body; 12: a ring or a full chunk of a larger body), the general one otherwise.
 template <int KIC, bool ENERGY, bool PT, bool RELAX, bool PI>
 __device__ __forceinline__ void pair_dispatch(const float4* xs, const float4* ps, int ni, const FFSys& S,
                                               const float4* ptab, float4 xj, float4 pj, bool valid,
                                               float (&f)[KIC][3], ESum& en) {
-    if (KIC == kSmallGroupAtoms) {
+    if (KIC == 4) {
         if (ni == 3) return pair_terms<KIC, (KIC >= 3 ? 3 : 0), ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
         if (ni == 1) return pair_terms<KIC, 1, ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
-    } else {
+    } else if (KIC == 8) {
         if (ni == 5) return pair_terms<KIC, (KIC >= 5 ? 5 : 0), ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
+    } else {
         if (ni == KIC) return pair_terms<KIC, KIC, ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
     }
     pair_terms<KIC, 0, ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
 }
 
 template <int KIC, bool ENERGY, bool PT, bool RELAX>
-__global__ void __launch_bounds__(32 * kFW, KIC == kSmallGroup ? 8 : 5)
+__global__ void __launch_bounds__(32 * kFW, KIC == 4 ? 8 : KIC == 8 ? 6 : 5)
     ff_force_groups(FFDev D, const int* __restrict__ work, int n_work, long long* __restrict__ force, int stride) {
     __shared__ float4 stab[PT ? kMaxTypesDev * kMaxTypesDev : 1];
     __shared__ float4 sxi[kFW][KIC];           // group atoms: position, type or charge
@@ -662,12 +663,16 @@ int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* 
     if (cudaMemsetAsync(D.rebuild, 0, (size_t)D.S, st) != cudaSuccess) return -1;
     long long* f = const_cast<long long*>(B.force);
     const bool typed = D.ntypes > 0 && D.ntypes <= kMaxTypesDev;
-    if (D.n_small) {
-        launch_force_pass<kSmallGroup>(D, D.small_groups, D.n_small, energy, typed, f, B.stride, st);
+    if (D.n_pass[0]) {
+        launch_force_pass<kPassKIC[0]>(D, D.pass_groups[0], D.n_pass[0], energy, typed, f, B.stride, st);
         n++;
     }
-    if (D.n_large) {
-        launch_force_pass<kLargeChunk>(D, D.large_groups, D.n_large, energy, typed, f, B.stride, st);
+    if (D.n_pass[1]) {
+        launch_force_pass<kPassKIC[1]>(D, D.pass_groups[1], D.n_pass[1], energy, typed, f, B.stride, st);
+        n++;
+    }
+    if (D.n_pass[2]) {
+        launch_force_pass<kPassKIC[2]>(D, D.pass_groups[2], D.n_pass[2], energy, typed, f, B.stride, st);
         n++;
     }
     if (energy) {

@@ -157,13 +157,15 @@ struct FFDev {
     const int* mc_sys;
     const int* sc_sys;
     const int* sc_g0;
-    // groups of the force pass (set at creation): at most 4 interacting atoms, and the others
-    int n_small, n_large;
-    const int* small_groups;
-    const int* large_groups;
+    // groups of the force passes (set at creation, put in spatial order with the state), by size:
+    // at most 4, at most 8 and more than 8 interacting atoms (force_pass_of)
+    int n_pass[3];
+    const int* pass_groups[3];
 };
-// Groups of at most this many interacting atoms run in the force pass's small-group launch.
-constexpr int kSmallGroupAtoms = 4;
+// The force pass runs in three launches by group size: at most 4 interacting atoms (waters, free
+// atoms), at most 8 (tetrahedral bodies) and more (rings, larger bodies, in chunks of 12).
+constexpr int kForcePasses = 3;
+inline int force_pass_of(int atoms) { return atoms <= 4 ? 0 : atoms <= 8 ? 1 : 2; }
 // Interacting atoms of one system: the force pass streams (atom << 5 | lane) words.
 constexpr int kMaxSystemAtoms = 1 << 26;
 int launch_forces(const FFDev& D, int prec, const DevBuf& B, bool energy, void* stream);
