@@ -441,7 +441,8 @@ __device__ __forceinline__ void pair_terms(const float4* xs, const float4* ps, i
 
 // The pair terms of one streamed neighbour, with the group size and image form chosen (the same
 // choice for every lane): exact-size forms for the common sizes (1: a free atom; 3: a water; 5:
-// a tetrahedral body; 12: a ring or a full chunk of a larger body), the general one otherwise.
+// a tetrahedral body; 6: a ring's carbons; 12: a full chunk of a larger body), the general one
+// otherwise.
 template <int KIC, bool ENERGY, bool PT, bool RELAX, bool PI>
 __device__ __forceinline__ void pair_dispatch(const float4* xs, const float4* ps, int ni, const FFSys& S,
                                               const float4* ptab, float4 xj, float4 pj, bool valid,
@@ -451,6 +452,7 @@ __device__ __forceinline__ void pair_dispatch(const float4* xs, const float4* ps
         if (ni == 1) return pair_terms<KIC, 1, ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
     } else if (KIC == 8) {
         if (ni == 5) return pair_terms<KIC, (KIC >= 5 ? 5 : 0), ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
+        if (ni == 6) return pair_terms<KIC, (KIC >= 6 ? 6 : 0), ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
     } else {
         if (ni == KIC) return pair_terms<KIC, KIC, ENERGY, PT, RELAX, PI>(xs, ps, ni, S, ptab, xj, pj, valid, f, en);
     }
