@@ -755,18 +755,22 @@ def run_batched(args, world, rank, local):
     barrier(world)
     t0 = time.perf_counter()
     b.set_state(xh, vh)
+    t1 = time.perf_counter()
     for _ in range(nchunks):
         b.step(chunk, dt)
         b.energies()
+    t2 = time.perf_counter()
     xo, vo = b.get_state()
-    t_e2e = max_over_ranks(time.perf_counter() - t0, world)
+    t3 = time.perf_counter()
+    t_e2e = max_over_ranks(t3 - t0, world)
     e2e_steps = nchunks * chunk
     e2e = {"value": world * nb * e2e_steps / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": int(2 * 24 * na / e2e_steps),
            "d2h_bytes_per_step": int((2 * 24 * na + 24 * len(systems) * nchunks) / e2e_steps),
            "call": f"BatchedSystems.set_state (positions and velocities in), {nchunks} x (step({chunk}) + "
                    "energies()), get_state (positions and velocities out): rbx_batch_set_state, rbx_batch_step, "
-                   "rbx_batch_energies, rbx_batch_get_state; wall clock"}
+                   "rbx_batch_energies, rbx_batch_get_state; wall clock",
+           "seconds": {"set_state": t1 - t0, "steps_and_energies": t2 - t1, "get_state": t3 - t2}}
 
     # the same systems, one system per launch (the plain drop-in way: one context per system)
     plain = None

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <map>
 #include <new>
+#include <thread>
 #include <vector>
 
 #include "../../include/rbx.h"
@@ -38,6 +39,37 @@ float int_bits(int v) {
     float f;
     std::memcpy(&f, &v, sizeof f);
     return f;
+}
+
+// body(s) for every system s, the systems split into contiguous ranges of about equal group counts
+// over the host's cores. Each call writes only its own system's outputs, so the results do not
+// depend on the split; a thread that cannot be started leaves its range to the calling thread.
+template <class F> void for_each_system(const std::vector<FFSys>& sys, F&& body) {
+    const int S = (int)sys.size();
+    const long long groups = S ? (long long)sys[S - 1].g1 - sys[0].g0 : 0;
+    const int nt = (int)std::min<long long>({(long long)std::max(1u, std::thread::hardware_concurrency()), 32LL,
+                                             std::max(1LL, groups / 20000)});
+    std::vector<int> lo(nt + 1, S);
+    lo[0] = 0;
+    for (int t = 1, s = 0; t < nt; t++) {
+        while (s < S && (long long)(sys[s].g0 - sys[0].g0) * nt < groups * t) s++;
+        lo[t] = s;
+    }
+    auto run = [&](int t) {
+        for (int s = lo[t]; s < lo[t + 1]; s++) body(s);
+    };
+    std::vector<std::thread> pool;
+    std::vector<int> inline_ranges;
+    for (int t = 1; t < nt; t++) {
+        try {
+            pool.emplace_back(run, t);
+        } catch (...) {
+            inline_ranges.push_back(t);
+        }
+    }
+    run(0);
+    for (int t : inline_ranges) run(t);
+    for (std::thread& th : pool) th.join();
 }
 
 template <class T> int upload_vec(DevArray<T>& a, const std::vector<T>& h) {
@@ -123,10 +155,11 @@ int setup_lists(rbx_batch* b, const double* x) {
     const int S = b->S;
     std::vector<FFSys> sys = b->sys_h;
     std::vector<int> mc_cell, mc_sys, sc_sys, sc_g0;
-    std::vector<uint64_t> zkey(b->grp_n_h.size());  // spatial order of the groups (see below)
-    double cap_need = 1.0;
-    for (int s = 0; s < S; s++) {
-        FFSys& f = sys[s];
+    std::vector<uint32_t> zkey(b->grp_n_h.size());  // spatial order of each system's groups (see below)
+    std::vector<double> rho(S, 0.0);                // largest atom distance from a group centroid
+    // per system (in parallel): centroids, their Z-order codes and the largest radius
+    for_each_system(sys, [&](int s) {
+        const FFSys& f = sys[s];
         const double L = b->box_h[s];
         auto img = [L](double d) { return d - L * std::nearbyint(d / L); };
         double rho_max = 0.0;
@@ -138,14 +171,14 @@ int setup_lists(rbx_batch* b, const double* x) {
                 for (int d = 0; d < 3; d++) c[d] += img(x[3 * (size_t)b->iatom_h[k0 + a] + d] - x0[d]);
             for (int d = 0; d < 3; d++) c[d] = x0[d] + c[d] / n;
             // Z-order (Morton) code of the centroid on a 1024^3 grid of the box
-            uint64_t z = 0;
+            uint32_t z = 0;
             for (int d = 0; d < 3; d++) {
                 double u = c[d] / L;
                 u -= std::floor(u);
-                const uint64_t q = std::min<uint64_t>(1023, (uint64_t)(u * 1024.0));
-                for (int bit = 0; bit < 10; bit++) z |= ((q >> bit) & 1ull) << (3 * bit + d);
+                const uint32_t q = std::min<uint32_t>(1023, (uint32_t)(u * 1024.0));
+                for (int bit = 0; bit < 10; bit++) z |= ((q >> bit) & 1u) << (3 * bit + d);
             }
-            zkey[g] = ((uint64_t)s << 30) | z;
+            zkey[g] = z;
             for (int a = 0; a < n; a++) {
                 double r2 = 0.0;
                 for (int d = 0; d < 3; d++) {
@@ -155,6 +188,12 @@ int setup_lists(rbx_batch* b, const double* x) {
                 rho_max = std::max(rho_max, std::sqrt(r2));
             }
         }
+        rho[s] = rho_max;
+    });
+    double cap_need = 1.0;
+    for (int s = 0; s < S; s++) {
+        FFSys& f = sys[s];
+        const double L = b->box_h[s], rho_max = rho[s];
         // the device forms the radii in FP32: a margin of 1e-3 nm keeps its ones within the cells
         const double edge = (double)f.rl + 2.0 * rho_max + 1e-3;
         f.pair_image = std::sqrt((double)f.rc2) + 2.0 * rho_max + 1e-3 >= 0.5 * L ? 1 : 0;
@@ -182,20 +221,36 @@ int setup_lists(rbx_batch* b, const double* x) {
     const size_t entries = (size_t)std::max(b->ff.n_groups, 1) * (size_t)cap;
     if (b->d_nbr.n < entries && b->d_nbr.alloc(entries) != cudaSuccess)
         return set_error(RBX_ERR_CUDA, "cudaMalloc of the neighbour lists failed (%d entries per group)", cap);
-    // The force pass takes its groups in this order: a system's groups in Z-order of their
-    // centroids, so that the warps resident on an SM at once work on neighbouring groups and find
-    // much of each other's neighbours in L1. The order schedules work only: every group's forces
-    // are formed alike whichever warp forms them.
+    // The force pass takes its groups in this order: system by system, each system's groups in
+    // Z-order of their centroids (ties by index), so that the warps resident on an SM at once work
+    // on neighbouring groups and find much of each other's neighbours in L1. The order schedules
+    // work only: every group's forces are formed alike whichever warp forms them. Each system's
+    // share of a pass is filled and sorted in place, the systems in parallel.
     {
         std::vector<int> pass[kForcePasses];
-        for (int g = 0; g < (int)zkey.size(); g++) pass[force_pass_of(b->grp_n_h[g])].push_back(g);
-        auto by_key = [&](int u, int v) { return zkey[u] < zkey[v] || (zkey[u] == zkey[v] && u < v); };
+        std::vector<size_t> at((size_t)kForcePasses * (S + 1), 0);  // at[k * (S + 1) + s]: system s's start in pass k
+        for (int s = 0; s < S; s++)
+            for (int g = sys[s].g0; g < sys[s].g1; g++) at[(size_t)force_pass_of(b->grp_n_h[g]) * (S + 1) + s + 1]++;
         for (int k = 0; k < kForcePasses; k++) {
-            std::sort(pass[k].begin(), pass[k].end(), by_key);
+            size_t* a = &at[(size_t)k * (S + 1)];
+            for (int s = 0; s < S; s++) a[s + 1] += a[s];
+            pass[k].resize(a[S]);
+        }
+        for_each_system(sys, [&](int s) {
+            size_t fill[kForcePasses];
+            for (int k = 0; k < kForcePasses; k++) fill[k] = at[(size_t)k * (S + 1) + s];
+            for (int g = sys[s].g0; g < sys[s].g1; g++) {
+                const int k = force_pass_of(b->grp_n_h[g]);
+                pass[k][fill[k]++] = g;
+            }
+            auto by_key = [&](int u, int v) { return zkey[u] < zkey[v] || (zkey[u] == zkey[v] && u < v); };
+            for (int k = 0; k < kForcePasses; k++)
+                std::sort(pass[k].begin() + at[(size_t)k * (S + 1) + s], pass[k].begin() + fill[k], by_key);
+        });
+        for (int k = 0; k < kForcePasses; k++)
             if (!pass[k].empty())
                 BATCH_TRY(cudaMemcpy(b->d_pass_groups[k].p, pass[k].data(), sizeof(int) * pass[k].size(),
                                      cudaMemcpyHostToDevice));
-        }
     }
     BATCH_TRY(cudaMemcpy(b->d_sys.p, sys.data(), sizeof(FFSys) * (size_t)S, cudaMemcpyHostToDevice));
     if (!mc_cell.empty()) {
