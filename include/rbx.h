@@ -338,7 +338,11 @@ int rbx_last_launch_count(const rbx_integrator* h);
  *   eps_solvent   reaction-field dielectric (OpenMM's default is 78.3)
  * Atoms live in device slots equal to their index in these arrays.
  * rbx_batch_step runs nsteps velocity-Verlet steps of size dt on every system: forces at the
- * current positions, part1, then (forces, fused part2+part1) x (nsteps-1), forces, part2. With
+ * current positions, part1, then (forces, fused part2+part1) x (nsteps-1), forces, part2. The
+ * forces at the starting positions are those the previous rbx_batch_step ended with when no other
+ * call has changed the state since (one force evaluation per step, as the reference's execute
+ * keeps the last step's forces, CudaRigidBodyKernels.cpp:421-426); otherwise the call forms them
+ * first. With
  * rbx_batch_set_graph_steps(k > 0), runs of k (forces, fused) pairs replay one captured CUDA graph
  * (captured on first use for a given dt; invalidated by rbx_batch_set_state).
  * rbx_batch_energies returns [U, KE_t, KE_r] per system (kJ/mol) at the current state
@@ -348,8 +352,10 @@ int rbx_last_launch_count(const rbx_integrator* h);
  * Forces come from neighbour lists of atom groups (each rigid body is one group, each free atom a
  * group of its own): two groups are listed together when their centroids lie within cutoff + a
  * skin of 0.06 nm + both groups' radii. Each system rebuilds its lists when one of its centroids has
- * moved half the skin, and every call rebuilds them at its first evaluation: a system's results are
- * a function of its own state and of the lengths of the calls that step it.
+ * moved half the skin, and every list is rebuilt for the state a step call ends in (and for the
+ * first evaluation after rbx_batch_set_state or rbx_batch_restore), so the forces and energy at a
+ * call's start and end depend on the positions alone: a system's results are a function of its own
+ * state and of the lengths of the calls that step it.
  */
 typedef struct rbx_batch rbx_batch;
 /* rbx_batch_set_state builds every body from the given positions and velocities (as

@@ -137,6 +137,8 @@ class BatchedSystems:
                                                _d(v)))
 
     def step(self, nsteps, dt, stream=None):
+        """nsteps velocity-Verlet steps of every system; a call that follows another step call
+        starts from the forces that call ended with (one force evaluation per step)."""
         _lib.check(self._lib.rbx_batch_step(self._h, _stream(stream), int(nsteps), float(dt)))
 
     def energies(self, stream=None):

@@ -110,6 +110,9 @@ struct rbx_batch {
     double* h_out = nullptr;  // pinned [3*S]
     int last_launches = 0;
     bool u_valid = false;  // d_energy holds the potential energy of the current positions
+    // the force buffer holds the forces of the current positions, formed (with their energy) from
+    // lists built at those positions: a step call then starts without a force evaluation
+    bool f_valid = false;
     // captured runs of (forces, fused step)
     // optional event timing of the force and integrator launch groups (direct launches only)
     bool timing = false;
@@ -305,9 +308,10 @@ struct Timed {
     }
 };
 
-// Every call that evaluates forces starts from freshly built neighbour lists, so that its results
-// depend only on the state it starts from (not on when earlier calls last rebuilt); later
-// evaluations in the call rebuild a system's lists when its atoms have moved half the skin.
+// Marks every system's lists for a rebuild at the next evaluation. Forces and energies at the state a
+// call starts or ends in are formed from lists built at that state, so they are a function of the
+// positions alone (not of when earlier calls last rebuilt); the evaluations in between rebuild a
+// system's lists when its atoms have moved half the skin.
 int force_rebuild(rbx_batch* b, void* stream) {
     BATCH_TRY(cudaMemsetAsync(b->d_rebuild.p, 1, (size_t)b->S, (cudaStream_t)stream));
     return RBX_OK;
@@ -618,6 +622,7 @@ int rbx_batch_destroy(rbx_batch* b) {
 int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, const double* velocities) {
     int rc = check(b);
     if (rc) return rc;
+    b->u_valid = b->f_valid = false;
     b->drop_graph();
     if (!positions || !velocities) return set_error(RBX_ERR_INVALID_ARGUMENT, "null positions or velocities");
     BATCH_TRY(cudaSetDevice(b->device));
@@ -638,7 +643,6 @@ int rbx_batch_set_state(rbx_batch* b, void* stream, const double* positions, con
     b->body0_h = body0;
     b->free0_h = free0;
     BATCH_TRY(cudaMemsetAsync(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)b->S, (cudaStream_t)stream));
-    b->u_valid = false;
     return RBX_OK;
 }
 
@@ -667,11 +671,11 @@ int rbx_batch_restore(rbx_batch* b, void* stream, const void* body_rows, const d
     int rc = check(b);
     if (rc) return rc;
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no geometry: call rbx_batch_set_state with the systems first");
+    b->u_valid = b->f_valid = false;
     if ((rc = rbx_context_load(b->integ, stream, positions, velocities))) return rc;
     if ((rc = rbx_set_body_state_raw(b->integ, body_rows))) return rc;
     if ((rc = rbx_context_sync_bodies(b->integ, stream))) return rc;
     BATCH_TRY(cudaMemsetAsync(b->d_sys_status.p, 0, sizeof(unsigned int) * (size_t)b->S, (cudaStream_t)stream));
-    b->u_valid = false;
     return RBX_OK;
 }
 
@@ -683,7 +687,13 @@ int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {
     if (!b->d_body0.p) return set_error(RBX_ERR_STATE, "no state: call rbx_batch_set_state first");
     BATCH_TRY(cudaSetDevice(b->device));
     b->last_launches = 0;
-    if ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, false))) return rc;
+    // forces at the starting positions: those the previous step call ended with while nothing has
+    // changed the state since (formed, as an evaluation here would form them, from lists built at
+    // these positions with the energy variant), else one evaluation. The reference likewise keeps
+    // the forces of the last step for the next one (CudaRigidBodyKernels.cpp:421-426).
+    if (!b->f_valid && ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, true)))) return rc;
+    b->f_valid = false;
+    b->u_valid = false;
     if ((rc = integrate(b, stream, STEP_PART1, dt))) return rc;
     int remaining = nsteps - 1;
     if (b->graph_k > 0 && !b->timing && remaining >= b->graph_k) {
@@ -699,11 +709,12 @@ int rbx_batch_step(rbx_batch* b, void* stream, int nsteps, double dt) {
     for (; remaining > 0; remaining--) {
         if ((rc = forces(b, stream, false)) || (rc = fused(b, stream, dt))) return rc;
     }
-    // the last evaluation also forms the potential energy of the state the call ends in
-    b->u_valid = false;
-    if ((rc = forces(b, stream, true))) return rc;
+    // the last evaluation builds every list at the final positions and also forms their potential
+    // energy
+    if ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, true))) return rc;
     if ((rc = integrate(b, stream, STEP_PART2, dt))) return rc;
     b->u_valid = true;
+    b->f_valid = true;
     return RBX_OK;
 }
 
@@ -721,6 +732,7 @@ int rbx_batch_relax(rbx_batch* b, void* stream, int nsteps, double dt, double ma
     const DevSys sys = device_system(b->integ);
     b->ff.fcap = (float)max_force;
     b->u_valid = false;
+    b->f_valid = false;
     if ((rc = force_rebuild(b, stream))) return rc;
     for (int n = 0; n < nsteps && !rc; n++) {
         rc = forces(b, stream, false);
@@ -746,6 +758,7 @@ int rbx_batch_energies(rbx_batch* b, void* stream, double* out) {
     // in that call's last force evaluation); otherwise a force evaluation that forms it
     if (!b->u_valid && ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, true)))) return rc;
     b->u_valid = true;
+    b->f_valid = true;
     if (launch_kinetic_systems(b->prec, device_system(b->integ), buffers(b), b->d_body0.p, b->d_free0.p, b->S,
                                b->d_ke.p, stream) < 0)
         return set_error(RBX_ERR_CUDA, "kinetic-energy kernel failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -769,6 +782,8 @@ int rbx_batch_forces(rbx_batch* b, void* stream, double* forces_out, double* ene
     BATCH_TRY(cudaSetDevice(b->device));
     b->last_launches = 0;
     if ((rc = force_rebuild(b, stream)) || (rc = forces(b, stream, true))) return rc;
+    b->u_valid = true;
+    b->f_valid = true;
     cudaStream_t st = (cudaStream_t)stream;
     const DevBuf d = buffers(b);
     if (forces_out) {

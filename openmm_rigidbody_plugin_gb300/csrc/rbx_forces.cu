@@ -10,9 +10,9 @@
 // atom) form a group, and a group's list holds every group whose centroid lies within cutoff +
 // skin (0.06 nm) + both groups' radii. A rigid group's atoms stay within its radius of its centroid
 // however the body turns, so a list ages only as the centroids move: each system rebuilds its
-// lists when one of its centroids has moved half the skin since its last build, and at the first
-// evaluation of every call (so a call's results depend only on the positions it starts from, never
-// on when earlier calls rebuilt). One evaluation, all systems at once:
+// lists when one of its centroids has moved half the skin since its last build, and every list is
+// rebuilt for the state a call starts or ends in (so the forces there depend only on the
+// positions, never on when earlier calls rebuilt). One evaluation, all systems at once:
 //   1. ff_gcheck   one thread per group: its atoms' positions (wrapped into the box, with their
 //                  type) in list order, its centroid and radius, and the centroid's displacement
 //                  since the last build (flags the system's rebuild)

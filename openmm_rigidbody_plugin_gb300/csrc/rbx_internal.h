@@ -130,7 +130,8 @@ struct FFDev {
     float4* cpos;         // [n_int] x, y, z (wrapped into the box), sqrt(K) q (or the atom's type)
     double* e_group;      // [n_groups] half pair-energy sums of each group (energy evaluations)
     // Neighbour lists of groups, rebuilt per system when one of its centroids has moved more than
-    // half the skin since the last build, and at the first evaluation of every call
+    // half the skin since the last build, and for every system at the last evaluation of every
+    // step call and at the first evaluation after a state is set
     unsigned char* rebuild;  // [S] 1: rebuild this system's lists before the next force pass
     unsigned int* rebuilds;  // [S] list builds of each system so far (a statistic)
     unsigned int* nbr;       // entries: listed group - g0 of the system; entry e of group g at

@@ -15,9 +15,10 @@ charged at the largest bytes per atom measured so far (from a probe batch at sta
 every group created). The budget is the smaller of the given one and the device's free memory at
 start-up less a reserve.
 
-A request's trajectory does not depend on its company: each step call starts from freshly built
-neighbour lists and every system is integrated independently, so run alone with the same chunk
-lengths it is bit for bit the same (``serve_alone``).
+A request's trajectory does not depend on its company: the forces a step call starts from are
+formed from neighbour lists built at its starting positions (by the previous call, or after a move
+between groups by the call itself), and every system is integrated independently, so run alone
+with the same chunk lengths it is bit for bit the same (``serve_alone``).
 
 A request whose system fails (a non-finite state after a step, or forces beyond the fixed-point
 range) is stopped at the end of that chunk and completed with ``failed`` set and no result; the

@@ -120,6 +120,29 @@ def test_graph_replay_equals_direct_launches(B):
     assert graphed.last_launch_count == direct.last_launch_count
 
 
+def test_step_calls_keep_the_last_forces(B):
+    """A step call that follows another starts from the forces that call ended with (one force
+    evaluation per step); after a restore it forms them itself, from lists built at the same
+    positions by the same kernels, so both runs stay equal bit for bit."""
+    from openmm_rigidbody_plugin_gb300 import workloads as W
+    systems = W.batch_systems(4, lo=64, hi=600, seed=21)
+    a = B.BatchedSystems.from_systems(systems, relax_steps=60)
+    b = B.BatchedSystems.from_systems(systems, relax_steps=60)
+    for h in (a, b):
+        h.step(10, 0.002)
+    first = a.last_launch_count
+    ck = b.checkpoint()
+    b.restore(ck)
+    a.step(10, 0.002)
+    kept = a.last_launch_count
+    b.step(10, 0.002)
+    formed = b.last_launch_count
+    assert kept < formed == first
+    for u, w in zip(a.get_state(), b.get_state()):
+        assert np.array_equal(u, w)
+    assert np.array_equal(a.energies(), b.energies())
+
+
 def test_degrees_of_freedom_per_system(B):
     from openmm_rigidbody_plugin_gb300 import workloads as W
     systems = [W.mixed_system(n_bodies=200, n_free=13, seed=3), W.water_box(27, seed=2)]
