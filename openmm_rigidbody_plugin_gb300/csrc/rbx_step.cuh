@@ -32,6 +32,7 @@
 #include "rbx_fast.cuh"
 #include "rbx_internal.h"
 #include "rbx_math.cuh"
+#include "rbx_tiles.h"
 
 namespace rbx {
 
@@ -304,21 +305,9 @@ __device__ __forceinline__ void free_atom_tile(const DevSys& S, const DevBuf& B,
     if (!finite_d((double)(v.x + v.y + v.z))) flag_failure(S.status, S.free_bad, j);
 }
 
-// Tile of this block: the body tile (>= 0) or -1 - the free-atom tile. Free-atom tiles are spread
-// over the grid in proportion rather than placed after the body tiles, where their FP64 velocity
-// arithmetic (then used in mixed precision) queued on GB300's narrow FP64 pipe as a tail at the end
-// of the grid: 100,000 free atoms cost 15 us of a 0.144 ms step, for 2 % of its bytes. Interleaved,
-// that work overlaps the body tiles' memory traffic (0.1437 -> 0.1383 ms). Block i is a free-atom
-// tile when c(i) = floor((i + 1) nf / T) (T = body + free-atom tiles) steps up there, so free-atom
-// tile j runs right after the body tiles that cover the same span of slots (both are in slot
-// order); c never steps by more than one, which makes the mapping a bijection onto [0, body tiles)
-// and [0, free-atom tiles).
+// Tile of this block (rbx_tiles.h): the body tile (>= 0) or -1 - the free-atom tile.
 __device__ __forceinline__ int block_tile(const DevSys& S) {
-    const int i = (int)blockIdx.x, nf = S.n_free_tiles;
-    if (nf == 0) return i;
-    const long long T = (long long)S.n_body_tiles + nf;
-    const int c = (int)(((long long)i + 1) * nf / T), c0 = (int)((long long)i * nf / T);
-    return c > c0 ? -c : i - c;
+    return tile_of_block((int)blockIdx.x, S.n_body_tiles, S.n_free_tiles);
 }
 
 // Shared-memory carve-up common to both step kernels.
