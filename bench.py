@@ -5,8 +5,10 @@ counts log-uniform in [64, 4096] (70 % 3-site waters, 20 % 5-atom tetrahedra, 10
 rings), each in its own periodic box at 1 g/cm^3, cutoff LJ + reaction-field forces from the
 library's neighbour-list kernel, 300 K, dt 2 fs, rotation mode 0, mixed precision. One step is one full
 velocity-Verlet step of every system (forces, then the integrator), all systems in one launch per
-kernel, runs of steps replayed from captured CUDA graphs. The working set (about 1 GB) exceeds the
-129 MB L2, so no flush is needed between steps.
+kernel, runs of steps replayed from captured CUDA graphs. The working set (2.2 GB of integrator
+traffic per step, the neighbour lists besides) exceeds the 129 MB L2, so no flush is needed between
+steps. Consecutive step calls take one force evaluation per step (a call starts from the forces the
+previous one ended with).
 
   value   body-steps/s = bodies x steps / device time of exactly --steps steps (CUDA events on the
           launching stream, max over ranks), inputs resident in HBM
@@ -15,7 +17,7 @@ kernel, runs of steps replayed from captured CUDA graphs. The working set (about
           whether the final states and energies of the two arms are bit-equal
   e2e     the same metric through the public API with host buffers: positions and velocities in
           (set_state), the steps in chunks of 10 with the energies read back after each, positions
-          and velocities out
+          and velocities out (wall clock; `seconds` splits it into the three parts)
   roofline  the integrator launches of the batched step (algorithmic bytes / event-timed launch
           time) against the measured HBM peak; the force kernels' share of the step beside it
   single_system  the single-large-system integrator step (1,000,000 bodies + 100,000 free atoms,
