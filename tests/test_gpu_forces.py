@@ -140,7 +140,10 @@ def test_step_calls_keep_the_last_forces(B):
     assert kept < formed == first
     for u, w in zip(a.get_state(), b.get_state()):
         assert np.array_equal(u, w)
-    assert np.array_equal(a.energies(), b.energies())
+    e_kept = a.energies()  # formed by the step's last evaluation
+    assert np.array_equal(e_kept, b.energies())
+    a.restore(a.checkpoint())
+    assert np.array_equal(a.energies(), e_kept)  # formed afresh at the same state
 
 
 def test_degrees_of_freedom_per_system(B):
