@@ -88,6 +88,7 @@ struct rbx_batch {
     DevArray<FFSys> d_sys;
     DevArray<int> d_iatom, d_isys, d_cell_of, d_cell_count, d_cell_start, d_cell_cursor, d_cell_list;
     DevArray<int> d_grp_k0, d_grp_n, d_gsys, d_kgrp;
+    DevArray<int2> d_grp_kn;
     DevArray<int> d_mc_cell, d_mc_sys, d_sc_sys, d_sc_g0;
     DevArray<int> d_pass_groups[kForcePasses];  // FFDev::pass_groups
     DevArray<float4> d_param, d_cpos, d_gcen, d_gref, d_gq, d_types;
@@ -497,6 +498,11 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     if (!rc) rc = upload_vec(b->d_param, param);
     if (!rc) rc = upload_vec(b->d_grp_k0, grp_k0);
     if (!rc) rc = upload_vec(b->d_grp_n, grp_n);
+    {
+        std::vector<int2> kn(grp_k0.size());
+        for (size_t g = 0; g < kn.size(); g++) kn[g] = make_int2(grp_k0[g], grp_n[g]);
+        if (!rc) rc = upload_vec(b->d_grp_kn, kn);
+    }
     if (!rc) rc = upload_vec(b->d_gsys, gsys);
     if (!rc) rc = upload_vec(b->d_kgrp, kgrp);
     std::vector<int> pass_groups[kForcePasses];  // the force passes' groups, by size
@@ -573,6 +579,7 @@ int rbx_batch_create(rbx_batch** out, int num_systems, const int* atom_offsets, 
     D.param = b->d_param.p;
     D.grp_k0 = b->d_grp_k0.p;
     D.grp_n = b->d_grp_n.p;
+    D.grp_kn = b->d_grp_kn.p;
     D.gsys = b->d_gsys.p;
     D.kgrp = b->d_kgrp.p;
     D.gcen = b->d_gcen.p;
@@ -821,7 +828,7 @@ int rbx_batch_memory(const rbx_batch* b, size_t* bytes) {
     if (!bytes) return set_error(RBX_ERR_INVALID_ARGUMENT, "null output");
     size_t n = b->d_sys.bytes() + b->d_iatom.bytes() + b->d_isys.bytes() + b->d_cell_of.bytes() +
                b->d_cell_count.bytes() + b->d_cell_start.bytes() + b->d_cell_cursor.bytes() + b->d_cell_list.bytes() +
-               b->d_grp_k0.bytes() + b->d_grp_n.bytes() + b->d_gsys.bytes() + b->d_kgrp.bytes() +
+               b->d_grp_k0.bytes() + b->d_grp_n.bytes() + b->d_grp_kn.bytes() + b->d_gsys.bytes() + b->d_kgrp.bytes() +
                b->d_mc_cell.bytes() + b->d_mc_sys.bytes() + b->d_sc_sys.bytes() + b->d_sc_g0.bytes() +
                b->d_pass_groups[0].bytes() + b->d_pass_groups[1].bytes() + b->d_pass_groups[2].bytes() +
                b->d_param.bytes() + b->d_cpos.bytes() + b->d_gcen.bytes() + b->d_gref.bytes() + b->d_gq.bytes() +

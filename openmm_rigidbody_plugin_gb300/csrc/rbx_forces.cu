@@ -512,7 +512,8 @@ __global__ void __launch_bounds__(32 * kFW, KIC == 4 ? 8 : KIC == 8 ? 6 : 5)
             if (e0 + lane < n) {
                 const int gj = S.g0 + (int)nb[e0 + lane];
                 const float4 cj = D.gcen[gj];
-                const int njg = D.grp_n[gj], j0g = D.grp_k0[gj];
+                const int2 kn = D.grp_kn[gj];
+                const int njg = kn.y, j0g = kn.x;
                 const float dx = cj.x - c.x, dy = cj.y - c.y, dz = cj.z - c.z;
                 shift = make_float4(-S.L * rintf(dx * S.invL), -S.L * rintf(dy * S.invL), -S.L * rintf(dz * S.invL), 0.f);
                 const float ex = dx + shift.x, ey = dy + shift.y, ez = dz + shift.z;
@@ -533,8 +534,16 @@ __global__ void __launch_bounds__(32 * kFW, KIC == 4 ? 8 : KIC == 8 ? 6 : 5)
             const int total = __shfl_sync(kAll, incl, 31), excl = incl - nj;
             for (int base = 0; base < total; base += kQ) {
                 __syncwarp();
-                const int hi = min(incl, base + kQ);
-                for (int t = max(excl, base); t < hi; t++) queue[t - base] = ((j0 + t - excl) << 5) | lane;
+                const int hi = min(incl, base + kQ), lo = max(excl, base);
+                // a lane's atoms into the queue: unrolled for up to 6 (every group of the
+                // benchmark mix), a loop beyond
+                if (hi - lo <= 6) {
+#pragma unroll
+                    for (int u = 0; u < 6; u++)
+                        if (lo + u < hi) queue[lo + u - base] = ((j0 + lo + u - excl) << 5) | lane;
+                } else {
+                    for (int t = lo; t < hi; t++) queue[t - base] = ((j0 + t - excl) << 5) | lane;
+                }
                 __syncwarp();
                 const int cnt = min(kQ, total - base);
                 bool valid = lane < cnt;

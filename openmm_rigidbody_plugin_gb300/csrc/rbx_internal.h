@@ -117,6 +117,7 @@ struct FFDev {
     const float4* param;  // [n_int] sqrt(K) q, sigma/2, sqrt(epsilon), body id (int bits; 0 = free)
     const int* grp_k0;    // [n_groups] first interacting atom of each group
     const int* grp_n;     // [n_groups] its atoms
+    const int2* grp_kn;   // [n_groups] (grp_k0, grp_n) together: one load per listed group
     const int* gsys;      // [n_groups] its system
     const int* kgrp;      // [n_int] group of each interacting atom
     float4* gcen;         // [n_groups] centroid (wrapped into the box) and radius, every evaluation
